@@ -1,0 +1,315 @@
+#!/usr/bin/env python3
+"""Benchmark of the brute-force squared-L2 kNN hot path on GB300.
+
+Default workload (one GB300): corpus 1,000,000 x 128 float32 holding integers
+clip(round(|N(0,40)|),0,255) with 8% of each row's coordinates zeroed,
+10,000 queries from the same generator, k = 100, seed 1.  A step is one
+search of the whole query batch against the whole corpus.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload int1m|uniform64k]
+
+Prints one JSON line (rank 0).  `value` is queries/s with the corpus and the
+queries resident in HBM; `e2e` is the same metric through the drop-in C ABI
+(gpuknnsBitonic) from pinned host buffers, host<->device copies included.
+`--impl reference` times the reference's CPU path (demo/knn.m, restated in C
+in oracle/knn_oracle.c) on the host cores on a bounded query sample.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "knn-toolbox_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+WORKLOADS = {
+    "int1m": dict(desc="int-descriptor corpus 1,000,000 x 128 (clip(round(|N(0,40)|),0,255), 8% of coords "
+                       "zeroed), 10,000 queries, k=100, seed 1",
+                  gen="int_descriptor", N=1_000_000, D=128, Q=10_000, k=100, seed=1),
+    "uniform64k": dict(desc="uniform [0,1) corpus 65,536 x 128, 1,024 queries, k=16, seed 0",
+                       gen="uniform", N=65_536, D=128, Q=1_024, k=16, seed=0),
+}
+METRIC = "queries/s (exact squared-L2 kNN, plain FP32 form)"
+
+
+def gen_data(w, rank=0):
+    import cuknns.synth as S
+    fn = getattr(S, w["gen"])
+    corpus, queries = fn(w["N"], w["D"], seed=w["seed"], nq=w["Q"])
+    if rank:
+        _, queries = fn(w["Q"], w["D"], seed=w["seed"] + 1000 * rank, nq=w["Q"])
+    return corpus, queries
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def profiled_traffic(kernel, workload):
+    """traffic_bytes_per_launch from a committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        rows = []
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), f[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[j] for _, _, r in rows for j, v in enumerate(r) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(corpus, queries, k, budget_s=12.0):
+    """demo/knn.m restated in C (oracle), all host threads, on a bounded query sample."""
+    import oracle
+    oracle.build()
+    threads = oracle.max_threads()
+    n = max(1, threads)
+    t0 = time.perf_counter()
+    oracle.knn_gemm(corpus, queries[:n], k, nthreads=threads)
+    t1 = time.perf_counter() - t0
+    m = int(min(len(queries), max(n, n * int(budget_s / max(t1, 1e-3)))))
+    t0 = time.perf_counter()
+    oracle.knn_gemm(corpus, queries[:m], k, nthreads=threads)
+    el = time.perf_counter() - t0
+    return {"value": m / el, "unit": "queries/s", "cores": threads, "kind": "port",
+            "sample": f"first {m} of {len(queries)} queries against the full corpus, "
+                      f"{el:.1f} s on {threads} host threads (demo/knn.m restated in C, oracle/knn_oracle.c)"}
+
+
+def run_reference(args, w):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import oracle
+    oracle.build()
+    corpus, queries = gen_data(w)
+    threads = oracle.max_threads()
+    k = w["k"]
+    # size each step so that warm-up + timed steps end within a few minutes
+    t0 = time.perf_counter()
+    oracle.knn_gemm(corpus, queries[:threads], k, nthreads=threads)
+    per_q = (time.perf_counter() - t0) / threads
+    budget = 150.0 / max(1, args.steps + args.warmup)
+    m = int(max(1, min(len(queries), budget / max(per_q, 1e-6))))
+    for s in range(args.warmup):
+        oracle.knn_gemm(corpus, queries[:m], k, nthreads=threads)
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        lo = (s * m) % max(1, len(queries) - m + 1)
+        oracle.knn_gemm(corpus, queries[lo:lo + m], k, nthreads=threads)
+    el = time.perf_counter() - t0
+    value = m * args.steps / el
+    sample = (f"{m} queries per step against the full {w['N']} x {w['D']} corpus, "
+              f"{threads} host threads, demo/knn.m restated in C (oracle/knn_oracle.c)")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "queries/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": w["desc"], "N": w["N"], "Q": w["Q"], "D": w["D"], "k": w["k"],
+                       "queries_per_step": m},
+            "cpu_baseline": {"value": value, "unit": "queries/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args, w):
+    import torch
+    import cuknns
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    corpus_np, queries_np = gen_data(w, rank)
+    N, D, Q, k = w["N"], w["D"], w["Q"], w["k"]
+    c = torch.from_numpy(corpus_np).to(dev)
+    q = torch.from_numpy(queries_np).to(dev)
+    dist_out = torch.empty((Q, k), dtype=torch.float32, device=dev)
+    idx_out = torch.empty((Q, k), dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step(timing=False):
+        cuknns.search(c, q, k, dist=dist_out, idx=idx_out, stream=stream, check=False, timing=timing)
+
+    for _ in range(args.warmup):
+        step()
+    cuknns.lib().knns_check_device(None)
+    st = cuknns.last_stats()
+    cuknns.timing_collect()  # drop anything recorded so far
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step(timing=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    el_ms = e0.elapsed_time(e1)
+    prep_ms, fused_ms, select_ms, nt = cuknns.timing_collect()
+    rc = cuknns.lib().knns_check_device(None)
+    if rc != 0:
+        raise RuntimeError(cuknns.last_error())
+    if dist is not None:
+        t = torch.tensor([el_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        el_ms = float(t.item())
+    value = Q * args.steps * world / (el_ms / 1e3)
+
+    # ---- end to end through the drop-in C ABI from pinned host buffers
+    e2e_steps = max(1, min(args.steps, 20))
+    hc = torch.from_numpy(corpus_np).pin_memory().numpy()
+    hq = torch.from_numpy(queries_np).pin_memory().numpy()
+    cuknns.gpuknnsBitonic(hq, hc, k, 1)  # warm (staging buffers)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        vals, idxf, secs = cuknns.gpuknnsBitonic(hq, hc, k, 1)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    if dist is not None:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": Q * world / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": int(hc.nbytes + hq.nbytes),
+           "d2h_bytes_per_step": int(vals.nbytes + idxf.nbytes), "api": "gpuknnsBitonic (include/cuknns.h)",
+           "host_buffers": "pinned inputs, pageable outputs", "steps": e2e_steps}
+
+    # ---- roofline of the dominant kernel (fused distance + shortlist)
+    peaks, peak_kind = measured_peaks()
+    fused_avg_ms = fused_ms / max(1, nt)
+    kern = "tc_kernel" if st["algo"] == cuknns.ALGO_TC else "simt_kernel"
+    if st["algo"] == cuknns.ALGO_TC:
+        flops = 3.0 * 2.0 * N * Q * D       # three TF32 products per useful product
+        peak = peaks["bf16_tflops"] / 2.0    # dense TF32 runs at half the BF16 rate
+        roof = {"bound": "tensor", "achieved": flops / (fused_avg_ms / 1e3) / 1e12, "peak": peak,
+                "unit": "TFLOP/s",
+                "peak_source": f"{peak_kind} bf16 dense burst / 2 (TF32 dense rate)"}
+    else:
+        flops = 2.0 * N * Q * D
+        peak = 152 * 128 * 2 * 2.07e9 / 1e12
+        roof = {"bound": "fp32-simt", "achieved": flops / (fused_avg_ms / 1e3) / 1e12, "peak": peak,
+                "unit": "TFLOP/s", "peak_source": "nominal FP32 FMA rate at max SM clock"}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    tr = profiled_traffic(kern, args.workload)
+    roof["traffic"] = tr
+    roof["kernel"] = kern
+    roof["kernel_ms"] = fused_avg_ms
+    roof["effective_fp32_tflops"] = 2.0 * N * Q * D / (fused_avg_ms / 1e3) / 1e12
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+    cpu = cpu_baseline(corpus_np, queries_np, k) if world == 1 and not args.no_cpu_baseline else None
+    line = {"metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": w["desc"], "N": N, "Q": Q, "D": D, "k": k,
+                       "parallelism": f"replicas x{world} (queries sharded, corpus replicated)",
+                       "l2": "inputs larger than L2 (512 MB corpus + 1 GB TF32 hi/lo copies)" if N * D * 4 > 129e6
+                       else "working set within L2 (65,536 x 128 corpus)",
+                       "algo": {1: "tcgen05 3xTF32", 2: "CUDA-core FP32"}[st["algo"]], "splits": st["splits"],
+                       "shortlist": st["kp"], "stages": st["stages"]},
+            "stage_ms": {"prep": prep_ms / max(1, nt), "fused": fused_avg_ms, "select": select_ms / max(1, nt)},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": st["launches"] * args.steps,
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="int1m", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, w)
+    return run_gb300(args, w)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

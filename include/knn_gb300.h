@@ -1,0 +1,116 @@
+/*
+ * knn_gb300.h -- status-returning C API of the GB300 brute-force kNN engine.
+ *
+ * The reference (shengren/knn-toolbox) has no error channel: its entry points
+ * return void or an elapsed time (include/cuknns.h:75,83,85,87) and never
+ * check a CUDA or cuBLAS status.  This header is the engine's native
+ * interface; include/cuknns.h keeps the reference's own names and signatures
+ * on top of it for drop-in use.
+ *
+ * Layout conventions (identical to the reference's, readme.txt:61-69):
+ *   corpus   N x D, each vector contiguous ("D is the leading dimension"),
+ *   queries  Q x D, each vector contiguous,
+ *   outputs  Q x k, each query's k results contiguous ("k is the leading
+ *            dimension"), sorted ascending by (distance, index), 0-based.
+ * Distances are squared L2.  All sizes are element counts.
+ */
+#ifndef KNN_GB300_H
+#define KNN_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define KNNS_OK 0
+#define KNNS_ERR_INVALID 1        /* bad argument (sizes, pointers, k > N, ...) */
+#define KNNS_ERR_CUDA 2           /* a CUDA runtime call failed */
+#define KNNS_ERR_UNSUPPORTED 3    /* shape outside what the kernels handle */
+#define KNNS_ERR_DEVICE_TIMEOUT 4 /* a kernel gave up a bounded wait and wound down */
+#define KNNS_ERR_NOMEM 5          /* device or host allocation failed */
+
+/* kernel families */
+#define KNNS_ALGO_AUTO 0 /* tensor cores when the shape allows, else CUDA cores */
+#define KNNS_ALGO_TC 1   /* tcgen05 3xTF32 fused distance + shortlist (D <= 128, shortlist <= 128) */
+#define KNNS_ALGO_SIMT 2 /* CUDA-core FP32 fused distance + shortlist (any D, shortlist <= 512) */
+
+typedef struct knns_options {
+    int algo;        /* KNNS_ALGO_* */
+    int splits;      /* corpus splits processed by independent CTAs; 0 = automatic */
+    int rerank;      /* 1 (default): shortlist re-ranked by the exact direct-difference distance;
+                        0: reference semantics, rank by ||c||^2 - 2 q.c, distance = key + ||q||^2 */
+    int kp;          /* shortlist length per query (multiple of 32, >= k); 0 = automatic */
+    int timing;      /* 1: record CUDA events around each stage (see knns_timing_collect) */
+    int reserved[3];
+} knns_options;
+
+typedef struct knns_stats {
+    int algo;        /* family that ran */
+    int splits;
+    int kp;
+    int stages;      /* shared-memory pipeline depth of the tensor-core kernel */
+    int launches;    /* kernels launched by the call */
+    int reserved;
+    int64_t workspace_bytes;
+} knns_stats;
+
+/* Fill *opt with the defaults (automatic algo, splits and shortlist, re-rank on). */
+void knns_default_options(knns_options *opt);
+
+/*
+ * Search with every buffer already in device memory.  Asynchronous on
+ * `stream` (a cudaStream_t, NULL = legacy default stream).  ldc / ldq are the
+ * row pitches (elements) of corpus and queries; dist / idx are Q x k.
+ * `idx` or `dist` may be NULL.  The engine keeps a per-device workspace that
+ * grows on demand; calls on one device are serialised on the host, and a
+ * later call's stream waits for the previous call's work on the workspace.
+ */
+int knns_search_device(const float *corpus, int64_t N, int64_t ldc, const float *queries, int64_t Q,
+                       int64_t ldq, int D, int k, float *dist, int32_t *idx, const knns_options *opt,
+                       void *stream);
+
+/*
+ * Search on host buffers: copies corpus and queries to the device, searches,
+ * copies results back and synchronises.  Returns KNNS_OK or an error code.
+ */
+int knns_search_host(const float *corpus, int64_t N, const float *queries, int64_t Q, int D, int k,
+                     float *dist, int32_t *idx, const knns_options *opt);
+
+/* Synchronise `stream` and report a kernel-side bounded-wait timeout, if any. */
+int knns_check_device(void *stream);
+
+/* Message for the last error raised on the calling thread ("" if none). */
+const char *knns_last_error(void);
+
+/* Statistics of the calling thread's last successful search. */
+int knns_last_stats(knns_stats *out);
+
+/*
+ * Stage timings of the searches run with opt->timing = 1 since the last
+ * collection, from CUDA events recorded on each search's stream:
+ * ms[0] preparation (norms, TF32 split), ms[1] fused distance + shortlist
+ * kernel, ms[2] shortlist merge / re-rank.  Synchronises the device; *count
+ * receives the number of searches summed.  Resets the accumulator.
+ * (The reference kept the same split in knntimes dst_time / srch_time,
+ * include/cuknns.h:43-47.)
+ */
+int knns_timing_collect(double ms[3], int *count);
+
+/* Library version as 10000*major + 100*minor + patch. */
+int knns_version(void);
+
+/*
+ * Test hook: raw 3xTF32 dot products of the first 128 queries against the
+ * first 128 corpus rows, as the tensor-core kernel's accumulator holds them
+ * (dump: 128 x 128 floats, device memory).  Synchronous.
+ */
+int knns_debug_tc_dot_tile(const float *corpus, int64_t N, const float *queries, int64_t Q, int D,
+                           float *dump);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KNN_GB300_H */

@@ -1,0 +1,252 @@
+// common.cuh -- shared device helpers for the GB300 brute-force kNN engine.
+//
+// Ranking keys are carried as one 64-bit word: the high 32 bits are the float
+// key mapped to an order-preserving unsigned integer, the low 32 bits are the
+// global corpus index.  Comparing two words as unsigned integers therefore
+// orders candidates by (key, index), i.e. ties go to the lower index, the rule
+// demo/knn.m:5 gets from MATLAB's stable sort.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace knn {
+
+constexpr uint64_t kSentinel = 0xFFFFFFFFFFFFFFFFull;
+constexpr int kWarp = 32;
+
+__device__ __forceinline__ uint32_t f2ord(float f)
+{
+    uint32_t u = __float_as_uint(f);
+    if (u == 0x80000000u) u = 0u;  // -0 sorts with +0
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__device__ __forceinline__ float ord2f(uint32_t o)
+{
+    uint32_t u = (o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o;
+    return __uint_as_float(u);
+}
+
+__device__ __forceinline__ uint64_t pack_key(float key, uint32_t idx)
+{
+    return ((uint64_t)f2ord(key) << 32) | (uint64_t)idx;
+}
+
+__device__ __forceinline__ float unpack_key(uint64_t w) { return ord2f((uint32_t)(w >> 32)); }
+__device__ __forceinline__ uint32_t unpack_idx(uint64_t w) { return (uint32_t)(w & 0xFFFFFFFFull); }
+
+// Threshold implied by the last kept list entry (+inf while the list is not full).
+__device__ __forceinline__ float thr_of(uint64_t last)
+{
+    return last == kSentinel ? __int_as_float(0x7f800000) : unpack_key(last);
+}
+
+// ---------------------------------------------------------------------------
+// Exact distance convention for the re-rank (bit-identical to the oracle):
+// eight float partial sums over d mod 8 of t*t, t = q_d - c_d, fmaf.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float exact_dist_row(const float* __restrict__ q,
+                                                const float* __restrict__ c, int D)
+{
+    float p[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    int d = 0;
+    for (; d + 8 <= D; d += 8) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            float t = __fsub_rn(q[d + u], __ldg(c + d + u));
+            p[u] = __fmaf_rn(t, t, p[u]);
+        }
+    }
+    for (; d < D; ++d) {
+        float t = __fsub_rn(q[d], __ldg(c + d));
+        p[d & 7] = __fmaf_rn(t, t, p[d & 7]);
+    }
+    return __fadd_rn(__fadd_rn(__fadd_rn(p[0], p[1]), __fadd_rn(p[2], p[3])),
+                     __fadd_rn(__fadd_rn(p[4], p[5]), __fadd_rn(p[6], p[7])));
+}
+
+// ---------------------------------------------------------------------------
+// Warp-level primitives
+// ---------------------------------------------------------------------------
+
+// Bitonic sort of one 64-bit word per lane, ascending by lane.
+__device__ __forceinline__ uint64_t warp_sort32(uint64_t v)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            uint64_t o = __shfl_xor_sync(0xffffffffu, v, stride);
+            bool up = (lane & size) == 0;
+            bool lower = (lane & stride) == 0;
+            bool keep_min = (lower == up);
+            uint64_t mn = o < v ? o : v;
+            uint64_t mx = o < v ? v : o;
+            v = keep_min ? mn : mx;
+        }
+    }
+    return v;
+}
+
+// lower_bound: number of a[0..n) strictly below x (a sorted ascending)
+__device__ __forceinline__ int count_less(const uint64_t* a, int n, uint64_t x)
+{
+    int lo = 0;
+    while (n > 0) {
+        int half = n >> 1;
+        if (a[lo + half] < x) { lo += half + 1; n -= half + 1; }
+        else n = half;
+    }
+    return lo;
+}
+
+// upper_bound: number of a[0..n) not above x
+__device__ __forceinline__ int count_not_above(const uint64_t* a, int n, uint64_t x)
+{
+    int lo = 0;
+    while (n > 0) {
+        int half = n >> 1;
+        if (a[lo + half] <= x) { lo += half + 1; n -= half + 1; }
+        else n = half;
+    }
+    return lo;
+}
+
+// Merge 32 sorted words (one per lane, ascending by lane) into the sorted list
+// L[0..kp) in shared memory, keeping the kp smallest.  scratch: 32 words of
+// per-warp shared memory.  kp is a multiple of 32.  Stable: on equal words the
+// buffered word goes first (only sentinels can be equal).
+__device__ __forceinline__ void warp_merge32(uint64_t* L, int kp, uint64_t b, uint64_t* scratch)
+{
+    const int lane = threadIdx.x & 31;
+    scratch[lane] = b;
+    __syncwarp();
+    const int pb = lane + count_less(L, kp, b);
+    const int nt = kp >> 5;
+    uint64_t lv[16];
+    int lp[16];
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+        if (t < nt) {
+            int j = lane + (t << 5);
+            lv[t] = L[j];
+            lp[t] = j + count_not_above(scratch, 32, lv[t]);
+        }
+    }
+    __syncwarp();
+    if (pb < kp) L[pb] = b;
+#pragma unroll
+    for (int t = 0; t < 16; ++t)
+        if (t < nt && lp[t] < kp) L[lp[t]] = lv[t];
+    __syncwarp();
+}
+
+// Merge two sorted lists A, B of length kp (shared memory) into out[0..kp)
+// (kp smallest), one warp.  out must not alias A or B.  Stable: A first on ties.
+__device__ __forceinline__ void warp_merge_lists(const uint64_t* A, const uint64_t* B, uint64_t* out, int kp)
+{
+    const int lane = threadIdx.x & 31;
+    for (int j = lane; j < kp; j += 32) {
+        uint64_t a = A[j];
+        int pa = j + count_less(B, kp, a);
+        if (pa < kp) out[pa] = a;
+        uint64_t bb = B[j];
+        int pbb = j + count_not_above(A, kp, bb);
+        if (pbb < kp) out[pbb] = bb;
+    }
+    __syncwarp();
+}
+
+// Bitonic sort of n (power of two, <= 1024) words in shared memory by one warp.
+__device__ __forceinline__ void warp_sort_smem(uint64_t* a, int n)
+{
+    const int lane = threadIdx.x & 31;
+    for (int size = 2; size <= n; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int i = lane; i < (n >> 1); i += 32) {
+                int lo = 2 * i - (i & (stride - 1));
+                int hi = lo + stride;
+                bool up = (lo & size) == 0;
+                uint64_t x = a[lo], y = a[hi];
+                if ((x > y) == up) { a[lo] = y; a[hi] = x; }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-query candidate filter with a shared-memory shortlist.
+//
+// Each owner thread holds one query: `thr` (the key of the kp-th kept entry),
+// and `cnt` (entries waiting in its buffer).  A candidate enters the buffer
+// when key < thr; candidates are visited in increasing corpus index, so a key
+// equal to thr can never win its tie and strict < is the exact rule.  Buffers
+// of lanes that could overflow are merged into the lists warp-cooperatively.
+// ---------------------------------------------------------------------------
+constexpr int kBufCap = 32;   // buffered candidates per query
+constexpr int kChunk = 16;    // candidates a lane may add between flush checks
+
+struct ShortlistView {
+    uint64_t* list;     // [nq][kp_pitch]
+    uint64_t* buf;      // [kBufCap][buf_pitch]
+    uint64_t* scratch;  // [warps][32]
+    int kp;
+    int kp_pitch;       // kp + 1
+    int buf_pitch;      // nq + 1
+};
+
+// Merge the buffers of every lane in `mask`; lane `ql` is the query row of this lane.
+__device__ __forceinline__ void flush_lanes(const ShortlistView& v, unsigned mask, int ql, int& cnt,
+                                            float& thr, uint64_t* scratch)
+{
+    const int lane = threadIdx.x & 31;
+    while (mask) {
+        const int src = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const int c = __shfl_sync(0xffffffffu, cnt, src);
+        const int qs = __shfl_sync(0xffffffffu, ql, src);
+        uint64_t b = lane < c ? v.buf[lane * v.buf_pitch + qs] : kSentinel;
+        b = warp_sort32(b);
+        uint64_t* L = v.list + (size_t)qs * v.kp_pitch;
+        warp_merge32(L, v.kp, b, scratch);
+        if (lane == src) {
+            cnt = 0;
+            thr = thr_of(L[v.kp - 1]);
+        }
+    }
+    __syncwarp();
+}
+
+__device__ __forceinline__ void maybe_flush(const ShortlistView& v, int ql, int& cnt, float& thr,
+                                            uint64_t* scratch)
+{
+    unsigned m = __ballot_sync(0xffffffffu, cnt > kBufCap - kChunk);
+    if (m) flush_lanes(v, m, ql, cnt, thr, scratch);
+}
+
+__device__ __forceinline__ void flush_all(const ShortlistView& v, int ql, int& cnt, float& thr,
+                                          uint64_t* scratch)
+{
+    unsigned m = __ballot_sync(0xffffffffu, cnt > 0);
+    if (m) flush_lanes(v, m, ql, cnt, thr, scratch);
+}
+
+__device__ __forceinline__ void offer(const ShortlistView& v, int ql, int& cnt, float thr, float key,
+                                      uint32_t idx)
+{
+    if (key < thr) {
+        v.buf[cnt * v.buf_pitch + ql] = pack_key(key, idx);
+        ++cnt;
+    }
+}
+
+// Bytes of dynamic shared memory used by the shortlist of nq queries.
+__host__ __device__ constexpr size_t shortlist_bytes(int nq, int kp, int warps)
+{
+    return (size_t)nq * (kp + 1) * 8 + (size_t)kBufCap * (nq + 1) * 8 + (size_t)warps * 32 * 8;
+}
+
+}  // namespace knn

@@ -1,0 +1,183 @@
+// dropin.cu -- the reference's C API (include/cuknns.h of shengren/knn-toolbox)
+// implemented on the GB300 engine.
+//
+//   gpuknnsBitonic / gpuknnsHeap  src/cuknnBitonic.cu:422, src/cuknnHeap.cu:394
+//   knnsplan                      src/knnsplan.cu:25
+//   knnsexecute                   src/knnsexecute.cu:6
+//
+// Same names, argument meaning, layouts and return value (elapsed seconds,
+// FLT_MAX on failure).  The two algorithm entry points survive because plans
+// store their addresses (knnplan.pt2Function); both run the same engine,
+// which picks tensor-core or CUDA-core kernels by shape.  knnsplan no longer
+// runs 2 algorithms x 4 stream counts x 10 full searches on host-generated
+// data: it generates [-50,50) data on the device and times the engine's own
+// candidate configurations (kernel family, corpus splits), remembering the
+// fastest in a process-wide plan cache keyed by the problem shape.
+#include <cfloat>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/cuknns.h"
+#include "../../include/knn_gb300.h"
+#include "engine.h"
+#include "kernels.h"
+
+namespace knn {
+
+namespace {
+typedef std::tuple<long, long, long, long> PlanKey;
+std::mutex g_plan_mu;
+std::map<PlanKey, knns_options> g_plans;
+
+knns_options planned_options(long N, long Q, long D, long k)
+{
+    knns_options o;
+    knns_default_options(&o);
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    auto it = g_plans.find(PlanKey(N, Q, D, k));
+    if (it != g_plans.end()) o = it->second;
+    return o;
+}
+
+__global__ void fill_uniform_kernel(float* x, int64_t n, uint32_t seed)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    // splitmix-style hash of (seed, i) -> [0,1) -> [-50, 50)
+    uint64_t z = (uint64_t)i * 0x9E3779B97F4A7C15ull + ((uint64_t)seed << 32 | 0x5bd1e995u);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    float u = (float)(z >> 40) * (1.0f / 16777216.0f);
+    x[i] = 100.0f * u - 50.0f;
+}
+
+double run_dropin(knntype* query, knntype* data, knntype* values, knntype* indices, int objects, int numQueries,
+                  int attributes, int k, int numStreams)
+{
+    (void)numStreams;  // opaque hint: the engine splits the corpus across CTAs, not streams
+    clear_error();
+    if (!query || !data || !values || !indices) {
+        set_error(KNNS_ERR_INVALID, "null pointer passed to the kNN entry point");
+        return FLT_MAX;
+    }
+    knns_options o = planned_options(objects, numQueries, attributes, k);
+    double secs = 0.0;
+    knns_stats st;
+    int rc = search_host(data, objects, query, numQueries, attributes, k, values, nullptr, indices, o, &secs, &st);
+    if (rc != KNNS_OK) return FLT_MAX;
+    remember_stats(st);
+    return secs;
+}
+}  // namespace
+
+}  // namespace knn
+
+using namespace knn;
+
+extern "C" {
+
+double gpuknnsBitonic(knntype* query, knntype* data, knntype* values, knntype* indices, int objects, int numQueries,
+                      int attributes, int k, int numStreams)
+{
+    return run_dropin(query, data, values, indices, objects, numQueries, attributes, k, numStreams);
+}
+
+double gpuknnsHeap(knntype* query, knntype* data, knntype* values, knntype* indices, int objects, int numQueries,
+                   int attributes, int k, int numStreams)
+{
+    return run_dropin(query, data, values, indices, objects, numQueries, attributes, k, numStreams);
+}
+
+void knnsplan(knnplan* plan, long int N, long int Q, long int D, long int k)
+{
+    if (!plan) return;
+    plan->pt2Function = &gpuknnsBitonic;
+    plan->objects = (int)N;
+    plan->numQueries = (int)Q;
+    plan->dimentions = (int)D;
+    plan->k = (int)k;
+    plan->numStreams = 1;
+    clear_error();
+    if (N <= 0 || Q <= 0 || D <= 0 || k <= 0 || k > N) {
+        set_error(KNNS_ERR_INVALID, "knnsplan: invalid sizes");
+        return;
+    }
+    Engine* E = nullptr;
+    if (get_engine(&E) != KNNS_OK) return;
+    std::lock_guard<std::mutex> lk(E->mu);
+    cudaStream_t s = E->host_stream();
+    if ((size_t)N * D > (size_t)1 << 33) return;  // beyond 32 GiB of test data: keep the automatic choice
+    if (E->in_corpus.ensure((size_t)N * D * 4) || E->in_queries.ensure((size_t)Q * D * 4) ||
+        E->out_dist.ensure((size_t)Q * k * 4) || E->out_idx.ensure((size_t)Q * k * 4))
+        return;
+    fill_uniform_kernel<<<(unsigned)(((int64_t)N * D + 255) / 256), 256, 0, s>>>((float*)E->in_corpus.p,
+                                                                              (int64_t)N * D, 1u);
+    fill_uniform_kernel<<<(unsigned)(((int64_t)Q * D + 255) / 256), 256, 0, s>>>((float*)E->in_queries.p,
+                                                                              (int64_t)Q * D, 2u);
+    // candidates: automatic configuration, the two kernel families, and split counts around the model's pick
+    std::vector<knns_options> cands;
+    knns_options base;
+    knns_default_options(&base);
+    cands.push_back(base);
+    Config c0;
+    if (resolve_config(*E, N, Q, (int)D, (int)k, base, &c0) != KNNS_OK) return;
+    for (int f : {2, 3}) {
+        knns_options o = base;
+        o.algo = c0.algo;
+        o.splits = std::max(1, c0.splits * f / 2);
+        if (o.splits != c0.splits) cands.push_back(o);
+        o.splits = std::max(1, c0.splits * 2 / f);
+        if (o.splits != c0.splits) cands.push_back(o);
+    }
+    if (c0.algo == KNNS_ALGO_TC) {
+        knns_options o = base;
+        o.algo = KNNS_ALGO_SIMT;
+        cands.push_back(o);
+    }
+    cudaEvent_t a = E->t0(), b = E->t1();
+    float best_ms = FLT_MAX;
+    knns_options best = base;
+    for (const knns_options& o : cands) {
+        float tot = 0.f;
+        bool ok = true;
+        for (int rep = 0; rep < 3 && ok; ++rep) {
+            cudaEventRecord(a, s);
+            int rc = run_search(*E, (const float*)E->in_corpus.p, N, D, (const float*)E->in_queries.p, Q, D,
+                                (int)D, (int)k, (float*)E->out_dist.p, (int32_t*)E->out_idx.p, nullptr, o, s, nullptr);
+            cudaEventRecord(b, s);
+            if (rc != KNNS_OK || check_device_error(*E, s) != KNNS_OK) { ok = false; break; }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, a, b);
+            if (rep > 0) tot += ms;  // first run warms the workspace
+        }
+        if (ok && tot / 2 < best_ms) {
+            best_ms = tot / 2;
+            best = o;
+        }
+    }
+    clear_error();
+    std::lock_guard<std::mutex> lk2(g_plan_mu);
+    g_plans[PlanKey(N, Q, D, k)] = best;
+}
+
+void knnsexecute(knnplan plan, knntype* data, knntype* queries, knntype* KNNdist, knntype* KNNidx)
+{
+    if (!plan.pt2Function) {
+        set_error(KNNS_ERR_INVALID, "knnsexecute: plan has no function (was knnsplan called?)");
+        printf("Time Elapsed: %f\n", (double)FLT_MAX);
+        return;
+    }
+    double time = plan.pt2Function(queries, data, KNNdist, KNNidx, plan.objects, plan.numQueries, plan.dimentions,
+                                   plan.k, plan.numStreams);
+    printf("Time Elapsed: %f\n", time);
+}
+
+}  // extern "C"

@@ -1,0 +1,67 @@
+// kernels.h -- launchers of the engine's CUDA kernels (internal interface).
+#pragma once
+
+#include <cstdint>
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+namespace knn {
+
+// Tile geometry shared by host and device.
+constexpr int kTileQ = 128;       // queries per CTA (tensor-core M, TMEM lanes)
+constexpr int kTileN = 128;       // corpus rows per tile (tensor-core N)
+constexpr int kChunkK = 32;       // fp32 elements per 128-byte swizzle row
+constexpr int kMaxDpTC = 128;     // A hi + lo must fit next to two accumulators in TMEM
+constexpr int kMaxKpTC = 128;     // shortlist entries per query held in shared memory
+constexpr int kSimtTileN = 64;
+
+// error codes written by kernels into the device error word
+enum DeviceError : int {
+    kDevOk = 0,
+    kDevTimeoutProducer = 1,
+    kDevTimeoutMma = 2,
+    kDevTimeoutEpilogue = 3,
+    kDevTimeoutAload = 4,
+};
+
+cudaError_t launch_norms(const float* x, int64_t n, int64_t ld, int D, float* out, int64_t n_pad,
+                         cudaStream_t s);
+cudaError_t launch_split(const float* x, int64_t n, int64_t ld, int D, int dp, float* hi, float* lo,
+                         cudaStream_t s);
+
+// CUDA-core FP32 fused distance + shortlist.  qpb in {32, 128}.
+size_t simt_smem_bytes(int qpb, int kp);
+cudaError_t launch_simt(const float* corpus, int64_t N, int64_t ldc, const float* cn,
+                        const float* queries, int64_t Q, int64_t ldq, int D, int kp, int qpb,
+                        int64_t split_len, int splits, uint64_t* part, cudaStream_t s);
+
+// Tensor-core 3xTF32 fused distance + shortlist (tcgen05, TMA, TMEM).
+struct TcArgs {
+    CUtensorMap tm_hi;        // corpus hi  [N][dp] fp32, box {32, 128}, 128B swizzle
+    CUtensorMap tm_lo;        // corpus lo
+    const float* cn;          // [>= roundup(N,128)] corpus norms, +inf padding
+    const float* queries;     // [Q][ldq]
+    int64_t Q;
+    int64_t ldq;
+    int64_t N;
+    int64_t split_len;        // corpus rows per split, multiple of kTileN
+    uint64_t* part;           // [splits][Q][kp]
+    float* dump;              // optional: raw dot tile of CTA (0,0), tile 0, [128][128]
+    int* err;                 // device error word
+    int D;
+    int dp;                   // D rounded up to kChunkK
+    int kp;
+    int stages;
+};
+size_t tc_smem_bytes(int kp, int stages);
+int tc_max_stages(int kp);
+cudaError_t launch_tc(const TcArgs& a, int splits, cudaStream_t s);
+
+// Merge of the per-split shortlists, optional exact re-rank, final top-k.
+size_t select_smem_bytes(int kp, int D, int rerank);
+cudaError_t launch_select(const uint64_t* part, int splits, int64_t Q, int kp, int k,
+                          const float* corpus, int64_t ldc, const float* queries, int64_t ldq,
+                          int D, int rerank, const float* qn, float* out_dist, int32_t* out_idx,
+                          float* out_idx_f, cudaStream_t s);
+
+}  // namespace knn

@@ -1,0 +1,88 @@
+// prep.cu -- corpus/query preparation: row norms and the TF32 hi/lo split.
+//
+// Replaces the reference's norm kernels crpdot2_* / dot4_* (include/utils.h:72-357,
+// 516-766), which reduce x_d^2 in float with a warp-synchronous tree.  Here a
+// row norm is the float rounding of a double sum taken in d order (exact for
+// the integer-valued data of the 1M x 128 workload and within one rounding of
+// exact otherwise); the same convention is used by the CPU oracle.
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "common.cuh"
+#include "kernels.h"
+
+namespace knn {
+
+__global__ void norms_kernel(const float* __restrict__ x, int64_t n, int64_t ld, int D,
+                             float* __restrict__ out, int64_t n_pad)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_pad) return;
+    if (i >= n) {  // padding rows never enter a shortlist
+        out[i] = __int_as_float(0x7f800000);
+        return;
+    }
+    const float* r = x + i * ld;
+    double acc = 0.0;
+    int d = 0;
+    for (; d + 4 <= D; d += 4) {
+        float a = __ldg(r + d), b = __ldg(r + d + 1), c = __ldg(r + d + 2), e = __ldg(r + d + 3);
+        acc = __fma_rn((double)a, (double)a, acc);
+        acc = __fma_rn((double)b, (double)b, acc);
+        acc = __fma_rn((double)c, (double)c, acc);
+        acc = __fma_rn((double)e, (double)e, acc);
+    }
+    for (; d < D; ++d) {
+        float a = __ldg(r + d);
+        acc = __fma_rn((double)a, (double)a, acc);
+    }
+    out[i] = __double2float_rn(acc);
+}
+
+// Round a float to the nearest TF32 value (10 explicit mantissa bits, ties to
+// even), returned as a float whose low 13 bits are zero.
+__device__ __forceinline__ float tf32_rne(float x)
+{
+    uint32_t u = __float_as_uint(x);
+    if ((u & 0x7f800000u) == 0x7f800000u) return x;  // inf / nan unchanged
+    u += 0xfffu + ((u >> 13) & 1u);
+    u &= 0xffffe000u;
+    return __uint_as_float(u);
+}
+
+// hi = tf32(x), lo = tf32(x - hi); rows padded with zeros to dp columns.
+__global__ void split_kernel(const float* __restrict__ x, int64_t n, int64_t ld, int D, int dp,
+                             float* __restrict__ hi, float* __restrict__ lo)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t total = n * dp;
+    if (i >= total) return;
+    int64_t r = i / dp;
+    int c = (int)(i - r * dp);
+    float v = c < D ? __ldg(x + r * ld + c) : 0.f;
+    float h = tf32_rne(v);
+    hi[i] = h;
+    lo[i] = tf32_rne(__fsub_rn(v, h));
+}
+
+cudaError_t launch_norms(const float* x, int64_t n, int64_t ld, int D, float* out, int64_t n_pad,
+                         cudaStream_t s)
+{
+    if (n_pad <= 0) return cudaSuccess;
+    int threads = 256;
+    int64_t blocks = (n_pad + threads - 1) / threads;
+    norms_kernel<<<(unsigned)blocks, threads, 0, s>>>(x, n, ld, D, out, n_pad);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_split(const float* x, int64_t n, int64_t ld, int D, int dp, float* hi, float* lo,
+                         cudaStream_t s)
+{
+    int64_t total = n * dp;
+    if (total <= 0) return cudaSuccess;
+    int threads = 256;
+    int64_t blocks = (total + threads - 1) / threads;
+    split_kernel<<<(unsigned)blocks, threads, 0, s>>>(x, n, ld, D, dp, hi, lo);
+    return cudaGetLastError();
+}
+
+}  // namespace knn

@@ -1,0 +1,261 @@
+"""Python mirror of knn-toolbox's interface over the GB300 engine's C ABI.
+
+The engine is the CUDA shared library built from ``knn-toolbox_gb300/csrc``
+(``_build/libknngb300.so``); this module only binds its C entry points with
+ctypes.  There is no fallback: if the library is missing or fails to load,
+every call raises.
+
+Reference interfaces mirrored here (paths within shengren/knn-toolbox):
+
+* ``gpuknnsBitonic`` / ``gpuknnsHeap`` -- include/cuknns.h:75,83: host arrays,
+  D-leading corpus and queries, k-leading outputs, 0-based float indices,
+  returns elapsed seconds.
+* ``knnsplan`` / ``knnsexecute`` -- include/cuknns.h:85,87.
+* ``gpuknnBitonic`` / ``gpuknnHeap`` / ``gpuknns`` -- toolbox/*.m: MATLAB
+  column matrices (d x n), 1-based indices, columns sorted ascending.
+* ``search`` / ``search_host`` -- the engine's status-returning API
+  (include/knn_gb300.h) on device tensors or host arrays.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG, "_build", "libknngb300.so")
+
+ALGO_AUTO, ALGO_TC, ALGO_SIMT = 0, 1, 2
+OK, ERR_INVALID, ERR_CUDA, ERR_UNSUPPORTED, ERR_DEVICE_TIMEOUT, ERR_NOMEM = range(6)
+
+# Every symbol include/knn_gb300.h and include/cuknns.h declare.
+EXPORTED = ["knns_default_options", "knns_search_device", "knns_search_host", "knns_check_device",
+            "knns_last_error", "knns_last_stats", "knns_version", "knns_debug_tc_dot_tile",
+            "knns_timing_collect",
+            "gpuknnsBitonic", "gpuknnsHeap", "knnsplan", "knnsexecute"]
+
+
+class KnnsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"knns error {code}: {msg}")
+        self.code = code
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("algo", ctypes.c_int), ("splits", ctypes.c_int), ("rerank", ctypes.c_int),
+                ("kp", ctypes.c_int), ("timing", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("algo", ctypes.c_int), ("splits", ctypes.c_int), ("kp", ctypes.c_int),
+                ("stages", ctypes.c_int), ("launches", ctypes.c_int), ("reserved", ctypes.c_int),
+                ("workspace_bytes", ctypes.c_int64)]
+
+
+KNNPTR2FUNCTION = ctypes.CFUNCTYPE(ctypes.c_double, *([ctypes.POINTER(ctypes.c_float)] * 4),
+                                   *([ctypes.c_int] * 5))
+
+
+class KnnPlan(ctypes.Structure):
+    """include/cuknns.h:34-41 knnplan (binary layout kept)."""
+    _fields_ = [("pt2Function", ctypes.c_void_p), ("objects", ctypes.c_int), ("numQueries", ctypes.c_int),
+                ("dimentions", ctypes.c_int), ("k", ctypes.c_int), ("numStreams", ctypes.c_int)]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return LIB_PATH
+
+
+def lib():
+    """Load the engine library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"GB300 kNN engine library not built: {LIB_PATH} (run __graft_entry__.build())")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, i64, ci = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.knns_default_options.argtypes = [ctypes.POINTER(Options)]
+    L.knns_default_options.restype = None
+    L.knns_search_device.argtypes = [vp, i64, i64, vp, i64, i64, ci, ci, vp, vp, ctypes.POINTER(Options), vp]
+    L.knns_search_host.argtypes = [vp, i64, vp, i64, ci, ci, vp, vp, ctypes.POINTER(Options)]
+    L.knns_check_device.argtypes = [vp]
+    L.knns_last_error.restype = ctypes.c_char_p
+    L.knns_last_stats.argtypes = [ctypes.POINTER(Stats)]
+    L.knns_debug_tc_dot_tile.argtypes = [vp, i64, vp, i64, ci, vp]
+    L.knns_timing_collect.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
+    L.gpuknnsBitonic.argtypes = [fp, fp, fp, fp, ci, ci, ci, ci, ci]
+    L.gpuknnsBitonic.restype = ctypes.c_double
+    L.gpuknnsHeap.argtypes = [fp, fp, fp, fp, ci, ci, ci, ci, ci]
+    L.gpuknnsHeap.restype = ctypes.c_double
+    L.knnsplan.argtypes = [ctypes.POINTER(KnnPlan), ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.c_long]
+    L.knnsplan.restype = None
+    L.knnsexecute.argtypes = [KnnPlan, fp, fp, fp, fp]
+    L.knnsexecute.restype = None
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return lib().knns_last_error().decode()
+
+
+def _check(rc):
+    if rc != OK:
+        raise KnnsError(rc, last_error())
+
+
+def options(algo=ALGO_AUTO, splits=0, rerank=True, kp=0, timing=False) -> Options:
+    o = Options()
+    lib().knns_default_options(ctypes.byref(o))
+    o.algo, o.splits, o.rerank, o.kp = int(algo), int(splits), int(bool(rerank)), int(kp)
+    o.timing = int(bool(timing))
+    return o
+
+
+def timing_collect():
+    """Sum of per-stage milliseconds of timed searches since the last call: (prep, fused, select, count)."""
+    ms = (ctypes.c_double * 3)()
+    n = ctypes.c_int(0)
+    _check(lib().knns_timing_collect(ms, ctypes.byref(n)))
+    return ms[0], ms[1], ms[2], n.value
+
+
+def last_stats() -> dict:
+    s = Stats()
+    _check(lib().knns_last_stats(ctypes.byref(s)))
+    return {"algo": s.algo, "splits": s.splits, "kp": s.kp, "stages": s.stages, "launches": s.launches,
+            "workspace_bytes": s.workspace_bytes}
+
+
+# --------------------------------------------------------------------------
+# engine API
+# --------------------------------------------------------------------------
+
+def search(corpus, queries, k, *, dist=None, idx=None, algo=ALGO_AUTO, splits=0, rerank=True, kp=0,
+           stream=None, check=True, timing=False):
+    """kNN on CUDA tensors (float32, rows contiguous).  Returns (dist[Q,k] f32, idx[Q,k] i32)."""
+    import torch
+    assert corpus.is_cuda and queries.is_cuda, "search() takes device tensors"
+    assert corpus.dtype == torch.float32 and queries.dtype == torch.float32
+    assert corpus.stride(1) == 1 and queries.stride(1) == 1
+    N, D = corpus.shape
+    Q = queries.shape[0]
+    assert queries.shape[1] == D
+    if dist is None:
+        dist = torch.empty((Q, k), dtype=torch.float32, device=corpus.device)
+    if idx is None:
+        idx = torch.empty((Q, k), dtype=torch.int32, device=corpus.device)
+    s = torch.cuda.current_stream(corpus.device) if stream is None else stream
+    o = options(algo, splits, rerank, kp, timing)
+    rc = lib().knns_search_device(corpus.data_ptr(), N, corpus.stride(0), queries.data_ptr(), Q,
+                                  queries.stride(0), D, k, dist.data_ptr(), idx.data_ptr(), ctypes.byref(o),
+                                  ctypes.c_void_p(s.cuda_stream))
+    _check(rc)
+    if check:
+        _check(lib().knns_check_device(ctypes.c_void_p(s.cuda_stream)))
+    return dist, idx
+
+
+def search_host(corpus, queries, k, *, algo=ALGO_AUTO, splits=0, rerank=True, kp=0):
+    """kNN on host arrays (N x D, Q x D float32).  Returns numpy (dist, idx)."""
+    corpus = np.ascontiguousarray(corpus, dtype=np.float32)
+    queries = np.ascontiguousarray(queries, dtype=np.float32)
+    N, D = corpus.shape
+    Q = queries.shape[0]
+    dist = np.empty((Q, k), np.float32)
+    idx = np.empty((Q, k), np.int32)
+    o = options(algo, splits, rerank, kp)
+    _check(lib().knns_search_host(corpus.ctypes.data, N, queries.ctypes.data, Q, D, k, dist.ctypes.data,
+                                  idx.ctypes.data, ctypes.byref(o)))
+    return dist, idx
+
+
+def debug_tc_dot_tile(corpus, queries):
+    import torch
+    dump = torch.empty((128, 128), dtype=torch.float32, device=corpus.device)
+    _check(lib().knns_debug_tc_dot_tile(corpus.data_ptr(), corpus.shape[0], queries.data_ptr(), queries.shape[0],
+                                        corpus.shape[1], dump.data_ptr()))
+    return dump
+
+
+# --------------------------------------------------------------------------
+# reference C API (include/cuknns.h)
+# --------------------------------------------------------------------------
+
+def _fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def _c_call(fn, query, data, k, numStreams):
+    """query: Q x D (D leading), data: N x D.  Returns (values[Q,k], indices[Q,k] float, seconds)."""
+    query = np.ascontiguousarray(query, dtype=np.float32)
+    data = np.ascontiguousarray(data, dtype=np.float32)
+    Q, D = query.shape
+    N = data.shape[0]
+    values = np.empty((Q, k), np.float32)
+    indices = np.empty((Q, k), np.float32)
+    t = fn(_fptr(query), _fptr(data), _fptr(values), _fptr(indices), N, Q, D, k, numStreams)
+    if t >= 3.0e38:
+        raise KnnsError(-1, last_error())
+    return values, indices, t
+
+
+def gpuknnsBitonic(query, data, k, numStreams=1):
+    return _c_call(lib().gpuknnsBitonic, query, data, k, numStreams)
+
+
+def gpuknnsHeap(query, data, k, numStreams=1):
+    return _c_call(lib().gpuknnsHeap, query, data, k, numStreams)
+
+
+def knnsplan(N, Q, D, k) -> KnnPlan:
+    plan = KnnPlan()
+    lib().knnsplan(ctypes.byref(plan), N, Q, D, k)
+    if not plan.pt2Function:
+        raise KnnsError(-1, last_error())
+    return plan
+
+
+def knnsexecute(plan: KnnPlan, data, queries):
+    data = np.ascontiguousarray(data, dtype=np.float32)
+    queries = np.ascontiguousarray(queries, dtype=np.float32)
+    KNNdist = np.empty((plan.numQueries, plan.k), np.float32)
+    KNNidx = np.empty((plan.numQueries, plan.k), np.float32)
+    lib().knnsexecute(plan, _fptr(data), _fptr(queries), _fptr(KNNdist), _fptr(KNNidx))
+    return KNNdist, KNNidx
+
+
+# --------------------------------------------------------------------------
+# MATLAB toolbox semantics (toolbox/gpuknnBitonic.m, gpuknnHeap.m, gpuknns.m)
+# --------------------------------------------------------------------------
+
+def _toolbox(fn, query, pdata, k, numStreams):
+    """query: d x Q, pdata: d x N (columns are vectors).  Returns (dist k x Q, idx k x Q 1-based, time)."""
+    q = np.asarray(query, dtype=np.float32).T
+    c = np.asarray(pdata, dtype=np.float32).T
+    values, indices, t = fn(q, c, k, numStreams)
+    idx = indices + 1                                   # gpuknnBitonic.m:24
+    order = np.argsort(values, axis=1, kind="stable")   # gpuknnBitonic.m:26-30
+    values = np.take_along_axis(values, order, axis=1)
+    idx = np.take_along_axis(idx, order, axis=1)
+    return values[:, :k].T.copy(), idx[:, :k].T.copy(), t  # gpuknnBitonic.m:32-33
+
+
+def gpuknnBitonic(query, pdata, k, numStreams=1):
+    return _toolbox(gpuknnsBitonic, query, pdata, k, numStreams)
+
+
+def gpuknnHeap(query, pdata, k, numStreams=1):
+    return _toolbox(gpuknnsHeap, query, pdata, k, numStreams)
+
+
+def gpuknns(plan: dict, queries, data):
+    """toolbox/gpuknns.m: plan is {'function': gpuknnBitonic|gpuknnHeap, 'k': k, 'streams': s}."""
+    return plan["function"](queries, data, plan["k"], plan["streams"])
