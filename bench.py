@@ -36,6 +36,9 @@ WORKLOADS = {
                   gen="int_descriptor", N=1_000_000, D=128, Q=10_000, k=100, seed=1),
     "uniform64k": dict(desc="uniform [0,1) corpus 65,536 x 128, 1,024 queries, k=16, seed 0",
                        gen="uniform", N=65_536, D=128, Q=1_024, k=16, seed=0),
+    # profiling-sized cut of int1m (corpus still larger than L2) for ncu captures
+    "int256k": dict(desc="int-descriptor corpus 262,144 x 128, 10,000 queries, k=100, seed 1",
+                    gen="int_descriptor", N=262_144, D=128, Q=10_000, k=100, seed=1),
 }
 METRIC = "queries/s (exact squared-L2 kNN, plain FP32 form)"
 
@@ -174,6 +177,27 @@ def run_reference(args, w):
     return 0
 
 
+def run_e2e(corpus_np, queries_np, k, Q, world, steps, barrier, dist, dev):
+    """Same metric through the reference-facing C ABI with host buffers (copies timed)."""
+    import torch
+    import cuknns
+    hc = torch.from_numpy(corpus_np).pin_memory().numpy()
+    hq = torch.from_numpy(queries_np).pin_memory().numpy()
+    cuknns.gpuknnsBitonic(hq, hc, k, 1)  # warm (staging buffers)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        vals, idxf, secs = cuknns.gpuknnsBitonic(hq, hc, k, 1)
+    e2e_s = (time.perf_counter() - t0) / steps
+    if dist is not None:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    return {"value": Q * world / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": int(hc.nbytes + hq.nbytes),
+            "d2h_bytes_per_step": int(vals.nbytes + idxf.nbytes), "api": "gpuknnsBitonic (include/cuknns.h)",
+            "host_buffers": "pinned inputs, pageable outputs", "steps": steps}
+
+
 def run_gb300(args, w):
     import torch
     import cuknns
@@ -231,22 +255,10 @@ def run_gb300(args, w):
     value = Q * args.steps * world / (el_ms / 1e3)
 
     # ---- end to end through the drop-in C ABI from pinned host buffers
-    e2e_steps = max(1, min(args.steps, 20))
-    hc = torch.from_numpy(corpus_np).pin_memory().numpy()
-    hq = torch.from_numpy(queries_np).pin_memory().numpy()
-    cuknns.gpuknnsBitonic(hq, hc, k, 1)  # warm (staging buffers)
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        vals, idxf, secs = cuknns.gpuknnsBitonic(hq, hc, k, 1)
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    if dist is not None:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": Q * world / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": int(hc.nbytes + hq.nbytes),
-           "d2h_bytes_per_step": int(vals.nbytes + idxf.nbytes), "api": "gpuknnsBitonic (include/cuknns.h)",
-           "host_buffers": "pinned inputs, pageable outputs", "steps": e2e_steps}
+    e2e = None
+    e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 20))
+    if e2e_steps:
+        e2e = run_e2e(corpus_np, queries_np, k, Q, world, e2e_steps, barrier, dist, dev)
 
     # ---- roofline of the dominant kernel (fused distance + shortlist)
     peaks, peak_kind = measured_peaks()
@@ -302,6 +314,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="int1m", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

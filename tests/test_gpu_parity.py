@@ -101,8 +101,12 @@ def test_tc_reference_semantics_parity(engine, oracle, N, Q, D, k):
     X, Qs = data_uniform(N, Q, D, 11 * N + D)
     d, i, st = run(engine, X, Qs, k, algo=engine.ALGO_TC, rerank=False)
     od, oi = oracle.knn_gemm(X, Qs, k)
-    # key-ranked: positions may differ only between near-equal FP64 distances
-    oracle.check_parity(X, Qs, k, d, i, ref_idx=oi, gap_rel=GAP, dist_rel=1e-4)
+    # Ranking by the FP32 GEMM-form key (the reference's own algorithm) carries
+    # an absolute key error of a few FP32 ulps of ||q||^2 + ||c||^2, about 1e-6
+    # of the distance on this data, so two FP32 implementations may order
+    # candidates whose FP64 distances differ by less than ~2e-5 differently.
+    # The default re-rank mode is held to the 1e-6 gap instead.
+    oracle.check_parity(X, Qs, k, d, i, ref_idx=oi, gap_rel=2e-5, dist_rel=1e-4)
     np.testing.assert_allclose(d, od, rtol=2e-5, atol=2e-5 * np.abs(od).max())
 
 
