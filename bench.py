@@ -121,6 +121,27 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def lo_tile_fraction(x, rows=128):
+    """Fraction of 128-row tiles whose TF32 low part (x - tf32(x), rounded to TF32) is nonzero.
+
+    The tensor-core kernel runs the two correction products of 3xTF32 only on
+    such tiles, so this sets the executed tensor work.
+    """
+    def tf32(a):
+        u = a.view(np.uint32).astype(np.uint64)
+        u = (u + 0xFFF + ((u >> 13) & 1)) & 0xFFFFE000
+        return u.astype(np.uint32).view(np.float32)
+    hits = []
+    for s in range(0, x.shape[0], 1 << 16):
+        blk = x[s:s + (1 << 16)]
+        lo = tf32((blk - tf32(blk)).astype(np.float32))
+        row = (lo != 0).any(axis=1)
+        pad = (-len(row)) % rows
+        hits.append(np.concatenate([row, np.zeros(pad, bool)]).reshape(-1, rows).any(axis=1))
+    h = np.concatenate(hits)
+    return float(h.mean()) if h.size else 0.0
+
+
 def cpu_baseline(corpus, queries, k, budget_s=12.0):
     """demo/knn.m restated in C (oracle), all host threads, on a bounded query sample."""
     import oracle
@@ -265,11 +286,16 @@ def run_gb300(args, w):
     fused_avg_ms = fused_ms / max(1, nt)
     kern = "tc_kernel" if st["algo"] == cuknns.ALGO_TC else "simt_kernel"
     if st["algo"] == cuknns.ALGO_TC:
-        flops = 3.0 * 2.0 * N * Q * D       # three TF32 products per useful product
+        # 3xTF32 issues hi.hi always and the two correction products only for
+        # tiles whose TF32 low part is nonzero (corpus tile / query tile)
+        f_c, f_q = lo_tile_fraction(corpus_np), lo_tile_fraction(queries_np)
+        products = 1.0 + f_c + f_q
+        flops = products * 2.0 * N * Q * D
         peak = peaks["bf16_tflops"] / 2.0    # dense TF32 runs at half the BF16 rate
         roof = {"bound": "tensor", "achieved": flops / (fused_avg_ms / 1e3) / 1e12, "peak": peak,
                 "unit": "TFLOP/s",
-                "peak_source": f"{peak_kind} bf16 dense burst / 2 (TF32 dense rate)"}
+                "peak_source": f"{peak_kind} bf16 dense burst / 2 (TF32 dense rate)",
+                "tf32_products_per_useful_product": products}
     else:
         flops = 2.0 * N * Q * D
         peak = 152 * 128 * 2 * 2.07e9 / 1e12

@@ -41,7 +41,7 @@ typedef struct knns_options {
     int splits;      /* corpus splits processed by independent CTAs; 0 = automatic */
     int rerank;      /* 1 (default): shortlist re-ranked by the exact direct-difference distance;
                         0: reference semantics, rank by ||c||^2 - 2 q.c, distance = key + ||q||^2 */
-    int kp;          /* shortlist length per query (multiple of 32, >= k); 0 = automatic */
+    int kp;          /* shortlist length per query (multiple of 16, >= 32, >= k); 0 = automatic */
     int timing;      /* 1: record CUDA events around each stage (see knns_timing_collect) */
     int reserved[3];
 } knns_options;

@@ -114,25 +114,37 @@ __device__ __forceinline__ int count_not_above(const uint64_t* a, int n, uint64_
     return lo;
 }
 
+// upper_bound over 32 words stored with a stride (in words)
+__device__ __forceinline__ int count_not_above32(const uint64_t* a, int stride, uint64_t x)
+{
+    int lo = 0, n = 32;
+    while (n > 0) {
+        int half = n >> 1;
+        if (a[(lo + half) * stride] <= x) { lo += half + 1; n -= half + 1; }
+        else n = half;
+    }
+    return lo;
+}
+
 // Merge 32 sorted words (one per lane, ascending by lane) into the sorted list
-// L[0..kp) in shared memory, keeping the kp smallest.  scratch: 32 words of
-// per-warp shared memory.  kp is a multiple of 32.  Stable: on equal words the
+// L[0..kp) in shared memory, keeping the kp smallest.  `sorted` holds the same
+// 32 words in shared memory at stride `stride` (read for the ranks of the list
+// entries).  kp is a multiple of 16, at most 512.  Stable: on equal words the
 // buffered word goes first (only sentinels can be equal).
-__device__ __forceinline__ void warp_merge32(uint64_t* L, int kp, uint64_t b, uint64_t* scratch)
+__device__ __forceinline__ void warp_merge32(uint64_t* L, int kp, uint64_t b, const uint64_t* sorted, int stride)
 {
     const int lane = threadIdx.x & 31;
-    scratch[lane] = b;
-    __syncwarp();
     const int pb = lane + count_less(L, kp, b);
-    const int nt = kp >> 5;
+    const int nt = (kp + 31) >> 5;
     uint64_t lv[16];
     int lp[16];
 #pragma unroll
     for (int t = 0; t < 16; ++t) {
-        if (t < nt) {
-            int j = lane + (t << 5);
+        const int j = lane + (t << 5);
+        lp[t] = kp;
+        if (t < nt && j < kp) {
             lv[t] = L[j];
-            lp[t] = j + count_not_above(scratch, 32, lv[t]);
+            lp[t] = j + count_not_above32(sorted, stride, lv[t]);
         }
     }
     __syncwarp();
@@ -180,27 +192,27 @@ __device__ __forceinline__ void warp_sort_smem(uint64_t* a, int n)
 // ---------------------------------------------------------------------------
 // Per-query candidate filter with a shared-memory shortlist.
 //
-// Each owner thread holds one query: `thr` (the key of the kp-th kept entry),
-// and `cnt` (entries waiting in its buffer).  A candidate enters the buffer
-// when key < thr; candidates are visited in increasing corpus index, so a key
-// equal to thr can never win its tie and strict < is the exact rule.  Buffers
-// of lanes that could overflow are merged into the lists warp-cooperatively.
+// Each owner thread holds one query: `thr_local` (the key of the kp-th kept
+// entry) and `cnt` (entries waiting in its buffer).  A candidate enters the
+// buffer when key < thr_local; candidates are visited in increasing corpus
+// index, so a key equal to thr_local can never win its tie and strict < is
+// the exact rule.  Buffers of lanes that would overflow are merged into the
+// lists warp-cooperatively, 32 candidates at a time.
 // ---------------------------------------------------------------------------
 constexpr int kBufCap = 32;   // buffered candidates per query
-constexpr int kChunk = 16;    // candidates a lane may add between flush checks
 
 struct ShortlistView {
     uint64_t* list;     // [nq][kp_pitch]
     uint64_t* buf;      // [kBufCap][buf_pitch]
-    uint64_t* scratch;  // [warps][32]
     int kp;
-    int kp_pitch;       // kp + 1
+    int kp_pitch;
     int buf_pitch;      // nq + 1
 };
 
 // Merge the buffers of every lane in `mask`; lane `ql` is the query row of this lane.
-__device__ __forceinline__ void flush_lanes(const ShortlistView& v, unsigned mask, int ql, int& cnt,
-                                            float& thr, uint64_t* scratch)
+// Kept out of line: it runs rarely and would otherwise be inlined at every offer site.
+static __device__ __noinline__ void flush_lanes(const ShortlistView& v, unsigned mask, int ql, int& cnt,
+                                                float& thr)
 {
     const int lane = threadIdx.x & 31;
     while (mask) {
@@ -208,10 +220,13 @@ __device__ __forceinline__ void flush_lanes(const ShortlistView& v, unsigned mas
         mask &= mask - 1;
         const int c = __shfl_sync(0xffffffffu, cnt, src);
         const int qs = __shfl_sync(0xffffffffu, ql, src);
-        uint64_t b = lane < c ? v.buf[lane * v.buf_pitch + qs] : kSentinel;
+        uint64_t* col = v.buf + qs;  // this query's buffer column, stride buf_pitch
+        uint64_t b = lane < c ? col[lane * v.buf_pitch] : kSentinel;
         b = warp_sort32(b);
+        col[lane * v.buf_pitch] = b;  // the column now holds the sorted words
+        __syncwarp();
         uint64_t* L = v.list + (size_t)qs * v.kp_pitch;
-        warp_merge32(L, v.kp, b, scratch);
+        warp_merge32(L, v.kp, b, col, v.buf_pitch);
         if (lane == src) {
             cnt = 0;
             thr = thr_of(L[v.kp - 1]);
@@ -220,33 +235,61 @@ __device__ __forceinline__ void flush_lanes(const ShortlistView& v, unsigned mas
     __syncwarp();
 }
 
-__device__ __forceinline__ void maybe_flush(const ShortlistView& v, int ql, int& cnt, float& thr,
-                                            uint64_t* scratch)
-{
-    unsigned m = __ballot_sync(0xffffffffu, cnt > kBufCap - kChunk);
-    if (m) flush_lanes(v, m, ql, cnt, thr, scratch);
-}
-
-__device__ __forceinline__ void flush_all(const ShortlistView& v, int ql, int& cnt, float& thr,
-                                          uint64_t* scratch)
+__device__ __forceinline__ void flush_all(const ShortlistView& v, int ql, int& cnt, float& thr)
 {
     unsigned m = __ballot_sync(0xffffffffu, cnt > 0);
-    if (m) flush_lanes(v, m, ql, cnt, thr, scratch);
+    if (m) flush_lanes(v, m, ql, cnt, thr);
 }
 
-__device__ __forceinline__ void offer(const ShortlistView& v, int ql, int& cnt, float thr, float key,
-                                      uint32_t idx)
+// Threshold shared by every CTA working on one query (other corpus splits):
+// the order-mapped key of some split's full kp-th entry, kept with atomicMin.
+// Any such value bounds the final kp-th key from above, so candidates with a
+// larger key can be dropped; equal keys are kept (their index may still win).
+__device__ __forceinline__ float shared_thr_of(uint32_t g)
 {
-    if (key < thr) {
-        v.buf[cnt * v.buf_pitch + ql] = pack_key(key, idx);
-        ++cnt;
+    if (g >= 0xFF800000u) return __int_as_float(0x7f800000);  // unset (or +inf)
+    return ord2f(g + 1u);                                       // next float above the bound
+}
+
+__device__ __forceinline__ void publish_thr(uint32_t* thr_g, int64_t q, float thr_local)
+{
+    if (thr_g != nullptr && thr_local < __int_as_float(0x7f800000)) atomicMin(thr_g + q, f2ord(thr_local));
+}
+
+// Offer 32 consecutive candidates of this lane's query: keys key[0..31] with
+// corpus indices nbase + j, visited in increasing index.  thr_glob is the
+// decoded shared threshold (+inf when unused).  Buffers that would overflow
+// are merged first; lanes that merged publish their new kp-th key.
+__device__ __forceinline__ void offer32(const ShortlistView& v, int ql, int& cnt, float& thr_local,
+                                        float thr_glob, const float (&key)[32], uint32_t nbase,
+                                        uint32_t* thr_g, int64_t q)
+{
+    float thr = fminf(thr_local, thr_glob);
+    uint32_t m = 0;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) m |= (key[j] < thr ? 1u : 0u) << j;
+    if (!__any_sync(0xffffffffu, m != 0u)) return;
+    const bool need = cnt + __popc(m) > kBufCap;
+    const unsigned fl = __ballot_sync(0xffffffffu, need);
+    if (fl) {
+        flush_lanes(v, fl, ql, cnt, thr_local);
+        if (need) {
+            publish_thr(thr_g, q, thr_local);
+            thr = fminf(thr_local, thr_glob);
+            m = 0;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) m |= (key[j] < thr ? 1u : 0u) << j;
+        }
     }
-}
-
-// Bytes of dynamic shared memory used by the shortlist of nq queries.
-__host__ __device__ constexpr size_t shortlist_bytes(int nq, int kp, int warps)
-{
-    return (size_t)nq * (kp + 1) * 8 + (size_t)kBufCap * (nq + 1) * 8 + (size_t)warps * 32 * 8;
+    if (m) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            if ((m >> j) & 1u) {
+                v.buf[cnt * v.buf_pitch + ql] = pack_key(key[j], nbase + (uint32_t)j);
+                ++cnt;
+            }
+        }
+    }
 }
 
 }  // namespace knn

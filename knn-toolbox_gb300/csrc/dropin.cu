@@ -24,8 +24,8 @@
 
 #include <cuda_runtime.h>
 
-#include "../../include/cuknns.h"
-#include "../../include/knn_gb300.h"
+#include "cuknns.h"
+#include "knn_gb300.h"
 #include "engine.h"
 #include "kernels.h"
 

@@ -21,7 +21,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
-#include "../../include/knn_gb300.h"
+#include "knn_gb300.h"
 #include "engine.h"
 #include "kernels.h"
 
@@ -150,10 +150,12 @@ static int encode_rows(CUtensorMap* m, const float* base, int64_t rows, int64_t 
 // ---------------------------------------------------------------- planning
 static inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 static inline int round32(int x) { return (x + 31) & ~31; }
+static inline int round16(int x) { return (x + 15) & ~15; }
 
+// Shortlist length: k plus a re-rank margin of max(8, k/8), in multiples of 16.
 int auto_kp(int k, int rerank)
 {
-    int kp = rerank ? round32(k + std::max(8, k / 8)) : round32(k);
+    int kp = rerank ? round16(k + std::max(8, k / 8)) : round16(k);
     return std::max(kp, 32);
 }
 
@@ -179,14 +181,15 @@ int resolve_config(const Engine& E, int64_t N, int64_t Q, int D, int k, const kn
 {
     c->rerank = o.rerank ? 1 : 0;
     c->kp = o.kp > 0 ? o.kp : auto_kp(k, c->rerank);
-    if (o.kp <= 0 && c->kp > 512 && k <= 512) c->kp = std::max(round32(k), 32);  // no margin at the limit
-    if (c->kp % 32 != 0 || c->kp < k)
-        return set_error(KNNS_ERR_INVALID, "shortlist length %d must be a multiple of 32 and >= k=%d", c->kp, k);
+    if (o.kp <= 0 && c->kp > 512 && k <= 512) c->kp = std::max(round16(k), 32);  // no margin at the limit
+    if (c->kp % 16 != 0 || c->kp < k || c->kp < 32)
+        return set_error(KNNS_ERR_INVALID, "shortlist length %d must be a multiple of 16, >= 32 and >= k=%d", c->kp,
+                         k);
     int algo = o.algo;
     const int dp = (int)round32(D);
     const bool tc_ok = E.cc >= 100 && dp <= kMaxDpTC;
     if (algo == KNNS_ALGO_AUTO) {
-        if (tc_ok && c->kp > kMaxKpTC && round32(k) <= kMaxKpTC && o.kp <= 0) c->kp = round32(k);
+        if (tc_ok && c->kp > kMaxKpTC && round16(k) <= kMaxKpTC && o.kp <= 0) c->kp = std::max(round16(k), 32);
         algo = (tc_ok && c->kp <= kMaxKpTC) ? KNNS_ALGO_TC : KNNS_ALGO_SIMT;
     }
     if (algo == KNNS_ALGO_TC) {
@@ -244,6 +247,9 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     rc = E.part.ensure((size_t)c.splits * Q * c.kp * sizeof(uint64_t));
     if (rc) return rc;
     ws += E.part.cap;
+    rc = E.thr.ensure(Q * sizeof(uint32_t));
+    if (rc) return rc;
+    ws += E.thr.cap;
     if (!c.rerank) {
         rc = E.qn.ensure(Q * sizeof(float));
         if (rc) return rc;
@@ -254,7 +260,9 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         if (rc) return rc;
         rc = E.lo.ensure((size_t)N * c.dp * sizeof(float));
         if (rc) return rc;
-        ws += E.hi.cap + E.lo.cap;
+        rc = E.loflags.ensure(((size_t)cdiv(N, 128) + 1) * sizeof(uint32_t));
+        if (rc) return rc;
+        ws += E.hi.cap + E.lo.cap + E.loflags.cap;
     }
 
     KNN_CUDA(cudaStreamWaitEvent(s, E.last_done, 0));
@@ -270,8 +278,13 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         ++launches;
     }
     uint64_t* part = (uint64_t*)E.part.p;
+    uint32_t* thr_g = (uint32_t*)E.thr.p;
+    KNN_CUDA(cudaMemsetAsync(thr_g, 0xFF, Q * sizeof(uint32_t), s));
     if (c.algo == KNNS_ALGO_TC) {
-        KNN_CUDA(launch_split(corpus, N, ldc, D, c.dp, (float*)E.hi.p, (float*)E.lo.p, s));
+        uint32_t* flags = (uint32_t*)E.loflags.p;
+        uint32_t* any_lo = flags + cdiv(N, 128);
+        KNN_CUDA(cudaMemsetAsync(any_lo, 0, sizeof(uint32_t), s));
+        KNN_CUDA(launch_split(corpus, N, ldc, D, c.dp, (float*)E.hi.p, (float*)E.lo.p, flags, any_lo, s));
         ++launches;
     }
     if (tv[1]) KNN_CUDA(cudaEventRecord(tv[1], s));
@@ -289,6 +302,9 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         a.N = N;
         a.split_len = c.split_len;
         a.part = part;
+        a.thr_g = thr_g;
+        a.lo_flags = (const uint32_t*)E.loflags.p;
+        a.corpus_any_lo = (const uint32_t*)E.loflags.p + cdiv(N, 128);
         a.dump = nullptr;
         a.err = (int*)E.err.p;
         a.D = D;
@@ -297,7 +313,8 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         a.stages = c.stages;
         KNN_CUDA(launch_tc(a, c.splits, s));
     } else {
-        KNN_CUDA(launch_simt(corpus, N, ldc, cn, queries, Q, ldq, D, c.kp, c.qtile, c.split_len, c.splits, part, s));
+        KNN_CUDA(launch_simt(corpus, N, ldc, cn, queries, Q, ldq, D, c.kp, c.qtile, c.split_len, c.splits, part,
+                             thr_g, s));
     }
     ++launches;
     if (tv[2]) KNN_CUDA(cudaEventRecord(tv[2], s));
@@ -508,7 +525,7 @@ int knns_debug_tc_dot_tile(const float* corpus, int64_t N, const float* queries,
     if ((rc = E->part.ensure((size_t)std::min<int64_t>(Q, kTileQ) * 32 * 8))) return rc;
     KNN_CUDA(cudaStreamWaitEvent(s, E->last_done, 0));
     KNN_CUDA(launch_norms(corpus, n_use, D, D, (float*)E->cn.p, n_pad, s));
-    KNN_CUDA(launch_split(corpus, n_use, D, D, dp, (float*)E->hi.p, (float*)E->lo.p, s));
+    KNN_CUDA(launch_split(corpus, n_use, D, D, dp, (float*)E->hi.p, (float*)E->lo.p, nullptr, nullptr, s));
     TcArgs a;
     memset(&a, 0, sizeof(a));
     if ((rc = encode_rows(&a.tm_hi, (const float*)E->hi.p, n_use, dp))) return rc;
@@ -520,6 +537,9 @@ int knns_debug_tc_dot_tile(const float* corpus, int64_t N, const float* queries,
     a.N = n_use;
     a.split_len = kTileN;
     a.part = (uint64_t*)E->part.p;
+    a.thr_g = nullptr;
+    a.lo_flags = nullptr;
+    a.corpus_any_lo = nullptr;
     a.dump = dump;
     a.err = (int*)E->err.p;
     a.D = D;

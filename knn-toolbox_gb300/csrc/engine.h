@@ -7,7 +7,7 @@
 #include <vector>
 #include <cuda_runtime.h>
 
-#include "../../include/knn_gb300.h"
+#include "knn_gb300.h"
 
 namespace knn {
 
@@ -35,7 +35,7 @@ struct Engine {
     int cc = 0;
     std::mutex mu;
     cudaEvent_t last_done = nullptr;
-    DevBuf cn, qn, part, hi, lo, err;
+    DevBuf cn, qn, part, hi, lo, err, thr, loflags;
     DevBuf in_corpus, in_queries, out_dist, out_idx;
     // stage timing: 4 events per timed search (start, after prep, after fused, end)
     std::vector<cudaEvent_t> tev;

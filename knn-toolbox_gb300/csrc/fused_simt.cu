@@ -33,7 +33,7 @@ template <int QPB>
 __global__ void __launch_bounds__(kThreads)
 simt_kernel(const float* __restrict__ corpus, int64_t N, int64_t ldc, const float* __restrict__ cn,
             const float* __restrict__ queries, int64_t Q, int64_t ldq, int D, int kp,
-            int64_t split_len, uint64_t* __restrict__ part)
+            int64_t split_len, uint64_t* __restrict__ part, uint32_t* __restrict__ thr_g_all)
 {
     constexpr int RQ = QPB / 16;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -47,9 +47,8 @@ simt_kernel(const float* __restrict__ corpus, int64_t N, int64_t ldc, const floa
     v.kp_pitch = kp;
     v.buf_pitch = QPB + 1;
     v.buf = sl + (size_t)QPB * kp;
-    v.scratch = v.buf + (size_t)kBufCap * (QPB + 1);
 
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tid = threadIdx.x;
     const int64_t q0 = (int64_t)blockIdx.x * QPB;
     const int64_t n_begin = (int64_t)blockIdx.y * split_len;
     const int64_t n_end = min(N, n_begin + split_len);
@@ -58,8 +57,10 @@ simt_kernel(const float* __restrict__ corpus, int64_t N, int64_t ldc, const floa
     __syncthreads();
 
     const bool owner = tid < QPB;
+    const int64_t q = q0 + tid;
     int cnt = 0;
-    float thr = __int_as_float(0x7f800000);
+    float thr = q < Q ? __int_as_float(0x7f800000) : -__int_as_float(0x7f800000);
+    uint32_t* thr_g = (owner && q < Q) ? thr_g_all : nullptr;
     const int tx = tid & 15, ty = tid >> 4;
 
     for (int64_t n0 = n_begin; n0 < n_end; n0 += kNT) {
@@ -112,33 +113,32 @@ simt_kernel(const float* __restrict__ corpus, int64_t N, int64_t ldc, const floa
             }
         __syncthreads();
         if (owner) {
-            uint64_t* scr = v.scratch + warp * 32;
-            for (int j0 = 0; j0 < kNT; j0 += kChunk) {
-                maybe_flush(v, tid, cnt, thr, scr);
-#pragma unroll 4
-                for (int j = j0; j < j0 + kChunk; ++j)
-                    offer(v, tid, cnt, thr, tile[tid * (kNT + 1) + j], (uint32_t)(n0 + j));
+            const float thr_glob = thr_g ? shared_thr_of(__ldcg(thr_g + q)) : __int_as_float(0x7f800000);
+#pragma unroll 1
+            for (int j0 = 0; j0 < kNT; j0 += 32) {
+                float key[32];
+#pragma unroll
+                for (int j = 0; j < 32; ++j) key[j] = tile[tid * (kNT + 1) + j0 + j];
+                offer32(v, tid, cnt, thr, thr_glob, key, (uint32_t)(n0 + j0), thr_g, q);
             }
         }
         __syncthreads();
     }
-    if (owner) flush_all(v, tid, cnt, thr, v.scratch + warp * 32);
+    if (owner) flush_all(v, tid, cnt, thr);
     __syncthreads();
     uint64_t* out = part + ((size_t)blockIdx.y * Q + q0) * kp;
     const int64_t nq = min((int64_t)QPB, Q - q0);
     for (int64_t i = tid; i < nq * kp; i += kThreads) out[i] = v.list[i];
-    (void)lane;
 }
 
 size_t simt_smem_bytes(int qpb, int kp)
 {
-    return ((simt_gemm_bytes(qpb) + 15) & ~size_t(15)) + (size_t)qpb * kp * 8 +
-           (size_t)kBufCap * (qpb + 1) * 8 + (size_t)(kThreads / 32) * 32 * 8;
+    return ((simt_gemm_bytes(qpb) + 15) & ~size_t(15)) + (size_t)qpb * kp * 8 + (size_t)kBufCap * (qpb + 1) * 8;
 }
 
 cudaError_t launch_simt(const float* corpus, int64_t N, int64_t ldc, const float* cn,
                         const float* queries, int64_t Q, int64_t ldq, int D, int kp, int qpb,
-                        int64_t split_len, int splits, uint64_t* part, cudaStream_t s)
+                        int64_t split_len, int splits, uint64_t* part, uint32_t* thr_g, cudaStream_t s)
 {
     size_t smem = simt_smem_bytes(qpb, kp);
     dim3 grid((unsigned)((Q + qpb - 1) / qpb), (unsigned)splits);
@@ -147,13 +147,13 @@ cudaError_t launch_simt(const float* corpus, int64_t N, int64_t ldc, const float
                                              (int)smem);
         if (e != cudaSuccess) return e;
         simt_kernel<128><<<grid, kThreads, smem, s>>>(corpus, N, ldc, cn, queries, Q, ldq, D, kp,
-                                                      split_len, part);
+                                                      split_len, part, thr_g);
     } else {
         cudaError_t e = cudaFuncSetAttribute(simt_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
         simt_kernel<32><<<grid, kThreads, smem, s>>>(corpus, N, ldc, cn, queries, Q, ldq, D, kp,
-                                                     split_len, part);
+                                                     split_len, part, thr_g);
     }
     return cudaGetLastError();
 }

@@ -8,18 +8,23 @@
 //
 // q.c runs as 3xTF32: with x = hi + lo (hi = tf32(x), lo = tf32(x - hi)),
 // q.c ~= qhi.chi + qhi.clo + qlo.chi, accumulated in FP32 by
-// tcgen05.mma.kind::tf32.  For integer data below 2^11 lo is zero and the
-// products and sums are exact, so the keys equal the oracle's bit for bit.
+// tcgen05.mma.kind::tf32.  A corpus tile (or the query tile) whose low part
+// is all zero skips its correction product: it would add exact zeros, so the
+// accumulator is bit-identical either way.  For integer data below 2^11 every
+// low part is zero and the products and sums are exact, so the keys equal the
+// oracle's bit for bit.
 //
 // Warp roles (192 threads):
-//   warp 0      TMA producer: corpus hi/lo K-chunks (128 rows x 32 fp32,
-//               128-byte swizzle) into a `stages`-deep shared-memory ring;
+//   warp 0      producer: per tile, the corpus norms (1-D bulk copy into a
+//               4-slot ring) and the corpus hi/lo K-chunks (2-D TMA, 128 rows x
+//               32 fp32, 128-byte swizzle) into a shared-memory ring;
 //   warp 1      TMEM owner + MMA issuer: A (this CTA's queries, hi and lo)
 //               sits in TMEM columns [0, 2*dp); two 128-column FP32
 //               accumulators at columns 256 and 384 alternate between tiles;
 //   warps 2..5  epilogue: thread = query (= TMEM lane); loads its query into
-//               TMEM, then per tile reads its 128 dot products (tcgen05.ld),
-//               forms key = ||c||^2 - 2 q.c and runs the shortlist filter.
+//               TMEM, then per tile reads its 128 dot products (tcgen05.ld,
+//               double-buffered), forms key = ||c||^2 - 2 q.c and runs the
+//               shortlist filter.
 // Every mbarrier wait is bounded; on timeout the kernel records an error
 // code in the device error word and winds down without hanging the GPU.
 #include <cstdint>
@@ -33,7 +38,12 @@ namespace knn {
 
 namespace {
 constexpr int kTcThreads = 192;
-constexpr uint32_t kStageBytes = 2u * kTileN * 128u;   // hi + lo, 128 rows x 128 B each
+constexpr uint32_t kHalfBytes = kTileN * 128u;     // one operand chunk: 128 rows x 32 fp32 (16 KB)
+constexpr uint32_t kStageBytes = 2u * kHalfBytes;  // hi + lo
+constexpr int kMaxStages = 4;                      // hi+lo stages (8 hi-only slots)
+constexpr int kNormSlots = 4;                      // tiles of corpus norms in flight
+constexpr uint32_t kNormBytes = kNormSlots * kTileN * 4u;
+constexpr uint32_t kCtrlBytes = 512;               // barriers and flags (284 bytes used)
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kAccCol = 256;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
@@ -49,37 +59,39 @@ __device__ __forceinline__ float tf32_rne_dev(float x)
 }
 
 struct TcSmem {
-    unsigned char* stages;   // [stages][hi 16K | lo 16K], 1024-aligned
-    uint64_t* full;
-    uint64_t* empty;
-    uint64_t* accf;
-    uint64_t* acce;
+    unsigned char* ring;      // operand slots, 1024-aligned
+    float* norms;             // [kNormSlots][128]
+    uint64_t* full;           // [2 * kMaxStages]
+    uint64_t* empty;          // [2 * kMaxStages]
+    uint64_t* accf;           // [2]
+    uint64_t* acce;           // [2]
+    uint64_t* nfull;          // [kNormSlots]
+    uint64_t* nempty;         // [kNormSlots]
     uint64_t* aready;
     uint64_t* drain;
     uint32_t* tmem_holder;
     volatile int* abort;
+    volatile uint32_t* alo_flag;  // 1 when any query of this tile has a nonzero TF32 low part
+    volatile uint32_t* stage_lo;  // [2 * kMaxStages] 1 when the slot carries the chunk's low part
     uint64_t* list;
     uint64_t* buf;
-    uint64_t* scratch;
 };
 
 __host__ __device__ inline size_t tc_list_offset(int stages)
 {
-    // stages, then 256 bytes of barriers / holders
-    return (size_t)stages * kStageBytes + 256;
+    return (size_t)stages * kStageBytes + kNormBytes + kCtrlBytes;
 }
 }  // namespace
 
 size_t tc_smem_bytes(int kp, int stages)
 {
-    return 1024 + tc_list_offset(stages) + (size_t)kTileQ * kp * 8 + (size_t)kBufCap * (kTileQ + 1) * 8 +
-           (size_t)4 * 32 * 8;
+    return tc_list_offset(stages) + (size_t)kTileQ * kp * 8 + (size_t)kBufCap * (kTileQ + 1) * 8;
 }
 
 int tc_max_stages(int kp)
 {
     int best = 0;
-    for (int s = 1; s <= 6; ++s)
+    for (int s = 1; s <= kMaxStages; ++s)
         if (tc_smem_bytes(kp, s) <= 232448) best = s;
     return best;
 }
@@ -98,27 +110,60 @@ __device__ __forceinline__ bool tc_wait(const TcArgs& a, const TcSmem& s, uint64
     return false;
 }
 
+// key = ||c||^2 - 2 q.c for 32 columns, then the shortlist filter
+__device__ __forceinline__ void tc_offer_chunk(const ShortlistView& v, int row, int& cnt, float& thr_local,
+                                               float thr_glob, const float (&vals)[32], const float* nrm,
+                                               uint32_t nbase, uint32_t* thr_g, int64_t q)
+{
+    const float4* n4 = reinterpret_cast<const float4*>(nrm);
+    float key[32];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        const float4 c4 = n4[u];
+        key[4 * u + 0] = __fmaf_rn(-2.0f, vals[4 * u + 0], c4.x);
+        key[4 * u + 1] = __fmaf_rn(-2.0f, vals[4 * u + 1], c4.y);
+        key[4 * u + 2] = __fmaf_rn(-2.0f, vals[4 * u + 2], c4.z);
+        key[4 * u + 3] = __fmaf_rn(-2.0f, vals[4 * u + 3], c4.w);
+    }
+    offer32(v, row, cnt, thr_local, thr_glob, key, nbase, thr_g, q);
+}
+
 __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant__ TcArgs a)
 {
-    extern __shared__ __align__(1024) unsigned char smem_raw[];
-    const uint32_t raw_addr = ptx::smem_u32(smem_raw);
-    unsigned char* sm = smem_raw + ((1024u - (raw_addr & 1023u)) & 1023u);
+    extern __shared__ __align__(1024) unsigned char sm[];
+    // The operand ring needs 1024-byte alignment (128-byte swizzle atoms).
+    // The dynamic shared-memory window starts 1024-aligned; refuse to run otherwise.
+    if ((ptx::smem_u32(sm) & 1023u) != 0u) {
+        if (threadIdx.x == 0) atomicCAS(a.err, 0, kDevMisaligned);
+        return;
+    }
 
     const int stages = a.stages;
+    // Ring layout: with a low part anywhere in the corpus, `stages` slots of
+    // hi+lo; otherwise twice as many hi-only slots (deeper prefetch).
+    const bool ring_lo = a.corpus_any_lo == nullptr || *a.corpus_any_lo != 0u;
+    const int nslot = ring_lo ? stages : 2 * stages;
+    const uint32_t slot_bytes = ring_lo ? kStageBytes : kHalfBytes;
+
     TcSmem s;
-    s.stages = sm;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + (size_t)stages * kStageBytes);
+    s.ring = sm;
+    s.norms = reinterpret_cast<float*>(sm + (size_t)stages * kStageBytes);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + (size_t)stages * kStageBytes + kNormBytes);
     s.full = bars;
-    s.empty = bars + stages;
-    s.accf = bars + 2 * stages;
+    s.empty = bars + 2 * kMaxStages;
+    s.accf = bars + 4 * kMaxStages;
     s.acce = s.accf + 2;
-    s.aready = s.acce + 2;
+    s.nfull = s.acce + 2;
+    s.nempty = s.nfull + kNormSlots;
+    s.aready = s.nempty + kNormSlots;
     s.drain = s.aready + 1;
-    s.tmem_holder = reinterpret_cast<uint32_t*>(s.drain + 1);
-    s.abort = reinterpret_cast<volatile int*>(s.tmem_holder + 1);
+    uint32_t* words = reinterpret_cast<uint32_t*>(s.drain + 1);
+    s.tmem_holder = words;
+    s.abort = reinterpret_cast<volatile int*>(words + 1);
+    s.alo_flag = words + 2;
+    s.stage_lo = words + 3;
     s.list = reinterpret_cast<uint64_t*>(sm + tc_list_offset(stages));
     s.buf = s.list + (size_t)kTileQ * a.kp;
-    s.scratch = s.buf + (size_t)kBufCap * (kTileQ + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int64_t q0 = (int64_t)blockIdx.x * kTileQ;
@@ -128,7 +173,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
     const int nchunks = a.dp / kChunkK;
 
     if (tid == 0) {
-        for (int i = 0; i < stages; ++i) {
+        for (int i = 0; i < nslot; ++i) {
             ptx::mbar_init(&s.full[i], 1);
             ptx::mbar_init(&s.empty[i], 1);
         }
@@ -136,9 +181,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
             ptx::mbar_init(&s.accf[b], 1);
             ptx::mbar_init(&s.acce[b], 4);
         }
+        for (int b = 0; b < kNormSlots; ++b) {
+            ptx::mbar_init(&s.nfull[b], 1);
+            ptx::mbar_init(&s.nempty[b], 4);
+        }
         ptx::mbar_init(s.aready, 4 * 32);
         ptx::mbar_init(s.drain, 1);
         *s.abort = 0;
+        *s.alo_flag = 0;
         ptx::fence_mbar_init();
         ptx::tma_prefetch_desc(&a.tm_hi);
         ptx::tma_prefetch_desc(&a.tm_lo);
@@ -158,23 +208,35 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
         if (lane == 0) {
             int it = 0;
             bool ok = true;
+            const int64_t tile0 = n_begin / kTileN;
             for (int t = 0; t < ntiles && ok; ++t) {
-                const int y = (int)(n_begin + (int64_t)t * kTileN);
+                const int64_t n0 = n_begin + (int64_t)t * kTileN;
+                // corpus norms of this tile (the array is padded with +inf to a multiple of 128)
+                const int ns = t % kNormSlots;
+                if (!tc_wait(a, s, &s.nempty[ns], ((uint32_t)(t / kNormSlots) & 1u) ^ 1u, kDevTimeoutProducer)) {
+                    ok = false;
+                    break;
+                }
+                ptx::mbar_arrive_expect_tx(&s.nfull[ns], kTileN * 4u);
+                ptx::bulk_load(s.norms + ns * kTileN, a.cn + n0, kTileN * 4u, &s.nfull[ns]);
+                // corpus tiles whose TF32 low part is zero skip the lo copy and its products
+                const uint32_t need_lo = ring_lo ? (a.lo_flags ? __ldg(a.lo_flags + tile0 + t) : 1u) : 0u;
                 for (int c = 0; c < nchunks; ++c, ++it) {
-                    const int st = it % stages;
-                    const uint32_t ph = (uint32_t)(it / stages) & 1u;
+                    const int st = it % nslot;
+                    const uint32_t ph = (uint32_t)(it / nslot) & 1u;
                     if (!tc_wait(a, s, &s.empty[st], ph ^ 1u, kDevTimeoutProducer)) { ok = false; break; }
-                    unsigned char* dst = s.stages + (size_t)st * kStageBytes;
-                    ptx::mbar_arrive_expect_tx(&s.full[st], kStageBytes);
-                    ptx::tma_load_2d(dst, &a.tm_hi, &s.full[st], c * kChunkK, y);
-                    ptx::tma_load_2d(dst + kStageBytes / 2, &a.tm_lo, &s.full[st], c * kChunkK, y);
+                    unsigned char* dst = s.ring + (size_t)st * slot_bytes;
+                    s.stage_lo[st] = need_lo;  // published by the arrive below
+                    ptx::mbar_arrive_expect_tx(&s.full[st], need_lo ? kStageBytes : kHalfBytes);
+                    ptx::tma_load_2d(dst, &a.tm_hi, &s.full[st], c * kChunkK, (int)n0);
+                    if (need_lo) ptx::tma_load_2d(dst + kHalfBytes, &a.tm_lo, &s.full[st], c * kChunkK, (int)n0);
                 }
             }
             if (!ok) {
                 // let copies already issued land before the CTA winds down
-                const int first = it - stages > 0 ? it - stages : 0;
+                const int first = it - nslot > 0 ? it - nslot : 0;
                 for (int j = first; j < it; ++j)
-                    ptx::mbar_wait(&s.full[j % stages], (uint32_t)(j / stages) & 1u, kTimeoutNs);
+                    ptx::mbar_wait(&s.full[j % nslot], (uint32_t)(j / nslot) & 1u, kTimeoutNs);
             }
         }
     } else if (warp == 1) {
@@ -182,6 +244,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
         if (lane == 0) {
             bool ok = tc_wait(a, s, s.aready, 0, kDevTimeoutAload);
             ptx::tc_fence_after();
+            const uint32_t a_lo = *s.alo_flag;
             int it = 0;
             for (int t = 0; t < ntiles && ok; ++t) {
                 const int b = t & 1;
@@ -190,21 +253,24 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
                 ptx::tc_fence_after();
                 const uint32_t d_tmem = tmem + kAccCol + (uint32_t)b * kTileN;
                 for (int c = 0; c < nchunks; ++c, ++it) {
-                    const int st = it % stages;
-                    const uint32_t ph = (uint32_t)(it / stages) & 1u;
+                    const int st = it % nslot;
+                    const uint32_t ph = (uint32_t)(it / nslot) & 1u;
                     if (!tc_wait(a, s, &s.full[st], ph, kDevTimeoutMma)) { ok = false; break; }
                     ptx::tc_fence_after();
-                    const uint32_t hi_addr = ptx::smem_u32(s.stages + (size_t)st * kStageBytes);
-                    const uint32_t lo_addr = hi_addr + kStageBytes / 2;
+                    const uint32_t b_lo = s.stage_lo[st];
+                    const uint32_t hi_addr = ptx::smem_u32(s.ring + (size_t)st * slot_bytes);
+                    const uint32_t lo_addr = hi_addr + kHalfBytes;
 #pragma unroll
                     for (int kk = 0; kk < kChunkK / 8; ++kk) {
                         const uint64_t dh = ptx::desc_sw128_kmajor(hi_addr + kk * 32);
-                        const uint64_t dl = ptx::desc_sw128_kmajor(lo_addr + kk * 32);
                         const uint32_t ahi = tmem + (uint32_t)(c * kChunkK + kk * 8);
                         const uint32_t alo = ahi + (uint32_t)a.dp;
+                        // an all-zero low part contributes exact zeros: skipping it leaves
+                        // the FP32 accumulator bit-identical
                         ptx::mma_tf32_ts(d_tmem, ahi, dh, kIdesc, (c | kk) != 0);
-                        ptx::mma_tf32_ts(d_tmem, ahi, dl, kIdesc, 1u);
-                        ptx::mma_tf32_ts(d_tmem, alo, dh, kIdesc, 1u);
+                        if (b_lo)
+                            ptx::mma_tf32_ts(d_tmem, ahi, ptx::desc_sw128_kmajor(lo_addr + kk * 32), kIdesc, 1u);
+                        if (a_lo) ptx::mma_tf32_ts(d_tmem, alo, dh, kIdesc, 1u);
                     }
                     ptx::mma_commit(&s.empty[st]);
                 }
@@ -224,14 +290,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
         ShortlistView v;
         v.list = s.list;
         v.buf = s.buf;
-        v.scratch = s.scratch;
         v.kp = a.kp;
         v.kp_pitch = a.kp;
         v.buf_pitch = kTileQ + 1;
-        uint64_t* scr = s.scratch + (warp - 2) * 32;
 
         // A operand: this thread's query row, split into TF32 hi/lo, into TMEM
         const float* qrow = a.queries + (q < a.Q ? q : 0) * a.ldq;
+        uint32_t any_lo = 0;
         for (int c = 0; c < nchunks; ++c) {
             float hi[32], lo[32];
 #pragma unroll
@@ -240,56 +305,73 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
                 const float x = (q < a.Q && d < a.D) ? __ldg(qrow + d) : 0.f;
                 hi[u] = tf32_rne_dev(x);
                 lo[u] = tf32_rne_dev(__fsub_rn(x, hi[u]));
+                any_lo |= (lo[u] != 0.f) ? 1u : 0u;
             }
             __syncwarp();
             ptx::tmem_st32(tmem + lane_base + (uint32_t)(c * kChunkK), hi);
             ptx::tmem_st32(tmem + lane_base + (uint32_t)(a.dp + c * kChunkK), lo);
         }
         ptx::tmem_wait_st();
+        if (any_lo) atomicOr(const_cast<uint32_t*>(s.alo_flag), 1u);
         ptx::tc_fence_before();
         ptx::mbar_arrive(s.aready);
 
         int cnt = 0;
-        float thr = __int_as_float(0x7f800000);
+        // padding rows of the last query tile accept nothing
+        float thr_local = q < a.Q ? __int_as_float(0x7f800000) : -__int_as_float(0x7f800000);
+        uint32_t* thr_g = q < a.Q ? a.thr_g : nullptr;
+        uint32_t g_pending = thr_g ? __ldcg(thr_g + q) : 0xFFFFFFFFu;
+        const bool dump = a.dump != nullptr && blockIdx.x == 0 && blockIdx.y == 0;
         for (int t = 0; t < ntiles; ++t) {
             const int b = t & 1;
             const uint32_t use = (uint32_t)(t >> 1);
             // warp-uniform outcome: tcgen05.ld below is warp-collective
-            const bool ok = __all_sync(0xffffffffu, tc_wait(a, s, &s.accf[b], use & 1u, kDevTimeoutEpilogue));
-            if (!ok) break;
+            const int ns = t % kNormSlots;
+            const bool ok = tc_wait(a, s, &s.accf[b], use & 1u, kDevTimeoutEpilogue) &&
+                            tc_wait(a, s, &s.nfull[ns], (uint32_t)(t / kNormSlots) & 1u, kDevTimeoutEpilogue);
+            if (!__all_sync(0xffffffffu, ok)) break;
             ptx::tc_fence_after();
-            const int64_t n0 = n_begin + (int64_t)t * kTileN;
+            // shared threshold loaded one tile ago; fetch the next one now
+            const float thr_glob = shared_thr_of(g_pending);
+            if (thr_g) g_pending = __ldcg(thr_g + q);
+            const uint32_t nb = (uint32_t)(n_begin + (int64_t)t * kTileN);
+            const float* nrm = s.norms + ns * kTileN;
             const uint32_t tb = tmem + kAccCol + (uint32_t)b * kTileN + lane_base;
-#pragma unroll 1
-            for (int cc = 0; cc < kTileN / 32; ++cc) {
-                float vals[32];
-                __syncwarp();
-                ptx::tmem_ld32(tb + (uint32_t)(cc * 32), vals);
-                ptx::tmem_wait_ld();
-                if (cc == kTileN / 32 - 1) {
-                    ptx::tc_fence_before();
-                    __syncwarp();
-                    if (lane == 0) ptx::mbar_arrive(&s.acce[b]);
-                }
-                if (a.dump != nullptr && blockIdx.x == 0 && blockIdx.y == 0 && t == 0) {
-#pragma unroll
-                    for (int u = 0; u < 32; ++u) a.dump[row * kTileN + cc * 32 + u] = vals[u];
-                }
-                const float* cnp = a.cn + n0 + cc * 32;
-                const uint32_t nb = (uint32_t)(n0 + cc * 32);
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    maybe_flush(v, row, cnt, thr, scr);
-#pragma unroll
-                    for (int u = 0; u < 16; ++u) {
-                        const int j = h * 16 + u;
-                        const float key = __fmaf_rn(-2.0f, vals[j], __ldg(cnp + j));
-                        offer(v, row, cnt, thr, key, nb + (uint32_t)j);
-                    }
-                }
-            }
+            // four 32-column chunks; the next chunk's TMEM load overlaps this chunk's filter
+            float va[32], vb[32];
+            __syncwarp();
+            ptx::tmem_ld32(tb, va);
+            ptx::tmem_wait_ld_regs(va);
+            __syncwarp();
+            ptx::tmem_ld32(tb + 32, vb);
+            if (dump && t == 0)
+                for (int u = 0; u < 32; ++u) a.dump[row * kTileN + u] = va[u];
+            tc_offer_chunk(v, row, cnt, thr_local, thr_glob, va, nrm, nb, thr_g, q);
+            ptx::tmem_wait_ld_regs(vb);
+            __syncwarp();
+            ptx::tmem_ld32(tb + 64, va);
+            if (dump && t == 0)
+                for (int u = 0; u < 32; ++u) a.dump[row * kTileN + 32 + u] = vb[u];
+            tc_offer_chunk(v, row, cnt, thr_local, thr_glob, vb, nrm + 32, nb + 32, thr_g, q);
+            ptx::tmem_wait_ld_regs(va);
+            __syncwarp();
+            ptx::tmem_ld32(tb + 96, vb);
+            if (dump && t == 0)
+                for (int u = 0; u < 32; ++u) a.dump[row * kTileN + 64 + u] = va[u];
+            tc_offer_chunk(v, row, cnt, thr_local, thr_glob, va, nrm + 64, nb + 64, thr_g, q);
+            ptx::tmem_wait_ld_regs(vb);
+            // accumulator b fully read: hand it back to the MMA issuer
+            ptx::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&s.acce[b]);
+            if (dump && t == 0)
+                for (int u = 0; u < 32; ++u) a.dump[row * kTileN + 96 + u] = vb[u];
+            tc_offer_chunk(v, row, cnt, thr_local, thr_glob, vb, nrm + 96, nb + 96, thr_g, q);
+            // norms slot no longer read by this warp
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&s.nempty[ns]);
         }
-        flush_all(v, row, cnt, thr, scr);
+        flush_all(v, row, cnt, thr_local);
     }
 
     ptx::tc_fence_before();
@@ -307,6 +389,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
 
 cudaError_t launch_tc(const TcArgs& a, int splits, cudaStream_t st)
 {
+    if (a.stages < 1 || a.stages > kMaxStages || a.dp % kChunkK != 0 || a.dp > kMaxDpTC || a.kp % 16 != 0)
+        return cudaErrorInvalidValue;
     const size_t smem = tc_smem_bytes(a.kp, a.stages);
     cudaError_t e = cudaFuncSetAttribute(tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

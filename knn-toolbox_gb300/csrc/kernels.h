@@ -22,18 +22,21 @@ enum DeviceError : int {
     kDevTimeoutMma = 2,
     kDevTimeoutEpilogue = 3,
     kDevTimeoutAload = 4,
+    kDevMisaligned = 5,
 };
 
 cudaError_t launch_norms(const float* x, int64_t n, int64_t ld, int D, float* out, int64_t n_pad,
                          cudaStream_t s);
+// TF32 hi/lo split into [n][dp] arrays; lo_flags[tile of 128 rows] = any lo != 0 (may be null);
+// *any_lo (zeroed by the caller, may be null) becomes 1 when some tile has a low part.
 cudaError_t launch_split(const float* x, int64_t n, int64_t ld, int D, int dp, float* hi, float* lo,
-                         cudaStream_t s);
+                         uint32_t* lo_flags, uint32_t* any_lo, cudaStream_t s);
 
 // CUDA-core FP32 fused distance + shortlist.  qpb in {32, 128}.
 size_t simt_smem_bytes(int qpb, int kp);
 cudaError_t launch_simt(const float* corpus, int64_t N, int64_t ldc, const float* cn,
                         const float* queries, int64_t Q, int64_t ldq, int D, int kp, int qpb,
-                        int64_t split_len, int splits, uint64_t* part, cudaStream_t s);
+                        int64_t split_len, int splits, uint64_t* part, uint32_t* thr_g, cudaStream_t s);
 
 // Tensor-core 3xTF32 fused distance + shortlist (tcgen05, TMA, TMEM).
 struct TcArgs {
@@ -46,6 +49,9 @@ struct TcArgs {
     int64_t N;
     int64_t split_len;        // corpus rows per split, multiple of kTileN
     uint64_t* part;           // [splits][Q][kp]
+    uint32_t* thr_g;          // [Q] shared per-query threshold (order-mapped key), or null
+    const uint32_t* lo_flags; // [ceil(N/128)] 1 when the corpus tile has a nonzero TF32 low part, or null
+    const uint32_t* corpus_any_lo;  // 1 when any corpus tile has a low part (null: assume so)
     float* dump;              // optional: raw dot tile of CTA (0,0), tile 0, [128][128]
     int* err;                 // device error word
     int D;

@@ -50,18 +50,31 @@ __device__ __forceinline__ float tf32_rne(float x)
 }
 
 // hi = tf32(x), lo = tf32(x - hi); rows padded with zeros to dp columns.
-__global__ void split_kernel(const float* __restrict__ x, int64_t n, int64_t ld, int D, int dp,
-                             float* __restrict__ hi, float* __restrict__ lo)
+// One block per 128-row tile; lo_flags[tile] = 1 when any lo in the tile is
+// nonzero (the tensor-core kernel skips the correction products otherwise).
+__global__ void split_tiles_kernel(const float* __restrict__ x, int64_t n, int64_t ld, int D, int dp,
+                                   float* __restrict__ hi, float* __restrict__ lo, uint32_t* __restrict__ lo_flags,
+                                   uint32_t* __restrict__ any_lo)
 {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int64_t total = n * dp;
-    if (i >= total) return;
-    int64_t r = i / dp;
-    int c = (int)(i - r * dp);
-    float v = c < D ? __ldg(x + r * ld + c) : 0.f;
-    float h = tf32_rne(v);
-    hi[i] = h;
-    lo[i] = tf32_rne(__fsub_rn(v, h));
+    const int64_t r0 = (int64_t)blockIdx.x * 128;
+    const int64_t rows = min((int64_t)128, n - r0);
+    const int64_t total = rows * dp;
+    int any = 0;
+    for (int64_t i = threadIdx.x; i < total; i += blockDim.x) {
+        const int64_t r = r0 + i / dp;
+        const int c = (int)(i % dp);
+        const float v = c < D ? __ldg(x + r * ld + c) : 0.f;
+        const float h = tf32_rne(v);
+        const float l = tf32_rne(__fsub_rn(v, h));
+        hi[r * dp + c] = h;
+        lo[r * dp + c] = l;
+        any |= (l != 0.f);
+    }
+    any = __syncthreads_or(any);
+    if (threadIdx.x == 0) {
+        if (lo_flags) lo_flags[blockIdx.x] = any ? 1u : 0u;
+        if (any && any_lo) atomicOr(any_lo, 1u);
+    }
 }
 
 cudaError_t launch_norms(const float* x, int64_t n, int64_t ld, int D, float* out, int64_t n_pad,
@@ -75,13 +88,11 @@ cudaError_t launch_norms(const float* x, int64_t n, int64_t ld, int D, float* ou
 }
 
 cudaError_t launch_split(const float* x, int64_t n, int64_t ld, int D, int dp, float* hi, float* lo,
-                         cudaStream_t s)
+                         uint32_t* lo_flags, uint32_t* any_lo, cudaStream_t s)
 {
-    int64_t total = n * dp;
-    if (total <= 0) return cudaSuccess;
-    int threads = 256;
-    int64_t blocks = (total + threads - 1) / threads;
-    split_kernel<<<(unsigned)blocks, threads, 0, s>>>(x, n, ld, D, dp, hi, lo);
+    if (n <= 0) return cudaSuccess;
+    const int64_t tiles = (n + 127) / 128;
+    split_tiles_kernel<<<(unsigned)tiles, 256, 0, s>>>(x, n, ld, D, dp, hi, lo, lo_flags, any_lo);
     return cudaGetLastError();
 }
 

@@ -188,7 +188,7 @@ def test_invalid_arguments(engine):
         engine.search(c, q, 11)
     assert e.value.code == engine.ERR_INVALID
     with pytest.raises(engine.KnnsError) as e:
-        engine.search(c, q, 4, kp=33)
+        engine.search(c, q, 4, kp=40)
     assert e.value.code == engine.ERR_INVALID
     with pytest.raises(engine.KnnsError) as e:
         engine.search(torch.zeros((600, 256), device="cuda"), torch.zeros((2, 256), device="cuda"), 4,
