@@ -114,24 +114,29 @@ __device__ __forceinline__ int count_not_above(const uint64_t* a, int n, uint64_
     return lo;
 }
 
-// upper_bound over 32 words stored with a stride (in words)
-__device__ __forceinline__ int count_not_above32(const uint64_t* a, int stride, uint64_t x)
+// Candidate buffer layout: slot c of query row ql lives at buf[c * pitch + (ql ^ c)]
+// (pitch = rows per CTA, >= 32).  Appends of one warp (equal c, consecutive ql)
+// and a merge's read of one query's 32 slots are both free of bank conflicts.
+__device__ __forceinline__ int buf_index(int pitch, int c, int ql) { return c * pitch + (ql ^ c); }
+
+// upper_bound over the 32 sorted buffer slots of query row qs
+__device__ __forceinline__ int count_not_above_slots(const uint64_t* buf, int pitch, int qs, uint64_t x)
 {
     int lo = 0, n = 32;
     while (n > 0) {
         int half = n >> 1;
-        if (a[(lo + half) * stride] <= x) { lo += half + 1; n -= half + 1; }
+        if (buf[buf_index(pitch, lo + half, qs)] <= x) { lo += half + 1; n -= half + 1; }
         else n = half;
     }
     return lo;
 }
 
 // Merge 32 sorted words (one per lane, ascending by lane) into the sorted list
-// L[0..kp) in shared memory, keeping the kp smallest.  `sorted` holds the same
-// 32 words in shared memory at stride `stride` (read for the ranks of the list
+// L[0..kp) in shared memory, keeping the kp smallest.  The same 32 words sit
+// sorted in query row qs's buffer slots (read for the ranks of the list
 // entries).  kp is a multiple of 16, at most 512.  Stable: on equal words the
 // buffered word goes first (only sentinels can be equal).
-__device__ __forceinline__ void warp_merge32(uint64_t* L, int kp, uint64_t b, const uint64_t* sorted, int stride)
+__device__ __forceinline__ void warp_merge32(uint64_t* L, int kp, uint64_t b, const uint64_t* buf, int pitch, int qs)
 {
     const int lane = threadIdx.x & 31;
     const int pb = lane + count_less(L, kp, b);
@@ -144,7 +149,7 @@ __device__ __forceinline__ void warp_merge32(uint64_t* L, int kp, uint64_t b, co
         lp[t] = kp;
         if (t < nt && j < kp) {
             lv[t] = L[j];
-            lp[t] = j + count_not_above32(sorted, stride, lv[t]);
+            lp[t] = j + count_not_above_slots(buf, pitch, qs, lv[t]);
         }
     }
     __syncwarp();
@@ -203,42 +208,50 @@ constexpr int kBufCap = 32;   // buffered candidates per query
 
 struct ShortlistView {
     uint64_t* list;     // [nq][kp_pitch]
-    uint64_t* buf;      // [kBufCap][buf_pitch]
+    uint64_t* buf;      // [kBufCap][buf_pitch], slots swizzled (buf_index)
     int kp;
     int kp_pitch;
-    int buf_pitch;      // nq + 1
+    int buf_pitch;      // nq (>= 32)
+};
+
+// Per-lane filter state: entries waiting in the buffer and the key of the kp-th
+// kept entry.  Passed by value so that it stays in registers across calls.
+struct LaneState {
+    int cnt;
+    float thr_local;
 };
 
 // Merge the buffers of every lane in `mask`; lane `ql` is the query row of this lane.
-// Kept out of line: it runs rarely and would otherwise be inlined at every offer site.
-static __device__ __noinline__ void flush_lanes(const ShortlistView& v, unsigned mask, int ql, int& cnt,
-                                                float& thr)
+__device__ __forceinline__ LaneState flush_lanes(const ShortlistView& v, unsigned mask, int ql, LaneState st)
 {
     const int lane = threadIdx.x & 31;
     while (mask) {
         const int src = __ffs(mask) - 1;
         mask &= mask - 1;
-        const int c = __shfl_sync(0xffffffffu, cnt, src);
+        const int c = __shfl_sync(0xffffffffu, st.cnt, src);
         const int qs = __shfl_sync(0xffffffffu, ql, src);
-        uint64_t* col = v.buf + qs;  // this query's buffer column, stride buf_pitch
-        uint64_t b = lane < c ? col[lane * v.buf_pitch] : kSentinel;
+        uint64_t* slot = v.buf + buf_index(v.buf_pitch, lane, qs);
+        uint64_t b = lane < c ? *slot : kSentinel;
         b = warp_sort32(b);
-        col[lane * v.buf_pitch] = b;  // the column now holds the sorted words
+        *slot = b;  // query qs's slots now hold the sorted words
         __syncwarp();
         uint64_t* L = v.list + (size_t)qs * v.kp_pitch;
-        warp_merge32(L, v.kp, b, col, v.buf_pitch);
+        warp_merge32(L, v.kp, b, v.buf, v.buf_pitch, qs);
         if (lane == src) {
-            cnt = 0;
-            thr = thr_of(L[v.kp - 1]);
+            st.cnt = 0;
+            st.thr_local = thr_of(L[v.kp - 1]);
         }
     }
     __syncwarp();
+    return st;
 }
 
-__device__ __forceinline__ void flush_all(const ShortlistView& v, int ql, int& cnt, float& thr)
+// Merge every non-empty buffer of the warp (end of a split).
+static __device__ __noinline__ LaneState flush_all(ShortlistView v, int ql, LaneState st)
 {
-    unsigned m = __ballot_sync(0xffffffffu, cnt > 0);
-    if (m) flush_lanes(v, m, ql, cnt, thr);
+    unsigned m = __ballot_sync(0xffffffffu, st.cnt > 0);
+    if (m) st = flush_lanes(v, m, ql, st);
+    return st;
 }
 
 // Threshold shared by every CTA working on one query (other corpus splits):
@@ -256,40 +269,54 @@ __device__ __forceinline__ void publish_thr(uint32_t* thr_g, int64_t q, float th
     if (thr_g != nullptr && thr_local < __int_as_float(0x7f800000)) atomicMin(thr_g + q, f2ord(thr_local));
 }
 
-// Offer 32 consecutive candidates of this lane's query: keys key[0..31] with
-// corpus indices nbase + j, visited in increasing index.  thr_glob is the
-// decoded shared threshold (+inf when unused).  Buffers that would overflow
-// are merged first; lanes that merged publish their new kp-th key.
-__device__ __forceinline__ void offer32(const ShortlistView& v, int ql, int& cnt, float& thr_local,
-                                        float thr_glob, const float (&key)[32], uint32_t nbase,
-                                        uint32_t* thr_g, int64_t q)
+// Offer 32 consecutive candidates of this lane's query: keys[0..31] (shared
+// memory, this lane's own row) with corpus indices nbase + j, visited in
+// increasing index.  thr_glob is the decoded shared threshold (+inf when
+// unused).  Buffers that would overflow are merged first; lanes that merged
+// publish their new kp-th key.  Called by the whole warp once some lane has a
+// candidate below its threshold; each lane then appends only its own hits.
+static __device__ __noinline__ LaneState offer_staged(ShortlistView v, const float* keys, uint32_t nbase, int ql,
+                                                      LaneState st, float thr_glob, uint32_t* thr_g, int64_t q)
 {
-    float thr = fminf(thr_local, thr_glob);
+    float thr = fminf(st.thr_local, thr_glob);
     uint32_t m = 0;
 #pragma unroll
-    for (int j = 0; j < 32; ++j) m |= (key[j] < thr ? 1u : 0u) << j;
-    if (!__any_sync(0xffffffffu, m != 0u)) return;
-    const bool need = cnt + __popc(m) > kBufCap;
+    for (int j = 0; j < 32; ++j) m |= (keys[j] < thr ? 1u : 0u) << j;
+    const bool need = st.cnt + __popc(m) > kBufCap;
     const unsigned fl = __ballot_sync(0xffffffffu, need);
     if (fl) {
-        flush_lanes(v, fl, ql, cnt, thr_local);
+        st = flush_lanes(v, fl, ql, st);
         if (need) {
-            publish_thr(thr_g, q, thr_local);
-            thr = fminf(thr_local, thr_glob);
+            publish_thr(thr_g, q, st.thr_local);
+            thr = fminf(st.thr_local, thr_glob);
             m = 0;
 #pragma unroll
-            for (int j = 0; j < 32; ++j) m |= (key[j] < thr ? 1u : 0u) << j;
+            for (int j = 0; j < 32; ++j) m |= (keys[j] < thr ? 1u : 0u) << j;
         }
     }
-    if (m) {
+    while (m) {
+        const int j = __ffs(m) - 1;
+        m &= m - 1;
+        v.buf[buf_index(v.buf_pitch, st.cnt, ql)] = pack_key(keys[j], nbase + (uint32_t)j);
+        ++st.cnt;
+    }
+    __syncwarp();
+    return st;
+}
+
+// Minimum of 32 keys (fast rejection: no candidate when min >= threshold).
+__device__ __forceinline__ float min32(const float (&key)[32])
+{
+    float m0 = fminf(key[0], key[1]), m1 = fminf(key[2], key[3]), m2 = fminf(key[4], key[5]),
+          m3 = fminf(key[6], key[7]);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-            if ((m >> j) & 1u) {
-                v.buf[cnt * v.buf_pitch + ql] = pack_key(key[j], nbase + (uint32_t)j);
-                ++cnt;
-            }
-        }
+    for (int j = 8; j < 32; j += 4) {
+        m0 = fminf(m0, key[j]);
+        m1 = fminf(m1, key[j + 1]);
+        m2 = fminf(m2, key[j + 2]);
+        m3 = fminf(m3, key[j + 3]);
     }
+    return fminf(fminf(m0, m1), fminf(m2, m3));
 }
 
 }  // namespace knn

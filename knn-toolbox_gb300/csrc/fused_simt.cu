@@ -45,7 +45,7 @@ simt_kernel(const float* __restrict__ corpus, int64_t N, int64_t ldc, const floa
     v.list = sl;
     v.kp = kp;
     v.kp_pitch = kp;
-    v.buf_pitch = QPB + 1;
+    v.buf_pitch = QPB;
     v.buf = sl + (size_t)QPB * kp;
 
     const int tid = threadIdx.x;
@@ -58,8 +58,7 @@ simt_kernel(const float* __restrict__ corpus, int64_t N, int64_t ldc, const floa
 
     const bool owner = tid < QPB;
     const int64_t q = q0 + tid;
-    int cnt = 0;
-    float thr = q < Q ? __int_as_float(0x7f800000) : -__int_as_float(0x7f800000);
+    LaneState st{0, q < Q ? __int_as_float(0x7f800000) : -__int_as_float(0x7f800000)};
     uint32_t* thr_g = (owner && q < Q) ? thr_g_all : nullptr;
     const int tx = tid & 15, ty = tid >> 4;
 
@@ -116,15 +115,18 @@ simt_kernel(const float* __restrict__ corpus, int64_t N, int64_t ldc, const floa
             const float thr_glob = thr_g ? shared_thr_of(__ldcg(thr_g + q)) : __int_as_float(0x7f800000);
 #pragma unroll 1
             for (int j0 = 0; j0 < kNT; j0 += 32) {
+                const float* row = tile + tid * (kNT + 1) + j0;
                 float key[32];
 #pragma unroll
-                for (int j = 0; j < 32; ++j) key[j] = tile[tid * (kNT + 1) + j0 + j];
-                offer32(v, tid, cnt, thr, thr_glob, key, (uint32_t)(n0 + j0), thr_g, q);
+                for (int j = 0; j < 32; ++j) key[j] = row[j];
+                const float thr = fminf(st.thr_local, thr_glob);
+                if (__any_sync(0xffffffffu, min32(key) < thr))
+                    st = offer_staged(v, row, (uint32_t)(n0 + j0), tid, st, thr_glob, thr_g, q);
             }
         }
         __syncthreads();
     }
-    if (owner) flush_all(v, tid, cnt, thr);
+    if (owner) st = flush_all(v, tid, st);
     __syncthreads();
     uint64_t* out = part + ((size_t)blockIdx.y * Q + q0) * kp;
     const int64_t nq = min((int64_t)QPB, Q - q0);
@@ -133,7 +135,7 @@ simt_kernel(const float* __restrict__ corpus, int64_t N, int64_t ldc, const floa
 
 size_t simt_smem_bytes(int qpb, int kp)
 {
-    return ((simt_gemm_bytes(qpb) + 15) & ~size_t(15)) + (size_t)qpb * kp * 8 + (size_t)kBufCap * (qpb + 1) * 8;
+    return ((simt_gemm_bytes(qpb) + 15) & ~size_t(15)) + (size_t)qpb * kp * 8 + (size_t)kBufCap * qpb * 8;
 }
 
 cudaError_t launch_simt(const float* corpus, int64_t N, int64_t ldc, const float* cn,

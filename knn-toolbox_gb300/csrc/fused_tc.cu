@@ -43,7 +43,9 @@ constexpr uint32_t kStageBytes = 2u * kHalfBytes;  // hi + lo
 constexpr int kMaxStages = 4;                      // hi+lo stages (8 hi-only slots)
 constexpr int kNormSlots = 4;                      // tiles of corpus norms in flight
 constexpr uint32_t kNormBytes = kNormSlots * kTileN * 4u;
-constexpr uint32_t kCtrlBytes = 512;               // barriers and flags (284 bytes used)
+constexpr uint32_t kCtrlBytes = 320;               // barriers and flags (284 bytes used)
+constexpr int kStagePitch = 33;                    // staged keys: [4 warps][32 lanes][33 floats]
+constexpr uint32_t kKeyStageBytes = 4u * 32u * kStagePitch * 4u;
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kAccCol = 256;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
@@ -75,6 +77,7 @@ struct TcSmem {
     volatile uint32_t* stage_lo;  // [2 * kMaxStages] 1 when the slot carries the chunk's low part
     uint64_t* list;
     uint64_t* buf;
+    float* keystage;
 };
 
 __host__ __device__ inline size_t tc_list_offset(int stages)
@@ -85,7 +88,7 @@ __host__ __device__ inline size_t tc_list_offset(int stages)
 
 size_t tc_smem_bytes(int kp, int stages)
 {
-    return tc_list_offset(stages) + (size_t)kTileQ * kp * 8 + (size_t)kBufCap * (kTileQ + 1) * 8;
+    return tc_list_offset(stages) + (size_t)kTileQ * kp * 8 + (size_t)kBufCap * kTileQ * 8 + kKeyStageBytes;
 }
 
 int tc_max_stages(int kp)
@@ -110,13 +113,10 @@ __device__ __forceinline__ bool tc_wait(const TcArgs& a, const TcSmem& s, uint64
     return false;
 }
 
-// key = ||c||^2 - 2 q.c for 32 columns, then the shortlist filter
-__device__ __forceinline__ void tc_offer_chunk(const ShortlistView& v, int row, int& cnt, float& thr_local,
-                                               float thr_glob, const float (&vals)[32], const float* nrm,
-                                               uint32_t nbase, uint32_t* thr_g, int64_t q)
+// key = ||c||^2 - 2 q.c for 32 columns (norms from shared memory)
+__device__ __forceinline__ void tc_keys(const float (&vals)[32], const float* nrm, float (&key)[32])
 {
     const float4* n4 = reinterpret_cast<const float4*>(nrm);
-    float key[32];
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
         const float4 c4 = n4[u];
@@ -125,7 +125,22 @@ __device__ __forceinline__ void tc_offer_chunk(const ShortlistView& v, int row, 
         key[4 * u + 2] = __fmaf_rn(-2.0f, vals[4 * u + 2], c4.z);
         key[4 * u + 3] = __fmaf_rn(-2.0f, vals[4 * u + 3], c4.w);
     }
-    offer32(v, row, cnt, thr_local, thr_glob, key, nbase, thr_g, q);
+}
+
+// One 32-column chunk: keys, their minimum and one vote; when some lane of the
+// warp has a candidate below its threshold, the keys are staged in this lane's
+// shared-memory row and the full filter runs out of line.  No TMEM load may be
+// outstanding when the slow path is entered.
+__device__ __forceinline__ bool tc_chunk_hot(const float (&vals)[32], const float* nrm, float thr, float (&key)[32])
+{
+    tc_keys(vals, nrm, key);
+    return __any_sync(0xffffffffu, min32(key) < thr);
+}
+
+__device__ __forceinline__ void stage_keys(float* srow, const float (&key)[32])
+{
+#pragma unroll
+    for (int j = 0; j < 32; ++j) srow[j] = key[j];
 }
 
 __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant__ TcArgs a)
@@ -164,6 +179,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
     s.stage_lo = words + 3;
     s.list = reinterpret_cast<uint64_t*>(sm + tc_list_offset(stages));
     s.buf = s.list + (size_t)kTileQ * a.kp;
+    s.keystage = reinterpret_cast<float*>(s.buf + (size_t)kBufCap * kTileQ);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int64_t q0 = (int64_t)blockIdx.x * kTileQ;
@@ -292,7 +308,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
         v.buf = s.buf;
         v.kp = a.kp;
         v.kp_pitch = a.kp;
-        v.buf_pitch = kTileQ + 1;
+        v.buf_pitch = kTileQ;
+        float* srow = s.keystage + ((warp - 2) * 32 + lane) * kStagePitch;
 
         // A operand: this thread's query row, split into TF32 hi/lo, into TMEM
         const float* qrow = a.queries + (q < a.Q ? q : 0) * a.ldq;
@@ -316,17 +333,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
         ptx::tc_fence_before();
         ptx::mbar_arrive(s.aready);
 
-        int cnt = 0;
         // padding rows of the last query tile accept nothing
-        float thr_local = q < a.Q ? __int_as_float(0x7f800000) : -__int_as_float(0x7f800000);
+        LaneState st{0, q < a.Q ? __int_as_float(0x7f800000) : -__int_as_float(0x7f800000)};
         uint32_t* thr_g = q < a.Q ? a.thr_g : nullptr;
         uint32_t g_pending = thr_g ? __ldcg(thr_g + q) : 0xFFFFFFFFu;
         const bool dump = a.dump != nullptr && blockIdx.x == 0 && blockIdx.y == 0;
         for (int t = 0; t < ntiles; ++t) {
             const int b = t & 1;
             const uint32_t use = (uint32_t)(t >> 1);
-            // warp-uniform outcome: tcgen05.ld below is warp-collective
             const int ns = t % kNormSlots;
+            // warp-uniform outcome: tcgen05.ld below is warp-collective
             const bool ok = tc_wait(a, s, &s.accf[b], use & 1u, kDevTimeoutEpilogue) &&
                             tc_wait(a, s, &s.nfull[ns], (uint32_t)(t / kNormSlots) & 1u, kDevTimeoutEpilogue);
             if (!__all_sync(0xffffffffu, ok)) break;
@@ -334,44 +350,57 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
             // shared threshold loaded one tile ago; fetch the next one now
             const float thr_glob = shared_thr_of(g_pending);
             if (thr_g) g_pending = __ldcg(thr_g + q);
+            float thr = fminf(st.thr_local, thr_glob);
             const uint32_t nb = (uint32_t)(n_begin + (int64_t)t * kTileN);
             const float* nrm = s.norms + ns * kTileN;
             const uint32_t tb = tmem + kAccCol + (uint32_t)b * kTileN + lane_base;
-            // four 32-column chunks; the next chunk's TMEM load overlaps this chunk's filter
+            // four 32-column chunks; the next chunk's TMEM load overlaps this chunk's test
             float va[32], vb[32];
             __syncwarp();
             ptx::tmem_ld32(tb, va);
             ptx::tmem_wait_ld_regs(va);
-            __syncwarp();
-            ptx::tmem_ld32(tb + 32, vb);
-            if (dump && t == 0)
-                for (int u = 0; u < 32; ++u) a.dump[row * kTileN + u] = va[u];
-            tc_offer_chunk(v, row, cnt, thr_local, thr_glob, va, nrm, nb, thr_g, q);
-            ptx::tmem_wait_ld_regs(vb);
-            __syncwarp();
-            ptx::tmem_ld32(tb + 64, va);
-            if (dump && t == 0)
-                for (int u = 0; u < 32; ++u) a.dump[row * kTileN + 32 + u] = vb[u];
-            tc_offer_chunk(v, row, cnt, thr_local, thr_glob, vb, nrm + 32, nb + 32, thr_g, q);
-            ptx::tmem_wait_ld_regs(va);
-            __syncwarp();
-            ptx::tmem_ld32(tb + 96, vb);
-            if (dump && t == 0)
-                for (int u = 0; u < 32; ++u) a.dump[row * kTileN + 64 + u] = va[u];
-            tc_offer_chunk(v, row, cnt, thr_local, thr_glob, va, nrm + 64, nb + 64, thr_g, q);
-            ptx::tmem_wait_ld_regs(vb);
-            // accumulator b fully read: hand it back to the MMA issuer
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int c0 = 2 * h, c1 = 2 * h + 1;
+                float key[32];
+                __syncwarp();
+                ptx::tmem_ld32(tb + (uint32_t)(32 * c1), vb);
+                if (dump && t == 0) {
+#pragma unroll
+                    for (int u = 0; u < 32; ++u) a.dump[row * kTileN + 32 * c0 + u] = va[u];
+                }
+                if (tc_chunk_hot(va, nrm + 32 * c0, thr, key)) {
+                    ptx::tmem_wait_ld_regs(vb);
+                    stage_keys(srow, key);
+                    st = offer_staged(v, srow, nb + 32 * c0, row, st, thr_glob, thr_g, q);
+                    thr = fminf(st.thr_local, thr_glob);
+                }
+                ptx::tmem_wait_ld_regs(vb);
+                if (h == 0) {
+                    __syncwarp();
+                    ptx::tmem_ld32(tb + (uint32_t)(32 * (c1 + 1)), va);
+                }
+                if (dump && t == 0) {
+#pragma unroll
+                    for (int u = 0; u < 32; ++u) a.dump[row * kTileN + 32 * c1 + u] = vb[u];
+                }
+                if (tc_chunk_hot(vb, nrm + 32 * c1, thr, key)) {
+                    if (h == 0) ptx::tmem_wait_ld_regs(va);
+                    stage_keys(srow, key);
+                    st = offer_staged(v, srow, nb + 32 * c1, row, st, thr_glob, thr_g, q);
+                    thr = fminf(st.thr_local, thr_glob);
+                }
+                if (h == 0) ptx::tmem_wait_ld_regs(va);
+            }
+            // accumulator b and norms slot ns fully consumed
             ptx::tc_fence_before();
             __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(&s.acce[b]);
-            if (dump && t == 0)
-                for (int u = 0; u < 32; ++u) a.dump[row * kTileN + 96 + u] = vb[u];
-            tc_offer_chunk(v, row, cnt, thr_local, thr_glob, vb, nrm + 96, nb + 96, thr_g, q);
-            // norms slot no longer read by this warp
-            __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(&s.nempty[ns]);
+            if (lane == 0) {
+                ptx::mbar_arrive(&s.acce[b]);
+                ptx::mbar_arrive(&s.nempty[ns]);
+            }
         }
-        flush_all(v, row, cnt, thr_local);
+        st = flush_all(v, row, st);
     }
 
     ptx::tc_fence_before();
