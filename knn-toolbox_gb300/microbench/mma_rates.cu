@@ -70,9 +70,15 @@ int main() {
     long long* h = new long long[sms];
     cudaFuncSetAttribute(bench, cudaFuncAttributeMaxDynamicSharedMemorySize, 16384 + 32768 + 1024);
     struct V { const char* name; int f16, a_tmem, N, commit_every, alt, iters; } vs[] = {
-        {"tf32 TMEM N128", 0, 1, 128, 0, 0, 4096}, {"tf32 TMEM N128 commit/4", 0, 1, 128, 1, 0, 4096},
-        {"tf32 TMEM N128 commit/4 alt16", 0, 1, 128, 1, 4, 4096}, {"tf32 TMEM N128 alt16", 0, 1, 128, 0, 4, 4096},
-        {"bf16 TMEM N128 commit/4 alt16", 1, 1, 128, 1, 4, 4096}, {"bf16 TMEM N256 commit/4", 1, 1, 256, 1, 0, 4096},
+        // instruction shapes, back to back
+        {"tf32 A=TMEM N=128", 0, 1, 128, 0, 0, 4096}, {"tf32 A=SMEM N=128", 0, 0, 128, 0, 0, 4096},
+        {"tf32 A=SMEM N=256", 0, 0, 256, 0, 0, 4096}, {"tf32 A=TMEM N=256", 0, 1, 256, 0, 0, 4096},
+        {"bf16 A=SMEM N=128", 1, 0, 128, 0, 0, 4096}, {"bf16 A=SMEM N=256", 1, 0, 256, 0, 0, 4096},
+        {"bf16 A=TMEM N=128", 1, 1, 128, 0, 0, 4096}, {"bf16 A=TMEM N=256", 1, 1, 256, 0, 0, 4096},
+        // pipeline effects: commit every 4 MMAs, alternate accumulators every 16
+        {"tf32 TMEM N128 commit/4", 0, 1, 128, 1, 0, 4096}, {"tf32 TMEM N128 commit/4 alt16", 0, 1, 128, 1, 4, 4096},
+        {"tf32 TMEM N128 alt16", 0, 1, 128, 0, 4, 4096}, {"bf16 TMEM N128 commit/4 alt16", 1, 1, 128, 1, 4, 4096},
+        {"bf16 TMEM N256 commit/4", 1, 1, 256, 1, 0, 4096},
         {"tf32 TMEM N128 latency(1 group)", 0, 1, 128, 0, 0, 1}, {"tf32 TMEM N128 (4 groups)", 0, 1, 128, 0, 0, 4}};
     for (auto& v : vs) {
         const int iters = v.iters;
