@@ -98,6 +98,29 @@ int knns_last_stats(knns_stats *out);
  */
 int knns_timing_collect(double ms[3], int *count);
 
+/*
+ * Allocation-free search.  No counterpart in the reference: it exists for
+ * callers that must not have device memory allocated during a search -- a
+ * process whose HBM is already reserved by another allocator (a framework's
+ * caching allocator), a latency-critical caller for which cudaMalloc/cudaFree
+ * would synchronise the device, or a plug-in host that owns all allocation.
+ * Inputs and outputs are the caller's device buffers, as for
+ * knns_search_device; the work runs asynchronously on `stream` with the
+ * CUDA-core kernel (exact re-rank on, automatic shortlist and splits).
+ * Scratch comes from one fixed 8 MiB array in device memory, held by every
+ * GPU that loads the library until the process exits; it must hold the corpus
+ * norms (4 * roundup(N, 128) bytes), the thresholds (4 * Q bytes) and at least
+ * one split of shortlists (8 * Q * kp bytes, kp = k + max(8, k/8) rounded up to
+ * 16, at least 32); larger problems are rejected with KNNS_ERR_UNSUPPORTED and
+ * a message.  The first call on a device looks the array's address up
+ * (cudaGetSymbolAddress), so make it before any stream capture.  Every call
+ * shares the array: calls whose GPU work overlaps (other streams, other host
+ * threads) race on it and must be serialised by the caller.  The function
+ * calls no cudaMalloc, cudaFree or allocating library routine.
+ */
+int knns_search_device_noalloc(const float *corpus, int64_t N, int64_t ldc, const float *queries, int64_t Q,
+                               int64_t ldq, int D, int k, float *dist, int32_t *idx, void *stream);
+
 /* Library version as 10000*major + 100*minor + patch. */
 int knns_version(void);
 

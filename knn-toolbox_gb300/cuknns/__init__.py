@@ -33,7 +33,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_UNSUPPORTED, ERR_DEVICE_TIMEOUT, ERR_NOMEM = rang
 # Every symbol include/knn_gb300.h and include/cuknns.h declare.
 EXPORTED = ["knns_default_options", "knns_search_device", "knns_search_host", "knns_check_device",
             "knns_last_error", "knns_last_stats", "knns_version", "knns_debug_tc_dot_tile",
-            "knns_timing_collect",
+            "knns_timing_collect", "knns_search_device_noalloc",
             "gpuknnsBitonic", "gpuknnsHeap", "knnsplan", "knnsexecute"]
 
 
@@ -90,6 +90,7 @@ def lib():
     L.knns_last_stats.argtypes = [ctypes.POINTER(Stats)]
     L.knns_debug_tc_dot_tile.argtypes = [vp, i64, vp, i64, ci, vp]
     L.knns_timing_collect.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
+    L.knns_search_device_noalloc.argtypes = [vp, i64, i64, vp, i64, i64, ci, ci, vp, vp, vp]
     L.gpuknnsBitonic.argtypes = [fp, fp, fp, fp, ci, ci, ci, ci, ci]
     L.gpuknnsBitonic.restype = ctypes.c_double
     L.gpuknnsHeap.argtypes = [fp, fp, fp, fp, ci, ci, ci, ci, ci]
