@@ -147,6 +147,23 @@ static int encode_rows(CUtensorMap* m, const float* base, int64_t rows, int64_t 
     return KNNS_OK;
 }
 
+// 2-D bf16 matrix [rows][cols], box {64 cols (128 B), 128 rows}, 128B swizzle
+static int encode_rows_bf16(CUtensorMap* m, const void* base, int64_t rows, int64_t cols)
+{
+    EncodeTiledFn fn;
+    int rc = get_encode_fn(&fn);
+    if (rc) return rc;
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
+    cuuint32_t box[2] = {64u, (cuuint32_t)kTileN};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(KNNS_ERR_CUDA, "cuTensorMapEncodeTiled (bf16) failed (%d)", (int)r);
+    return KNNS_OK;
+}
+
 // ---------------------------------------------------------------- planning
 static inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 static inline int round32(int x) { return (x + 31) & ~31; }
@@ -197,6 +214,7 @@ int resolve_config(const Engine& E, int64_t N, int64_t Q, int D, int k, const kn
         if (c->kp > kMaxKpTC)
             return set_error(KNNS_ERR_UNSUPPORTED, "tensor-core path holds at most %d shortlist entries", kMaxKpTC);
         c->dp = dp;
+        c->dpb = (D + 63) & ~63;
         c->stages = std::min(4, tc_max_stages(c->kp));
         c->qtile = kTileQ;
     } else if (algo == KNNS_ALGO_SIMT) {
@@ -260,9 +278,11 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         if (rc) return rc;
         rc = E.lo.ensure((size_t)N * c.dp * sizeof(float));
         if (rc) return rc;
-        rc = E.loflags.ensure(((size_t)cdiv(N, 128) + 1) * sizeof(uint32_t));
+        rc = E.bf.ensure((size_t)N * c.dpb * 2);
         if (rc) return rc;
-        ws += E.hi.cap + E.lo.cap + E.loflags.cap;
+        rc = E.loflags.ensure(((size_t)cdiv(N, 128) + 2) * sizeof(uint32_t));
+        if (rc) return rc;
+        ws += E.hi.cap + E.lo.cap + E.bf.cap + E.loflags.cap;
     }
 
     KNN_CUDA(cudaStreamWaitEvent(s, E.last_done, 0));
@@ -283,9 +303,14 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     if (c.algo == KNNS_ALGO_TC) {
         uint32_t* flags = (uint32_t*)E.loflags.p;
         uint32_t* any_lo = flags + cdiv(N, 128);
-        KNN_CUDA(cudaMemsetAsync(any_lo, 0, sizeof(uint32_t), s));
-        KNN_CUDA(launch_split(corpus, N, ldc, D, c.dp, (float*)E.hi.p, (float*)E.lo.p, flags, any_lo, s));
-        ++launches;
+        uint32_t* not_exact = any_lo + 1;
+        KNN_CUDA(cudaMemsetAsync(any_lo, 0, 2 * sizeof(uint32_t), s));
+        // BF16 copy of the corpus and the exactness test of corpus and queries;
+        // the TF32 split then runs only for data that is not BF16-exact
+        KNN_CUDA(launch_bf16(corpus, N, ldc, D, c.dpb, E.bf.p, not_exact, s));
+        KNN_CUDA(launch_bf16(queries, Q, ldq, D, c.dpb, nullptr, not_exact, s));
+        KNN_CUDA(launch_split(corpus, N, ldc, D, c.dp, (float*)E.hi.p, (float*)E.lo.p, flags, any_lo, not_exact, s));
+        launches += 3;
     }
     if (tv[1]) KNN_CUDA(cudaEventRecord(tv[1], s));
     if (c.algo == KNNS_ALGO_TC) {
@@ -295,6 +320,10 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         if (rc) return rc;
         rc = encode_rows(&a.tm_lo, (const float*)E.lo.p, N, c.dp);
         if (rc) return rc;
+        rc = encode_rows_bf16(&a.tm_bf, E.bf.p, N, c.dpb);
+        if (rc) return rc;
+        a.not_exact = (const uint32_t*)E.loflags.p + cdiv(N, 128) + 1;
+        a.dpb = c.dpb;
         a.cn = cn;
         a.queries = queries;
         a.Q = Q;
@@ -311,7 +340,10 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         a.dp = c.dp;
         a.kp = c.kp;
         a.stages = c.stages;
-        KNN_CUDA(launch_tc(a, c.splits, s));
+        // both precisions are launched; the one that does not match the data returns at once
+        KNN_CUDA(launch_tc(a, c.splits, false, s));
+        KNN_CUDA(launch_tc(a, c.splits, true, s));
+        ++launches;
     } else {
         KNN_CUDA(launch_simt(corpus, N, ldc, cn, queries, Q, ldq, D, c.kp, c.qtile, c.split_len, c.splits, part,
                              thr_g, s));
@@ -515,6 +547,7 @@ int knns_debug_tc_dot_tile(const float* corpus, int64_t N, const float* queries,
     std::lock_guard<std::mutex> lk(E->mu);
     if (E->cc < 100) return set_error(KNNS_ERR_UNSUPPORTED, "needs sm_100+");
     const int dp = (D + 31) & ~31;
+    const int dpb = (D + 63) & ~63;
     if (dp > kMaxDpTC) return set_error(KNNS_ERR_UNSUPPORTED, "D > %d", kMaxDpTC);
     const int64_t n_use = std::min<int64_t>(N, kTileN);
     const int64_t n_pad = 128;
@@ -522,14 +555,24 @@ int knns_debug_tc_dot_tile(const float* corpus, int64_t N, const float* queries,
     if ((rc = E->cn.ensure(n_pad * 4))) return rc;
     if ((rc = E->hi.ensure((size_t)n_use * dp * 4))) return rc;
     if ((rc = E->lo.ensure((size_t)n_use * dp * 4))) return rc;
+    if ((rc = E->bf.ensure((size_t)n_use * dpb * 2))) return rc;
+    if ((rc = E->loflags.ensure(4 * sizeof(uint32_t)))) return rc;
     if ((rc = E->part.ensure((size_t)std::min<int64_t>(Q, kTileQ) * 32 * 8))) return rc;
     KNN_CUDA(cudaStreamWaitEvent(s, E->last_done, 0));
     KNN_CUDA(launch_norms(corpus, n_use, D, D, (float*)E->cn.p, n_pad, s));
-    KNN_CUDA(launch_split(corpus, n_use, D, D, dp, (float*)E->hi.p, (float*)E->lo.p, nullptr, nullptr, s));
+    uint32_t* not_exact = (uint32_t*)E->loflags.p;
+    const int64_t q_use = std::min<int64_t>(Q, kTileQ);
+    KNN_CUDA(cudaMemsetAsync(not_exact, 0, sizeof(uint32_t), s));
+    KNN_CUDA(launch_bf16(corpus, n_use, D, D, dpb, E->bf.p, not_exact, s));
+    KNN_CUDA(launch_bf16(queries, q_use, D, D, dpb, nullptr, not_exact, s));
+    KNN_CUDA(launch_split(corpus, n_use, D, D, dp, (float*)E->hi.p, (float*)E->lo.p, nullptr, nullptr, nullptr, s));
     TcArgs a;
     memset(&a, 0, sizeof(a));
     if ((rc = encode_rows(&a.tm_hi, (const float*)E->hi.p, n_use, dp))) return rc;
     if ((rc = encode_rows(&a.tm_lo, (const float*)E->lo.p, n_use, dp))) return rc;
+    if ((rc = encode_rows_bf16(&a.tm_bf, E->bf.p, n_use, dpb))) return rc;
+    a.not_exact = not_exact;
+    a.dpb = dpb;
     a.cn = (const float*)E->cn.p;
     a.queries = queries;
     a.Q = std::min<int64_t>(Q, kTileQ);
@@ -547,7 +590,8 @@ int knns_debug_tc_dot_tile(const float* corpus, int64_t N, const float* queries,
     a.kp = 32;
     a.stages = std::min(4, tc_max_stages(32));
     KNN_CUDA(cudaMemsetAsync(dump, 0, (size_t)kTileQ * kTileN * 4, s));
-    KNN_CUDA(launch_tc(a, 1, s));
+    KNN_CUDA(launch_tc(a, 1, false, s));
+    KNN_CUDA(launch_tc(a, 1, true, s));
     KNN_CUDA(cudaEventRecord(E->last_done, s));
     return check_device_error(*E, s);
 }

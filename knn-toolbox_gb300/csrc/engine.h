@@ -26,6 +26,7 @@ struct Config {
     int64_t split_len = 0;
     int qtile = 128;
     int dp = 0;
+    int dpb = 0;
     int stages = 0;
 };
 
@@ -35,7 +36,7 @@ struct Engine {
     int cc = 0;
     std::mutex mu;
     cudaEvent_t last_done = nullptr;
-    DevBuf cn, qn, part, hi, lo, err, thr, loflags;
+    DevBuf cn, qn, part, hi, lo, bf, err, thr, loflags;
     DevBuf in_corpus, in_queries, out_dist, out_idx;
     // stage timing: 4 events per timed search (start, after prep, after fused, end)
     std::vector<cudaEvent_t> tev;

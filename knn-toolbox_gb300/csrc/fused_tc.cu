@@ -6,9 +6,16 @@
 // bitonic_shared2 / relloc, src/cuknnBitonic.cu:45-254): the distance matrix
 // stays in tensor memory and only shortlist survivors reach shared memory.
 //
-// q.c runs as 3xTF32: with x = hi + lo (hi = tf32(x), lo = tf32(x - hi)),
-// q.c ~= qhi.chi + qhi.clo + qlo.chi, accumulated in FP32 by
-// tcgen05.mma.kind::tf32.  A corpus tile (or the query tile) whose low part
+// Two precisions share the kernel (template parameter kBF16); both are
+// launched and the one that does not match the data returns at once (a
+// device flag set by the preparation pass decides, so the host never waits):
+//  * BF16-exact data (every corpus and query element equals its BF16
+//    rounding, e.g. integer descriptors up to 256): q.c runs as
+//    tcgen05.mma.kind::f16 with BF16 operands and FP32 accumulation -- exact
+//    products, so the keys are the FP32 keys;
+//  * otherwise 3xTF32: with x = hi + lo (hi = tf32(x), lo = tf32(x - hi)),
+//    q.c ~= qhi.chi + qhi.clo + qlo.chi, accumulated in FP32 by
+//    tcgen05.mma.kind::tf32.  A corpus tile (or the query tile) whose low part
 // is all zero skips its correction product: it would add exact zeros, so the
 // accumulator is bit-identical either way.  For integer data below 2^11 every
 // low part is zero and the products and sums are exact, so the keys equal the
@@ -29,6 +36,7 @@
 // code in the device error word and winds down without hanging the GPU.
 #include <cstdint>
 #include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include "common.cuh"
 #include "kernels.h"
@@ -50,6 +58,8 @@ constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kAccCol = 256;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 constexpr uint32_t kIdesc = ptx::idesc_tf32(kTileQ, kTileN);
+constexpr uint32_t kIdescBf16 = ptx::idesc_bf16(kTileQ, kTileN);
+constexpr int kBoxElemsBf16 = 64;                  // bf16 elements per 128-byte swizzle row
 
 __device__ __forceinline__ float tf32_rne_dev(float x)
 {
@@ -143,9 +153,16 @@ __device__ __forceinline__ void stage_keys(float* srow, const float (&key)[32])
     for (int j = 0; j < 32; ++j) srow[j] = key[j];
 }
 
+template <bool kBF16>
 __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant__ TcArgs a)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
+    // only the variant that matches the data runs
+    if (a.not_exact != nullptr) {
+        if ((*a.not_exact != 0u) == kBF16) return;
+    } else if (kBF16) {
+        return;
+    }
     // The operand ring needs 1024-byte alignment (128-byte swizzle atoms).
     // The dynamic shared-memory window starts 1024-aligned; refuse to run otherwise.
     if ((ptx::smem_u32(sm) & 1023u) != 0u) {
@@ -154,11 +171,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
     }
 
     const int stages = a.stages;
-    // Ring layout: with a low part anywhere in the corpus, `stages` slots of
-    // hi+lo; otherwise twice as many hi-only slots (deeper prefetch).
-    const bool ring_lo = a.corpus_any_lo == nullptr || *a.corpus_any_lo != 0u;
-    const int nslot = ring_lo ? stages : 2 * stages;
-    const uint32_t slot_bytes = ring_lo ? kStageBytes : kHalfBytes;
+    // Ring layout (TF32): with a low part anywhere in the corpus, `stages`
+    // slots of hi+lo; otherwise twice as many hi-only slots (deeper prefetch).
+    // Ring layout (BF16): slots of whole tiles (all K boxes, one commit per
+    // tile) when two fit, else one box per slot.
+    const int nbox_bf = a.dpb / kBoxElemsBf16;
+    const int bps = (2 * nbox_bf * (int)kHalfBytes <= stages * (int)kStageBytes) ? nbox_bf : 1;
+    const bool ring_lo = !kBF16 && (a.corpus_any_lo == nullptr || *a.corpus_any_lo != 0u);
+    const uint32_t slot_bytes = kBF16 ? (uint32_t)bps * kHalfBytes : (ring_lo ? kStageBytes : kHalfBytes);
+    const int nslot = (int)min((uint32_t)(2 * kMaxStages), (uint32_t)(stages * kStageBytes) / slot_bytes);
 
     TcSmem s;
     s.ring = sm;
@@ -186,7 +207,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
     const int64_t n_begin = (int64_t)blockIdx.y * a.split_len;
     const int64_t n_end = min(a.N, n_begin + a.split_len);
     const int ntiles = (int)((n_end - n_begin + kTileN - 1) / kTileN);
-    const int nchunks = a.dp / kChunkK;
+    // K steps: TF32 chunks of 32 elements per 128-byte row; BF16 groups of `bps` boxes of 64
+    const int nchunks = kBF16 ? nbox_bf / bps : a.dp / kChunkK;
 
     if (tid == 0) {
         for (int i = 0; i < nslot; ++i) {
@@ -206,8 +228,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
         *s.abort = 0;
         *s.alo_flag = 0;
         ptx::fence_mbar_init();
-        ptx::tma_prefetch_desc(&a.tm_hi);
-        ptx::tma_prefetch_desc(&a.tm_lo);
+        if (kBF16) {
+            ptx::tma_prefetch_desc(&a.tm_bf);
+        } else {
+            ptx::tma_prefetch_desc(&a.tm_hi);
+            ptx::tma_prefetch_desc(&a.tm_lo);
+        }
     }
     if (warp == 1) {
         ptx::tmem_alloc(s.tmem_holder, kTmemCols);
@@ -242,10 +268,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
                     const uint32_t ph = (uint32_t)(it / nslot) & 1u;
                     if (!tc_wait(a, s, &s.empty[st], ph ^ 1u, kDevTimeoutProducer)) { ok = false; break; }
                     unsigned char* dst = s.ring + (size_t)st * slot_bytes;
-                    s.stage_lo[st] = need_lo;  // published by the arrive below
-                    ptx::mbar_arrive_expect_tx(&s.full[st], need_lo ? kStageBytes : kHalfBytes);
-                    ptx::tma_load_2d(dst, &a.tm_hi, &s.full[st], c * kChunkK, (int)n0);
-                    if (need_lo) ptx::tma_load_2d(dst + kHalfBytes, &a.tm_lo, &s.full[st], c * kChunkK, (int)n0);
+                    if (kBF16) {
+                        ptx::mbar_arrive_expect_tx(&s.full[st], slot_bytes);
+                        for (int bx = 0; bx < bps; ++bx)
+                            ptx::tma_load_2d(dst + bx * kHalfBytes, &a.tm_bf, &s.full[st],
+                                             (c * bps + bx) * kBoxElemsBf16, (int)n0);
+                    } else {
+                        s.stage_lo[st] = need_lo;  // published by the arrive below
+                        ptx::mbar_arrive_expect_tx(&s.full[st], need_lo ? kStageBytes : kHalfBytes);
+                        ptx::tma_load_2d(dst, &a.tm_hi, &s.full[st], c * kChunkK, (int)n0);
+                        if (need_lo)
+                            ptx::tma_load_2d(dst + kHalfBytes, &a.tm_lo, &s.full[st], c * kChunkK, (int)n0);
+                    }
                 }
             }
             if (!ok) {
@@ -273,20 +307,33 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
                     const uint32_t ph = (uint32_t)(it / nslot) & 1u;
                     if (!tc_wait(a, s, &s.full[st], ph, kDevTimeoutMma)) { ok = false; break; }
                     ptx::tc_fence_after();
-                    const uint32_t b_lo = s.stage_lo[st];
                     const uint32_t hi_addr = ptx::smem_u32(s.ring + (size_t)st * slot_bytes);
-                    const uint32_t lo_addr = hi_addr + kHalfBytes;
+                    if (kBF16) {
+                        // bps boxes of 64 bf16 (128-byte rows); K = 16 per instruction
+                        for (int bx = 0; bx < bps; ++bx) {
+                            const uint32_t box = (uint32_t)(c * bps + bx);
 #pragma unroll
-                    for (int kk = 0; kk < kChunkK / 8; ++kk) {
-                        const uint64_t dh = ptx::desc_sw128_kmajor(hi_addr + kk * 32);
-                        const uint32_t ahi = tmem + (uint32_t)(c * kChunkK + kk * 8);
-                        const uint32_t alo = ahi + (uint32_t)a.dp;
-                        // an all-zero low part contributes exact zeros: skipping it leaves
-                        // the FP32 accumulator bit-identical
-                        ptx::mma_tf32_ts(d_tmem, ahi, dh, kIdesc, (c | kk) != 0);
-                        if (b_lo)
-                            ptx::mma_tf32_ts(d_tmem, ahi, ptx::desc_sw128_kmajor(lo_addr + kk * 32), kIdesc, 1u);
-                        if (a_lo) ptx::mma_tf32_ts(d_tmem, alo, dh, kIdesc, 1u);
+                            for (int kk = 0; kk < 4; ++kk) {
+                                const uint64_t db = ptx::desc_sw128_kmajor(hi_addr + bx * kHalfBytes + kk * 32);
+                                const uint32_t acol = tmem + box * 32u + (uint32_t)(kk * 8);
+                                ptx::mma_bf16_ts(d_tmem, acol, db, kIdescBf16, (c | bx | kk) != 0);
+                            }
+                        }
+                    } else {
+                        const uint32_t b_lo = s.stage_lo[st];
+                        const uint32_t lo_addr = hi_addr + kHalfBytes;
+#pragma unroll
+                        for (int kk = 0; kk < kChunkK / 8; ++kk) {
+                            const uint64_t dh = ptx::desc_sw128_kmajor(hi_addr + kk * 32);
+                            const uint32_t ahi = tmem + (uint32_t)(c * kChunkK + kk * 8);
+                            const uint32_t alo = ahi + (uint32_t)a.dp;
+                            // an all-zero low part contributes exact zeros: skipping it leaves
+                            // the FP32 accumulator bit-identical
+                            ptx::mma_tf32_ts(d_tmem, ahi, dh, kIdesc, (c | kk) != 0);
+                            if (b_lo)
+                                ptx::mma_tf32_ts(d_tmem, ahi, ptx::desc_sw128_kmajor(lo_addr + kk * 32), kIdesc, 1u);
+                            if (a_lo) ptx::mma_tf32_ts(d_tmem, alo, dh, kIdesc, 1u);
+                        }
                     }
                     ptx::mma_commit(&s.empty[st]);
                 }
@@ -311,10 +358,27 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
         v.buf_pitch = kTileQ;
         float* srow = s.keystage + ((warp - 2) * 32 + lane) * kStagePitch;
 
-        // A operand: this thread's query row, split into TF32 hi/lo, into TMEM
+        // A operand: this thread's query row into TMEM (BF16 pairs, or TF32 hi/lo)
         const float* qrow = a.queries + (q < a.Q ? q : 0) * a.ldq;
         uint32_t any_lo = 0;
-        for (int c = 0; c < nchunks; ++c) {
+        if (kBF16) {
+            for (int bx = 0; bx < nbox_bf; ++bx) {
+                float packed[32];
+#pragma unroll
+                for (int u = 0; u < 32; ++u) {
+                    const int d0 = bx * kBoxElemsBf16 + 2 * u;
+                    const float x0 = (q < a.Q && d0 < a.D) ? __ldg(qrow + d0) : 0.f;
+                    const float x1 = (q < a.Q && d0 + 1 < a.D) ? __ldg(qrow + d0 + 1) : 0.f;
+                    // lower K index in the low half of the 32-bit column
+                    const uint32_t lo16 = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(x0));
+                    const uint32_t hi16 = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(x1));
+                    packed[u] = __uint_as_float(lo16 | (hi16 << 16));
+                }
+                __syncwarp();
+                ptx::tmem_st32(tmem + lane_base + (uint32_t)(bx * 32), packed);
+            }
+        }
+        for (int c = 0; c < (kBF16 ? 0 : nchunks); ++c) {
             float hi[32], lo[32];
 #pragma unroll
             for (int u = 0; u < 32; ++u) {
@@ -416,15 +480,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
     for (int64_t i = tid; i < nq * a.kp; i += kTcThreads) out[i] = s.list[i];
 }
 
-cudaError_t launch_tc(const TcArgs& a, int splits, cudaStream_t st)
+cudaError_t launch_tc(const TcArgs& a, int splits, bool bf16, cudaStream_t st)
 {
-    if (a.stages < 1 || a.stages > kMaxStages || a.dp % kChunkK != 0 || a.dp > kMaxDpTC || a.kp % 16 != 0)
+    if (a.stages < 1 || a.stages > kMaxStages || a.dp % kChunkK != 0 || a.dp > kMaxDpTC || a.kp % 16 != 0 ||
+        a.dpb % kBoxElemsBf16 != 0 || a.dpb / 2 > kMaxDpTC)
         return cudaErrorInvalidValue;
     const size_t smem = tc_smem_bytes(a.kp, a.stages);
-    cudaError_t e = cudaFuncSetAttribute(tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
     dim3 grid((unsigned)((a.Q + kTileQ - 1) / kTileQ), (unsigned)splits);
-    tc_kernel<<<grid, kTcThreads, smem, st>>>(a);
+    cudaError_t e;
+    if (bf16) {
+        e = cudaFuncSetAttribute(tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        tc_kernel<true><<<grid, kTcThreads, smem, st>>>(a);
+    } else {
+        e = cudaFuncSetAttribute(tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        tc_kernel<false><<<grid, kTcThreads, smem, st>>>(a);
+    }
     return cudaGetLastError();
 }
 

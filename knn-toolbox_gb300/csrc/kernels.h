@@ -28,9 +28,14 @@ enum DeviceError : int {
 cudaError_t launch_norms(const float* x, int64_t n, int64_t ld, int D, float* out, int64_t n_pad,
                          cudaStream_t s);
 // TF32 hi/lo split into [n][dp] arrays; lo_flags[tile of 128 rows] = any lo != 0 (may be null);
-// *any_lo (zeroed by the caller, may be null) becomes 1 when some tile has a low part.
+// *any_lo (zeroed by the caller, may be null) becomes 1 when some tile has a low part.  When
+// skip_unless is given and *skip_unless == 0 at run time, the kernel does nothing.
 cudaError_t launch_split(const float* x, int64_t n, int64_t ld, int D, int dp, float* hi, float* lo,
-                         uint32_t* lo_flags, uint32_t* any_lo, cudaStream_t s);
+                         uint32_t* lo_flags, uint32_t* any_lo, const uint32_t* skip_unless, cudaStream_t s);
+// BF16 copy into [n][dpb] (out may be null: check only); *not_exact |= 1 when some element
+// is not exactly representable in BF16.
+cudaError_t launch_bf16(const float* x, int64_t n, int64_t ld, int D, int dpb, void* out, uint32_t* not_exact,
+                        cudaStream_t s);
 
 // CUDA-core FP32 fused distance + shortlist.  qpb in {32, 128}.
 size_t simt_smem_bytes(int qpb, int kp);
@@ -42,6 +47,7 @@ cudaError_t launch_simt(const float* corpus, int64_t N, int64_t ldc, const float
 struct TcArgs {
     CUtensorMap tm_hi;        // corpus hi  [N][dp] fp32, box {32, 128}, 128B swizzle
     CUtensorMap tm_lo;        // corpus lo
+    CUtensorMap tm_bf;        // corpus bf16 [N][dpb], box {64, 128}, 128B swizzle
     const float* cn;          // [>= roundup(N,128)] corpus norms, +inf padding
     const float* queries;     // [Q][ldq]
     int64_t Q;
@@ -52,16 +58,20 @@ struct TcArgs {
     uint32_t* thr_g;          // [Q] shared per-query threshold (order-mapped key), or null
     const uint32_t* lo_flags; // [ceil(N/128)] 1 when the corpus tile has a nonzero TF32 low part, or null
     const uint32_t* corpus_any_lo;  // 1 when any corpus tile has a low part (null: assume so)
+    const uint32_t* not_exact;      // 0 when corpus and queries are BF16-exact (null: TF32 path only)
     float* dump;              // optional: raw dot tile of CTA (0,0), tile 0, [128][128]
     int* err;                 // device error word
     int D;
     int dp;                   // D rounded up to kChunkK
+    int dpb;                  // D rounded up to 64 (BF16 boxes)
     int kp;
     int stages;
 };
 size_t tc_smem_bytes(int kp, int stages);
 int tc_max_stages(int kp);
-cudaError_t launch_tc(const TcArgs& a, int splits, cudaStream_t s);
+// Launches the BF16 (bf16 = true) or TF32 variant; each returns at once unless
+// *a.not_exact selects it (BF16: inputs exact in BF16; TF32: otherwise).
+cudaError_t launch_tc(const TcArgs& a, int splits, bool bf16, cudaStream_t s);
 
 // Merge of the per-split shortlists, optional exact re-rank, final top-k.
 size_t select_smem_bytes(int kp, int D, int rerank);

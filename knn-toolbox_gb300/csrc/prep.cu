@@ -6,6 +6,7 @@
 // the integer-valued data of the 1M x 128 workload and within one rounding of
 // exact otherwise); the same convention is used by the CPU oracle.
 #include <cstdint>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include "common.cuh"
 #include "kernels.h"
@@ -49,13 +50,38 @@ __device__ __forceinline__ float tf32_rne(float x)
     return __uint_as_float(u);
 }
 
+// BF16 copy of a row-major matrix, rows padded with zeros to dpb columns, and
+// a global "not exactly representable" flag: *not_exact becomes 1 when some
+// element differs from its BF16 rounding (inf/nan count as not exact).  One
+// block per 128-row tile.
+__global__ void bf16_tiles_kernel(const float* __restrict__ x, int64_t n, int64_t ld, int D, int dpb,
+                                  __nv_bfloat16* __restrict__ out, uint32_t* __restrict__ not_exact)
+{
+    const int64_t r0 = (int64_t)blockIdx.x * 128;
+    const int64_t rows = min((int64_t)128, n - r0);
+    const int64_t total = rows * dpb;
+    int bad = 0;
+    for (int64_t i = threadIdx.x; i < total; i += blockDim.x) {
+        const int64_t r = r0 + i / dpb;
+        const int c = (int)(i % dpb);
+        const float v = c < D ? __ldg(x + r * ld + c) : 0.f;
+        const __nv_bfloat16 b = __float2bfloat16_rn(v);
+        if (out) out[r * dpb + c] = b;
+        bad |= !(__bfloat162float(b) == v);
+    }
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0 && bad) atomicOr(not_exact, 1u);
+}
+
 // hi = tf32(x), lo = tf32(x - hi); rows padded with zeros to dp columns.
 // One block per 128-row tile; lo_flags[tile] = 1 when any lo in the tile is
 // nonzero (the tensor-core kernel skips the correction products otherwise).
 __global__ void split_tiles_kernel(const float* __restrict__ x, int64_t n, int64_t ld, int D, int dp,
                                    float* __restrict__ hi, float* __restrict__ lo, uint32_t* __restrict__ lo_flags,
-                                   uint32_t* __restrict__ any_lo)
+                                   uint32_t* __restrict__ any_lo, const uint32_t* __restrict__ skip_unless)
 {
+    // BF16-exact inputs are searched by the BF16 kernel: nothing to prepare
+    if (skip_unless && *skip_unless == 0u) return;
     const int64_t r0 = (int64_t)blockIdx.x * 128;
     const int64_t rows = min((int64_t)128, n - r0);
     const int64_t total = rows * dp;
@@ -88,11 +114,20 @@ cudaError_t launch_norms(const float* x, int64_t n, int64_t ld, int D, float* ou
 }
 
 cudaError_t launch_split(const float* x, int64_t n, int64_t ld, int D, int dp, float* hi, float* lo,
-                         uint32_t* lo_flags, uint32_t* any_lo, cudaStream_t s)
+                         uint32_t* lo_flags, uint32_t* any_lo, const uint32_t* skip_unless, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
     const int64_t tiles = (n + 127) / 128;
-    split_tiles_kernel<<<(unsigned)tiles, 256, 0, s>>>(x, n, ld, D, dp, hi, lo, lo_flags, any_lo);
+    split_tiles_kernel<<<(unsigned)tiles, 256, 0, s>>>(x, n, ld, D, dp, hi, lo, lo_flags, any_lo, skip_unless);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bf16(const float* x, int64_t n, int64_t ld, int D, int dpb, void* out, uint32_t* not_exact,
+                        cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    const int64_t tiles = (n + 127) / 128;
+    bf16_tiles_kernel<<<(unsigned)tiles, 256, 0, s>>>(x, n, ld, D, dpb, static_cast<__nv_bfloat16*>(out), not_exact);
     return cudaGetLastError();
 }
 

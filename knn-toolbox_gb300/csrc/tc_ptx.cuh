@@ -115,6 +115,18 @@ __device__ __forceinline__ void mma_tf32_ts(uint32_t d_tmem, uint32_t a_tmem, ui
         : "memory");
 }
 
+// D[tmem] (+)= A[tmem] * B[smem desc]^T, kind::f16 (BF16 operands, FP32 accumulate), cta_group::1
+__device__ __forceinline__ void mma_bf16_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc, uint32_t idesc,
+                                            uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "r"(a_tmem), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
 // Arrive on an mbarrier once all previously issued tcgen05 async ops of this thread complete.
 __device__ __forceinline__ void mma_commit(uint64_t* bar)
 {
@@ -188,6 +200,16 @@ __device__ __forceinline__ uint64_t desc_sw128_kmajor(uint32_t smem_addr)
     d |= (uint64_t)1 << 46;                           // descriptor version (tcgen05)
     d |= (uint64_t)2 << 61;                           // swizzle mode: 128B
     return d;
+}
+
+// Instruction descriptor: kind::f16 with BF16 A/B, D f32, K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
+{
+    return (1u << 4)                       // D format f32
+           | (1u << 7)                     // A format bf16
+           | (1u << 10)                    // B format bf16
+           | ((uint32_t)(N >> 3) << 17)    // N / 8
+           | ((uint32_t)(M >> 4) << 24);   // M / 16
 }
 
 // Instruction descriptor: kind::tf32, D f32, A/B tf32 K-major, M x N.
