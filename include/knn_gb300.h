@@ -43,7 +43,9 @@ typedef struct knns_options {
                         0: reference semantics, rank by ||c||^2 - 2 q.c, distance = key + ||q||^2 */
     int kp;          /* shortlist length per query (multiple of 16, >= 32, >= k); 0 = automatic */
     int timing;      /* 1: record CUDA events around each stage (see knns_timing_collect) */
-    int reserved[3];
+    int pilot;       /* 1 (default): seed per-query thresholds from a pass over a 1/16 corpus sample
+                        (large corpora only); results are identical either way */
+    int reserved[2];
 } knns_options;
 
 typedef struct knns_stats {
@@ -52,11 +54,11 @@ typedef struct knns_stats {
     int kp;
     int stages;      /* shared-memory pipeline depth of the tensor-core kernel */
     int launches;    /* kernels launched by the call */
-    int reserved;
+    int pilot;       /* 1 when the threshold-seeding pilot pass ran */
     int64_t workspace_bytes;
 } knns_stats;
 
-/* Fill *opt with the defaults (automatic algo, splits and shortlist, re-rank on). */
+/* Fill *opt with the defaults (automatic algo, splits and shortlist, re-rank on, pilot on). */
 void knns_default_options(knns_options *opt);
 
 /*

@@ -130,14 +130,15 @@ static int get_encode_fn(EncodeTiledFn* fn)
     return KNNS_OK;
 }
 
-// 2-D fp32 matrix [rows][cols] (cols contiguous), box {32 cols, 128 rows}, 128B swizzle
-static int encode_rows(CUtensorMap* m, const float* base, int64_t rows, int64_t cols)
+// 2-D fp32 matrix [rows][cols] (cols contiguous, rows `pitch` elements apart),
+// box {32 cols, 128 rows}, 128B swizzle
+static int encode_rows(CUtensorMap* m, const float* base, int64_t rows, int64_t cols, int64_t pitch = 0)
 {
     EncodeTiledFn fn;
     int rc = get_encode_fn(&fn);
     if (rc) return rc;
     cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)cols * sizeof(float)};
+    cuuint64_t strides[1] = {(cuuint64_t)(pitch > 0 ? pitch : cols) * sizeof(float)};
     cuuint32_t box[2] = {(cuuint32_t)kChunkK, (cuuint32_t)kTileN};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, estr,
@@ -147,14 +148,14 @@ static int encode_rows(CUtensorMap* m, const float* base, int64_t rows, int64_t 
     return KNNS_OK;
 }
 
-// 2-D bf16 matrix [rows][cols], box {64 cols (128 B), 128 rows}, 128B swizzle
-static int encode_rows_bf16(CUtensorMap* m, const void* base, int64_t rows, int64_t cols)
+// 2-D bf16 matrix [rows][cols] (rows `pitch` elements apart), box {64 cols (128 B), 128 rows}, 128B swizzle
+static int encode_rows_bf16(CUtensorMap* m, const void* base, int64_t rows, int64_t cols, int64_t pitch = 0)
 {
     EncodeTiledFn fn;
     int rc = get_encode_fn(&fn);
     if (rc) return rc;
     cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
+    cuuint64_t strides[1] = {(cuuint64_t)(pitch > 0 ? pitch : cols) * 2};
     cuuint32_t box[2] = {64u, (cuuint32_t)kTileN};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
@@ -197,6 +198,7 @@ int auto_splits(int64_t qtiles, int64_t tiles, int sms, int max_splits)
 int resolve_config(const Engine& E, int64_t N, int64_t Q, int D, int k, const knns_options& o, Config* c)
 {
     c->rerank = o.rerank ? 1 : 0;
+    c->pilot = o.pilot != 0;
     c->kp = o.kp > 0 ? o.kp : auto_kp(k, c->rerank);
     if (o.kp <= 0 && c->kp > 512 && k <= 512) c->kp = std::max(round16(k), 32);  // no margin at the limit
     if (c->kp % 16 != 0 || c->kp < k || c->kp < 32)
@@ -268,6 +270,35 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     rc = E.thr.ensure(Q * sizeof(uint32_t));
     if (rc) return rc;
     ws += E.thr.cap;
+    // Threshold seeding: a pilot pass over every s-th corpus row gives each
+    // query the key of a conservatively high rank r of its sample shortlist;
+    // the main pass drops candidates above it from the first tile on.  Exact:
+    // a query whose merged shortlist ends up with fewer than min(kp, N)
+    // entries is redone (its whole query tile) without the seed.
+    const int sample_stride = 16;
+    const bool pilot = c.pilot && N >= (int64_t)sample_stride * 4096;
+    const int qt = (int)cdiv(Q, c.qtile);
+    const int tile_n = c.algo == KNNS_ALGO_TC ? kTileN : kSimtTileN;
+    int64_t ns = 0, ns_pad = 0, split_len1 = 0;
+    int rank = 0, kp1 = 0, stages1 = 0, splits1 = 0;
+    if (pilot) {
+        ns = (N - 1) / sample_stride + 1;
+        ns_pad = cdiv(ns, 128) * 128;
+        const double per = (double)c.kp / sample_stride;
+        rank = (int)std::ceil(2.0 * per + 3.0 * std::sqrt(per)) + 1;
+        kp1 = std::max(32, round16(rank));
+        stages1 = c.algo == KNNS_ALGO_TC ? std::min(4, tc_max_stages(kp1)) : 0;
+        const int64_t tiles1 = cdiv(ns, tile_n);
+        splits1 = auto_splits(qt, tiles1, E.sms, 64);
+        split_len1 = cdiv(tiles1, splits1) * tile_n;
+        splits1 = (int)cdiv(ns, split_len1);
+        rc = E.cn_s.ensure((size_t)ns_pad * sizeof(float));
+        if (!rc) rc = E.thr2.ensure(Q * sizeof(uint32_t));
+        if (!rc) rc = E.redo.ensure((size_t)qt * sizeof(uint32_t));
+        if (!rc) rc = E.part.ensure((size_t)splits1 * Q * kp1 * sizeof(uint64_t));
+        if (rc) return rc;
+        ws += E.cn_s.cap + E.thr2.cap + E.redo.cap;
+    }
     if (!c.rerank) {
         rc = E.qn.ensure(Q * sizeof(float));
         if (rc) return rc;
@@ -299,11 +330,13 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     }
     uint64_t* part = (uint64_t*)E.part.p;
     uint32_t* thr_g = (uint32_t*)E.thr.p;
-    KNN_CUDA(cudaMemsetAsync(thr_g, 0xFF, Q * sizeof(uint32_t), s));
+    uint32_t* flags = nullptr;
+    uint32_t* any_lo = nullptr;
+    uint32_t* not_exact = nullptr;
     if (c.algo == KNNS_ALGO_TC) {
-        uint32_t* flags = (uint32_t*)E.loflags.p;
-        uint32_t* any_lo = flags + cdiv(N, 128);
-        uint32_t* not_exact = any_lo + 1;
+        flags = (uint32_t*)E.loflags.p;
+        any_lo = flags + cdiv(N, 128);
+        not_exact = any_lo + 1;
         KNN_CUDA(cudaMemsetAsync(any_lo, 0, 2 * sizeof(uint32_t), s));
         // BF16 copy of the corpus and the exactness test of corpus and queries;
         // the TF32 split then runs only for data that is not BF16-exact
@@ -313,49 +346,94 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         launches += 3;
     }
     if (tv[1]) KNN_CUDA(cudaEventRecord(tv[1], s));
-    if (c.algo == KNNS_ALGO_TC) {
-        TcArgs a;
-        memset(&a, 0, sizeof(a));
-        rc = encode_rows(&a.tm_hi, (const float*)E.hi.p, N, c.dp);
+
+    // One fused pass over a corpus view: rows 0, stride, 2*stride, ... (nview of them).
+    auto fused_pass = [&](int64_t nview, int64_t stride, const float* cn_view, int kp, int stages, int splits,
+                          int64_t split_len, uint32_t* thr, const uint32_t* redo, bool tile_flags) -> int {
+        if (c.algo == KNNS_ALGO_TC) {
+            TcArgs a;
+            memset(&a, 0, sizeof(a));
+            int r = encode_rows(&a.tm_hi, (const float*)E.hi.p, nview, c.dp, stride * c.dp);
+            if (!r) r = encode_rows(&a.tm_lo, (const float*)E.lo.p, nview, c.dp, stride * c.dp);
+            if (!r) r = encode_rows_bf16(&a.tm_bf, E.bf.p, nview, c.dpb, stride * c.dpb);
+            if (r) return r;
+            a.not_exact = not_exact;
+            a.tile_redo = redo;
+            a.dpb = c.dpb;
+            a.cn = cn_view;
+            a.queries = queries;
+            a.Q = Q;
+            a.ldq = ldq;
+            a.N = nview;
+            a.split_len = split_len;
+            a.part = part;
+            a.thr_g = thr;
+            a.lo_flags = tile_flags ? flags : nullptr;
+            a.corpus_any_lo = tile_flags ? any_lo : nullptr;
+            a.dump = nullptr;
+            a.err = (int*)E.err.p;
+            a.D = D;
+            a.dp = c.dp;
+            a.kp = kp;
+            a.stages = stages;
+            // both precisions are launched; the one that does not match the data returns at once
+            KNN_CUDA(launch_tc(a, splits, false, s));
+            KNN_CUDA(launch_tc(a, splits, true, s));
+            launches += 2;
+        } else {
+            KNN_CUDA(launch_simt(corpus, nview, ldc * stride, cn_view, queries, Q, ldq, D, kp, c.qtile, split_len,
+                                 splits, part, thr, s, redo));
+            ++launches;
+        }
+        return KNNS_OK;
+    };
+
+    if (pilot) {
+        float* cn_s = (float*)E.cn_s.p;
+        KNN_CUDA(launch_gather_norms(cn, ns, sample_stride, cn_s, ns_pad, s));
+        KNN_CUDA(cudaMemsetAsync(thr_g, 0xFF, Q * sizeof(uint32_t), s));
+        rc = fused_pass(ns, sample_stride, cn_s, kp1, stages1, splits1, split_len1, thr_g, nullptr, false);
         if (rc) return rc;
-        rc = encode_rows(&a.tm_lo, (const float*)E.lo.p, N, c.dp);
-        if (rc) return rc;
-        rc = encode_rows_bf16(&a.tm_bf, E.bf.p, N, c.dpb);
-        if (rc) return rc;
-        a.not_exact = (const uint32_t*)E.loflags.p + cdiv(N, 128) + 1;
-        a.dpb = c.dpb;
-        a.cn = cn;
-        a.queries = queries;
-        a.Q = Q;
-        a.ldq = ldq;
-        a.N = N;
-        a.split_len = c.split_len;
-        a.part = part;
-        a.thr_g = thr_g;
-        a.lo_flags = (const uint32_t*)E.loflags.p;
-        a.corpus_any_lo = (const uint32_t*)E.loflags.p + cdiv(N, 128);
-        a.dump = nullptr;
-        a.err = (int*)E.err.p;
-        a.D = D;
-        a.dp = c.dp;
-        a.kp = c.kp;
-        a.stages = c.stages;
-        // both precisions are launched; the one that does not match the data returns at once
-        KNN_CUDA(launch_tc(a, c.splits, false, s));
-        KNN_CUDA(launch_tc(a, c.splits, true, s));
-        ++launches;
+        SelectExtra ex;
+        ex.thr_out = thr_g;
+        ex.thr_rank = rank;
+        ex.qtile = c.qtile;
+        KNN_CUDA(launch_select(part, splits1, Q, kp1, std::min(kp1, (int)ns), corpus, ldc, queries, ldq, D, 0,
+                               nullptr, nullptr, nullptr, nullptr, s, ex));
+        launches += 2;
     } else {
-        KNN_CUDA(launch_simt(corpus, N, ldc, cn, queries, Q, ldq, D, c.kp, c.qtile, c.split_len, c.splits, part,
-                             thr_g, s));
+        KNN_CUDA(cudaMemsetAsync(thr_g, 0xFF, Q * sizeof(uint32_t), s));
     }
-    ++launches;
+    rc = fused_pass(N, 1, cn, c.kp, c.stages, c.splits, c.split_len, thr_g, nullptr, true);
+    if (rc) return rc;
     if (tv[2]) KNN_CUDA(cudaEventRecord(tv[2], s));
+    SelectExtra ex;
+    ex.qtile = c.qtile;
+    uint32_t* redo = (uint32_t*)E.redo.p;
+    if (pilot) {
+        KNN_CUDA(cudaMemsetAsync(redo, 0, qt * sizeof(uint32_t), s));
+        ex.redo_out = redo;
+        ex.need = (int)std::min<int64_t>(c.kp, N);
+    }
     KNN_CUDA(launch_select(part, c.splits, Q, c.kp, k, corpus, ldc, queries, ldq, D, c.rerank,
-                           c.rerank ? nullptr : (const float*)E.qn.p, dist, idx, idx_f, s));
+                           c.rerank ? nullptr : (const float*)E.qn.p, dist, idx, idx_f, s, ex));
     ++launches;
+    if (pilot) {
+        // fix-up: flagged query tiles again, unseeded (CTAs of other tiles return at once)
+        uint32_t* thr2 = (uint32_t*)E.thr2.p;
+        KNN_CUDA(cudaMemsetAsync(thr2, 0xFF, Q * sizeof(uint32_t), s));
+        rc = fused_pass(N, 1, cn, c.kp, c.stages, c.splits, c.split_len, thr2, redo, true);
+        if (rc) return rc;
+        SelectExtra ex2;
+        ex2.qtile = c.qtile;
+        ex2.redo_in = redo;
+        KNN_CUDA(launch_select(part, c.splits, Q, c.kp, k, corpus, ldc, queries, ldq, D, c.rerank,
+                               c.rerank ? nullptr : (const float*)E.qn.p, dist, idx, idx_f, s, ex2));
+        ++launches;
+    }
     if (tv[3]) KNN_CUDA(cudaEventRecord(tv[3], s));
     KNN_CUDA(cudaEventRecord(E.last_done, s));
-    if (st) *st = knns_stats{c.algo, c.splits, c.kp, c.stages, launches, 0, (int64_t)ws};
+    if (st) *st = knns_stats{c.algo, c.splits, c.kp, c.stages, launches, pilot ? 1 : 0, (int64_t)ws};
     return KNNS_OK;
 }
 
@@ -461,6 +539,8 @@ void knns_default_options(knns_options* opt)
     opt->splits = 0;
     opt->rerank = 1;
     opt->kp = 0;
+    opt->timing = 0;
+    opt->pilot = 1;
 }
 
 int knns_search_device(const float* corpus, int64_t N, int64_t ldc, const float* queries, int64_t Q, int64_t ldq,

@@ -22,6 +22,7 @@ struct Config {
     int algo = 0;
     int kp = 0;
     int rerank = 1;
+    bool pilot = true;
     int splits = 1;
     int64_t split_len = 0;
     int qtile = 128;
@@ -36,7 +37,7 @@ struct Engine {
     int cc = 0;
     std::mutex mu;
     cudaEvent_t last_done = nullptr;
-    DevBuf cn, qn, part, hi, lo, bf, err, thr, loflags;
+    DevBuf cn, qn, part, hi, lo, bf, err, thr, loflags, cn_s, thr2, redo;
     DevBuf in_corpus, in_queries, out_dist, out_idx;
     // stage timing: 4 events per timed search (start, after prep, after fused, end)
     std::vector<cudaEvent_t> tev;

@@ -33,8 +33,10 @@ template <int QPB>
 __global__ void __launch_bounds__(kThreads)
 simt_kernel(const float* __restrict__ corpus, int64_t N, int64_t ldc, const float* __restrict__ cn,
             const float* __restrict__ queries, int64_t Q, int64_t ldq, int D, int kp,
-            int64_t split_len, uint64_t* __restrict__ part, uint32_t* __restrict__ thr_g_all)
+            int64_t split_len, uint64_t* __restrict__ part, uint32_t* __restrict__ thr_g_all,
+            const uint32_t* __restrict__ tile_redo)
 {
+    if (tile_redo != nullptr && tile_redo[blockIdx.x] == 0u) return;
     constexpr int RQ = QPB / 16;
     extern __shared__ __align__(16) unsigned char smem[];
     float* qs = reinterpret_cast<float*>(smem);
@@ -140,7 +142,8 @@ size_t simt_smem_bytes(int qpb, int kp)
 
 cudaError_t launch_simt(const float* corpus, int64_t N, int64_t ldc, const float* cn,
                         const float* queries, int64_t Q, int64_t ldq, int D, int kp, int qpb,
-                        int64_t split_len, int splits, uint64_t* part, uint32_t* thr_g, cudaStream_t s)
+                        int64_t split_len, int splits, uint64_t* part, uint32_t* thr_g, cudaStream_t s,
+                        const uint32_t* tile_redo)
 {
     size_t smem = simt_smem_bytes(qpb, kp);
     dim3 grid((unsigned)((Q + qpb - 1) / qpb), (unsigned)splits);
@@ -149,13 +152,13 @@ cudaError_t launch_simt(const float* corpus, int64_t N, int64_t ldc, const float
                                              (int)smem);
         if (e != cudaSuccess) return e;
         simt_kernel<128><<<grid, kThreads, smem, s>>>(corpus, N, ldc, cn, queries, Q, ldq, D, kp,
-                                                      split_len, part, thr_g);
+                                                      split_len, part, thr_g, tile_redo);
     } else {
         cudaError_t e = cudaFuncSetAttribute(simt_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
         simt_kernel<32><<<grid, kThreads, smem, s>>>(corpus, N, ldc, cn, queries, Q, ldq, D, kp,
-                                                     split_len, part, thr_g);
+                                                     split_len, part, thr_g, tile_redo);
     }
     return cudaGetLastError();
 }

@@ -157,6 +157,8 @@ template <bool kBF16>
 __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant__ TcArgs a)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
+    // redo pass: only flagged query tiles run
+    if (a.tile_redo != nullptr && a.tile_redo[blockIdx.x] == 0u) return;
     // only the variant that matches the data runs
     if (a.not_exact != nullptr) {
         if ((*a.not_exact != 0u) == kBF16) return;

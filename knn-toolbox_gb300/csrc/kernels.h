@@ -39,9 +39,11 @@ cudaError_t launch_bf16(const float* x, int64_t n, int64_t ld, int D, int dpb, v
 
 // CUDA-core FP32 fused distance + shortlist.  qpb in {32, 128}.
 size_t simt_smem_bytes(int qpb, int kp);
+// tile_redo (optional): a CTA runs only when tile_redo[blockIdx.x] != 0.
 cudaError_t launch_simt(const float* corpus, int64_t N, int64_t ldc, const float* cn,
                         const float* queries, int64_t Q, int64_t ldq, int D, int kp, int qpb,
-                        int64_t split_len, int splits, uint64_t* part, uint32_t* thr_g, cudaStream_t s);
+                        int64_t split_len, int splits, uint64_t* part, uint32_t* thr_g, cudaStream_t s,
+                        const uint32_t* tile_redo = nullptr);
 
 // Tensor-core 3xTF32 fused distance + shortlist (tcgen05, TMA, TMEM).
 struct TcArgs {
@@ -59,6 +61,7 @@ struct TcArgs {
     const uint32_t* lo_flags; // [ceil(N/128)] 1 when the corpus tile has a nonzero TF32 low part, or null
     const uint32_t* corpus_any_lo;  // 1 when any corpus tile has a low part (null: assume so)
     const uint32_t* not_exact;      // 0 when corpus and queries are BF16-exact (null: TF32 path only)
+    const uint32_t* tile_redo;      // optional: a CTA runs only when tile_redo[blockIdx.x] != 0
     float* dump;              // optional: raw dot tile of CTA (0,0), tile 0, [128][128]
     int* err;                 // device error word
     int D;
@@ -74,10 +77,28 @@ int tc_max_stages(int kp);
 cudaError_t launch_tc(const TcArgs& a, int splits, bool bf16, cudaStream_t s);
 
 // Merge of the per-split shortlists, optional exact re-rank, final top-k.
+// Extra modes (all optional):
+//  * thr_out: instead of results, write the order-mapped key of the merged
+//    shortlist's entry thr_rank (1-based; all ones when missing) per query;
+//  * redo_out / need: when the merged shortlist holds fewer than `need` real
+//    entries, set redo_out[q / qtile] = 1 and write no result for q;
+//  * redo_in: process only queries whose tile has redo_in[q / qtile] != 0.
+struct SelectExtra {
+    uint32_t* thr_out = nullptr;
+    int thr_rank = 0;
+    uint32_t* redo_out = nullptr;
+    int need = 0;
+    const uint32_t* redo_in = nullptr;
+    int qtile = 128;
+};
 size_t select_smem_bytes(int kp, int D, int rerank);
 cudaError_t launch_select(const uint64_t* part, int splits, int64_t Q, int kp, int k,
                           const float* corpus, int64_t ldc, const float* queries, int64_t ldq,
                           int D, int rerank, const float* qn, float* out_dist, int32_t* out_idx,
-                          float* out_idx_f, cudaStream_t s);
+                          float* out_idx_f, cudaStream_t s, const SelectExtra& ex = SelectExtra());
+
+// out[i] = src[i * stride] for i < n, +inf for n <= i < n_pad (norms of a strided corpus sample).
+cudaError_t launch_gather_norms(const float* src, int64_t n, int64_t stride, float* out, int64_t n_pad,
+                                cudaStream_t s);
 
 }  // namespace knn

@@ -103,6 +103,22 @@ __global__ void split_tiles_kernel(const float* __restrict__ x, int64_t n, int64
     }
 }
 
+__global__ void gather_norms_kernel(const float* __restrict__ src, int64_t n, int64_t stride, float* __restrict__ out,
+                                    int64_t n_pad)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_pad) return;
+    out[i] = i < n ? src[i * stride] : __int_as_float(0x7f800000);
+}
+
+cudaError_t launch_gather_norms(const float* src, int64_t n, int64_t stride, float* out, int64_t n_pad,
+                                cudaStream_t s)
+{
+    if (n_pad <= 0) return cudaSuccess;
+    gather_norms_kernel<<<(unsigned)((n_pad + 255) / 256), 256, 0, s>>>(src, n, stride, out, n_pad);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_norms(const float* x, int64_t n, int64_t ld, int D, float* out, int64_t n_pad,
                          cudaStream_t s)
 {

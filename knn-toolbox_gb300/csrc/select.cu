@@ -33,7 +33,8 @@ __global__ void __launch_bounds__(kSelWarps * 32)
 select_kernel(const uint64_t* __restrict__ part, int splits, int64_t Q, int kp, int k,
               const float* __restrict__ corpus, int64_t ldc, const float* __restrict__ queries,
               int64_t ldq, int D, int rerank, const float* __restrict__ qn,
-              float* __restrict__ out_dist, int32_t* __restrict__ out_idx, float* __restrict__ out_idx_f)
+              float* __restrict__ out_dist, int32_t* __restrict__ out_idx, float* __restrict__ out_idx_f,
+              const SelectExtra ex)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int P = pow2_at_least(kp);
@@ -48,6 +49,7 @@ select_kernel(const uint64_t* __restrict__ part, int splits, int64_t Q, int kp, 
 
     const int64_t q = (int64_t)blockIdx.x * kSelWarps + warp;
     if (q >= Q) return;
+    if (ex.redo_in != nullptr && ex.redo_in[q / ex.qtile] == 0u) return;
 
     for (int j = lane; j < kp; j += 32) cur[j] = part[(size_t)q * kp + j];
     __syncwarp();
@@ -58,6 +60,20 @@ select_kernel(const uint64_t* __restrict__ part, int splits, int64_t Q, int kp, 
         warp_merge_lists(cur, oth, nxt, kp);
         uint64_t* t = cur; cur = nxt; nxt = t;
         __syncwarp();
+    }
+
+    if (ex.thr_out != nullptr) {
+        // threshold extraction: key of the thr_rank-th entry
+        if (lane == 0) {
+            const uint64_t w = cur[ex.thr_rank - 1];
+            ex.thr_out[q] = w == kSentinel ? 0xFFFFFFFFu : (uint32_t)(w >> 32);
+        }
+        return;
+    }
+    if (ex.redo_out != nullptr && ex.need > 0 && cur[ex.need - 1] == kSentinel) {
+        // fewer entries than required passed a seeded threshold: this query's tile is redone
+        if (lane == 0) ex.redo_out[q / ex.qtile] = 1u;
+        return;
     }
 
     if (rerank) {
@@ -107,7 +123,7 @@ size_t select_smem_bytes(int kp, int D, int rerank)
 cudaError_t launch_select(const uint64_t* part, int splits, int64_t Q, int kp, int k,
                           const float* corpus, int64_t ldc, const float* queries, int64_t ldq,
                           int D, int rerank, const float* qn, float* out_dist, int32_t* out_idx,
-                          float* out_idx_f, cudaStream_t s)
+                          float* out_idx_f, cudaStream_t s, const SelectExtra& ex)
 {
     if (Q <= 0) return cudaSuccess;
     size_t smem = select_smem_bytes(kp, D, rerank);
@@ -115,7 +131,7 @@ cudaError_t launch_select(const uint64_t* part, int splits, int64_t Q, int kp, i
     if (e != cudaSuccess) return e;
     unsigned blocks = (unsigned)((Q + kSelWarps - 1) / kSelWarps);
     select_kernel<<<blocks, kSelWarps * 32, smem, s>>>(part, splits, Q, kp, k, corpus, ldc, queries, ldq, D,
-                                                       rerank, qn, out_dist, out_idx, out_idx_f);
+                                                       rerank, qn, out_dist, out_idx, out_idx_f, ex);
     return cudaGetLastError();
 }
 

@@ -45,12 +45,13 @@ class KnnsError(RuntimeError):
 
 class Options(ctypes.Structure):
     _fields_ = [("algo", ctypes.c_int), ("splits", ctypes.c_int), ("rerank", ctypes.c_int),
-                ("kp", ctypes.c_int), ("timing", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+                ("kp", ctypes.c_int), ("timing", ctypes.c_int), ("pilot", ctypes.c_int),
+                ("reserved", ctypes.c_int * 2)]
 
 
 class Stats(ctypes.Structure):
     _fields_ = [("algo", ctypes.c_int), ("splits", ctypes.c_int), ("kp", ctypes.c_int),
-                ("stages", ctypes.c_int), ("launches", ctypes.c_int), ("reserved", ctypes.c_int),
+                ("stages", ctypes.c_int), ("launches", ctypes.c_int), ("pilot", ctypes.c_int),
                 ("workspace_bytes", ctypes.c_int64)]
 
 
@@ -112,11 +113,12 @@ def _check(rc):
         raise KnnsError(rc, last_error())
 
 
-def options(algo=ALGO_AUTO, splits=0, rerank=True, kp=0, timing=False) -> Options:
+def options(algo=ALGO_AUTO, splits=0, rerank=True, kp=0, timing=False, pilot=True) -> Options:
     o = Options()
     lib().knns_default_options(ctypes.byref(o))
     o.algo, o.splits, o.rerank, o.kp = int(algo), int(splits), int(bool(rerank)), int(kp)
     o.timing = int(bool(timing))
+    o.pilot = int(bool(pilot))
     return o
 
 
@@ -132,7 +134,7 @@ def last_stats() -> dict:
     s = Stats()
     _check(lib().knns_last_stats(ctypes.byref(s)))
     return {"algo": s.algo, "splits": s.splits, "kp": s.kp, "stages": s.stages, "launches": s.launches,
-            "workspace_bytes": s.workspace_bytes}
+            "pilot": s.pilot, "workspace_bytes": s.workspace_bytes}
 
 
 # --------------------------------------------------------------------------
@@ -140,7 +142,7 @@ def last_stats() -> dict:
 # --------------------------------------------------------------------------
 
 def search(corpus, queries, k, *, dist=None, idx=None, algo=ALGO_AUTO, splits=0, rerank=True, kp=0,
-           stream=None, check=True, timing=False):
+           stream=None, check=True, timing=False, pilot=True):
     """kNN on CUDA tensors (float32, rows contiguous).  Returns (dist[Q,k] f32, idx[Q,k] i32)."""
     import torch
     assert corpus.is_cuda and queries.is_cuda, "search() takes device tensors"
@@ -154,7 +156,7 @@ def search(corpus, queries, k, *, dist=None, idx=None, algo=ALGO_AUTO, splits=0,
     if idx is None:
         idx = torch.empty((Q, k), dtype=torch.int32, device=corpus.device)
     s = torch.cuda.current_stream(corpus.device) if stream is None else stream
-    o = options(algo, splits, rerank, kp, timing)
+    o = options(algo, splits, rerank, kp, timing, pilot)
     rc = lib().knns_search_device(corpus.data_ptr(), N, corpus.stride(0), queries.data_ptr(), Q,
                                   queries.stride(0), D, k, dist.data_ptr(), idx.data_ptr(), ctypes.byref(o),
                                   ctypes.c_void_p(s.cuda_stream))

@@ -252,3 +252,41 @@ def test_int_1m_x128_q10000_k100(engine, oracle):
     od, oi = oracle.knn_gemm(X, Qs[sub], 100, kp=st["kp"], rerank=True)
     np.testing.assert_array_equal(i[sub], oi)
     np.testing.assert_array_equal(d[sub], od)
+
+
+# ---------------------------------------------------------------- threshold seeding (pilot pass)
+@pytest.mark.parametrize("algo", [1, 2])
+@pytest.mark.parametrize("kind", ["uniform", "int"])
+def test_pilot_does_not_change_results(engine, oracle, algo, kind):
+    import cuknns.synth as S
+    if kind == "uniform":
+        X, Qs = S.uniform(70000, 64, seed=3, nq=200)
+    else:
+        X, Qs = S.int_descriptor(70000, 64, seed=4, nq=200)
+    k = 24
+    d0, i0, st0 = run(engine, X, Qs, k, algo=algo, pilot=False)
+    d1, i1, st1 = run(engine, X, Qs, k, algo=algo, pilot=True)
+    assert st0["pilot"] == 0 and st1["pilot"] == 1
+    np.testing.assert_array_equal(i0, i1)
+    np.testing.assert_array_equal(d0, d1)
+    od, oi = oracle.knn_gemm(X, Qs, k, kp=st1["kp"], rerank=True)
+    oracle.check_parity(X, Qs, k, d1, i1, ref_idx=oi, gap_rel=GAP, dist_rel=DIST_REL)
+
+
+@pytest.mark.parametrize("algo", [1, 2])
+def test_pilot_fixup_on_unrepresentative_sample(engine, oracle, algo):
+    # Only every 16th corpus row (the pilot's sample) lies near the queries, so
+    # the seeded threshold admits fewer than kp rows: the fix-up pass must redo
+    # those query tiles and the result must still be exact.
+    rng = np.random.default_rng(77)
+    N, D, Q, k = 16 * 4096, 32, 150, 10
+    Qs = rng.random((Q, D), dtype=np.float32)
+    X = (10.0 + rng.random((N, D), dtype=np.float32)).astype(np.float32)
+    near = np.arange(0, N, 16)
+    X[near] = Qs[rng.integers(0, Q, near.size)] + 0.01 * rng.random((near.size, D), dtype=np.float32)
+    d, i, st = run(engine, X, Qs, k, algo=algo)
+    assert st["pilot"] == 1
+    od, oi = oracle.knn_gemm(X, Qs, k, kp=st["kp"], rerank=True)
+    oracle.check_parity(X, Qs, k, d, i, ref_idx=oi, gap_rel=GAP, dist_rel=DIST_REL, dist_abs=1e-6)
+    d0, i0, _ = run(engine, X, Qs, k, algo=algo, pilot=False)
+    np.testing.assert_array_equal(i, i0)
