@@ -289,7 +289,8 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         kp1 = std::max(32, round16(rank));
         stages1 = c.algo == KNNS_ALGO_TC ? std::min(4, tc_max_stages(kp1)) : 0;
         const int64_t tiles1 = cdiv(ns, tile_n);
-        splits1 = auto_splits(qt, tiles1, E.sms, 64);
+        // at most one wave of CTAs: every extra split pays its own shortlist warm-up
+        splits1 = (int)std::max<int64_t>(1, std::min<int64_t>(tiles1, E.sms / std::max(1, qt)));
         split_len1 = cdiv(tiles1, splits1) * tile_n;
         splits1 = (int)cdiv(ns, split_len1);
         rc = E.cn_s.ensure((size_t)ns_pad * sizeof(float));
