@@ -36,6 +36,9 @@ WORKLOADS = {
                   gen="int_descriptor", N=1_000_000, D=128, Q=10_000, k=100, seed=1),
     "uniform64k": dict(desc="uniform [0,1) corpus 65,536 x 128, 1,024 queries, k=16, seed 0",
                        gen="uniform", N=65_536, D=128, Q=1_024, k=16, seed=0),
+    "mix4m": dict(desc="Gaussian mixture corpus 4,000,000 x 96 (1,024 centres N(0,1), sigma 0.15, rows "
+                       "L2-normalised), 10,000 queries, k=10, seed 2",
+                  gen="gauss_mixture", N=4_000_000, D=96, Q=10_000, k=10, seed=2),
     # profiling-sized cut of int1m (corpus still larger than L2) for ncu captures
     "int256k": dict(desc="int-descriptor corpus 262,144 x 128, 10,000 queries, k=100, seed 1",
                     gen="int_descriptor", N=262_144, D=128, Q=10_000, k=100, seed=1),
@@ -241,8 +244,11 @@ def run_gb300(args, w):
     idx_out = torch.empty((Q, k), dtype=torch.int32, device=dev)
     stream = torch.cuda.current_stream(dev)
 
+    prec = cuknns.PREC_BF16 if args.precision == "bf16" else cuknns.PREC_EXACT
+
     def step(timing=False):
-        cuknns.search(c, q, k, dist=dist_out, idx=idx_out, stream=stream, check=False, timing=timing)
+        cuknns.search(c, q, k, dist=dist_out, idx=idx_out, stream=stream, check=False, timing=timing,
+                      precision=prec, shortlist=args.shortlist)
 
     for _ in range(args.warmup):
         step()
@@ -275,9 +281,24 @@ def run_gb300(args, w):
         el_ms = float(t.item())
     value = Q * args.steps * world / (el_ms / 1e3)
 
+    # ---- accuracy against the FP64 oracle on a query sample
+    accuracy = None
+    nrq = args.recall_queries if args.recall_queries else (100 if args.precision == "bf16" else 0)
+    if nrq and rank == 0:
+        import oracle
+        oracle.build()
+        sub = np.linspace(0, Q - 1, nrq).astype(np.int64)
+        got_i = idx_out[torch.from_numpy(sub).to(dev)].cpu().numpy()
+        got_d = dist_out[torch.from_numpy(sub).to(dev)].cpu().numpy()
+        ex_d, ex_i = oracle.knn_f64(corpus_np, queries_np[sub], k)
+        d64 = oracle.pair_dist_f64(corpus_np, queries_np[sub], got_i)
+        accuracy = {"queries": int(nrq), "recall_at_k": oracle.recall_at_k(got_i, ex_i),
+                    "max_dist_rel_err": float((np.abs(got_d - d64) / np.maximum(d64, 1e-30)).max()),
+                    "oracle": "FP64 direct difference (oracle/knn_oracle.c)"}
+
     # ---- end to end through the drop-in C ABI from pinned host buffers
     e2e = None
-    e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 20))
+    e2e_steps = 0 if (args.no_e2e or args.precision != "exact") else max(1, min(args.steps, 20))
     if e2e_steps:
         e2e = run_e2e(corpus_np, queries_np, k, Q, world, e2e_steps, barrier, dist, dev)
 
@@ -286,16 +307,24 @@ def run_gb300(args, w):
     fused_avg_ms = fused_ms / max(1, nt)
     kern = "tc_kernel" if st["algo"] == cuknns.ALGO_TC else "simt_kernel"
     if st["algo"] == cuknns.ALGO_TC:
-        # 3xTF32 issues hi.hi always and the two correction products only for
-        # tiles whose TF32 low part is nonzero (corpus tile / query tile)
-        f_c, f_q = lo_tile_fraction(corpus_np), lo_tile_fraction(queries_np)
-        products = 1.0 + f_c + f_q
-        flops = products * 2.0 * N * Q * D
-        peak = peaks["bf16_tflops"] / 2.0    # dense TF32 runs at half the BF16 rate
+        # executed tensor work of the fused stage (main pass + the 1/16-sample pilot pass)
+        pilot_f = 1.0 + (1.0 / 16.0 if st["pilot"] else 0.0)
+        bf16_exact = bool(((corpus_np.view(np.uint32) & 0xFFFF) == 0).all() and
+                          ((queries_np.view(np.uint32) & 0xFFFF) == 0).all())
+        if args.precision == "bf16" or bf16_exact:
+            kind, products, peak = ("bf16 shortlist" if args.precision == "bf16" else "bf16 (data BF16-exact)",
+                                    1.0, peaks["bf16_tflops"])
+            peak_src = f"{peak_kind} bf16 dense burst"
+        else:
+            # 3xTF32 issues hi.hi always and the two correction products only for
+            # tiles whose TF32 low part is nonzero (corpus tile / query tile)
+            f_c, f_q = lo_tile_fraction(corpus_np), lo_tile_fraction(queries_np)
+            kind, products, peak = "3xTF32", 1.0 + f_c + f_q, peaks["bf16_tflops"] / 2.0
+            peak_src = f"{peak_kind} bf16 dense burst / 2 (TF32 dense rate)"
+        flops = products * 2.0 * N * Q * D * pilot_f
         roof = {"bound": "tensor", "achieved": flops / (fused_avg_ms / 1e3) / 1e12, "peak": peak,
-                "unit": "TFLOP/s",
-                "peak_source": f"{peak_kind} bf16 dense burst / 2 (TF32 dense rate)",
-                "tf32_products_per_useful_product": products}
+                "unit": "TFLOP/s", "peak_source": peak_src, "mma_kind": kind,
+                "products_per_useful_product": products, "pilot_pass_included": bool(st["pilot"])}
     else:
         flops = 2.0 * N * Q * D
         peak = 152 * 128 * 2 * 2.07e9 / 1e12
@@ -320,10 +349,11 @@ def run_gb300(args, w):
                        "parallelism": f"replicas x{world} (queries sharded, corpus replicated)",
                        "l2": "inputs larger than L2 (512 MB corpus + 1 GB TF32 hi/lo copies)" if N * D * 4 > 129e6
                        else "working set within L2 (65,536 x 128 corpus)",
-                       "algo": {1: "tcgen05 3xTF32", 2: "CUDA-core FP32"}[st["algo"]], "splits": st["splits"],
+                       "algo": {1: "tcgen05", 2: "CUDA-core FP32"}[st["algo"]], "precision": args.precision,
+                       "pilot": st["pilot"], "splits": st["splits"],
                        "shortlist": st["kp"], "stages": st["stages"]},
             "stage_ms": {"prep": prep_ms / max(1, nt), "fused": fused_avg_ms, "select": select_ms / max(1, nt)},
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "accuracy": accuracy,
             "gpu_launches": st["launches"] * args.steps,
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
@@ -341,6 +371,11 @@ def main():
     ap.add_argument("--workload", default="int1m", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
+    ap.add_argument("--precision", default="exact", choices=["exact", "bf16"],
+                    help="exact: FP32-accurate keys (plain form); bf16: BF16 shortlist + exact re-rank")
+    ap.add_argument("--shortlist", type=int, default=0, help="bf16: shortlist factor c (0 = 4)")
+    ap.add_argument("--recall-queries", type=int, default=0,
+                    help="measure recall@k and distance error against the FP64 oracle on this many queries")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -36,6 +36,11 @@ extern "C" {
 #define KNNS_ALGO_TC 1   /* tcgen05 3xTF32 fused distance + shortlist (D <= 128, shortlist <= 128) */
 #define KNNS_ALGO_SIMT 2 /* CUDA-core FP32 fused distance + shortlist (any D, shortlist <= 512) */
 
+/* precision of the ranking keys */
+#define KNNS_PREC_EXACT 0 /* FP32-accurate keys (BF16 products when the data are BF16-exact, else 3xTF32) */
+#define KNNS_PREC_BF16 1  /* BF16 keys pick a shortlist of c*k per query, re-ranked by exact distance
+                             (tensor cores, D <= 256, c*k <= 128) */
+
 typedef struct knns_options {
     int algo;        /* KNNS_ALGO_* */
     int splits;      /* corpus splits processed by independent CTAs; 0 = automatic */
@@ -45,7 +50,8 @@ typedef struct knns_options {
     int timing;      /* 1: record CUDA events around each stage (see knns_timing_collect) */
     int pilot;       /* 1 (default): seed per-query thresholds from a pass over a 1/16 corpus sample
                         (large corpora only); results are identical either way */
-    int reserved[2];
+    int precision;   /* KNNS_PREC_EXACT (default) or KNNS_PREC_BF16 */
+    int shortlist;   /* KNNS_PREC_BF16: shortlist factor c, kp = c*k rounded up to 16 (0 = 4) */
 } knns_options;
 
 typedef struct knns_stats {

@@ -199,6 +199,33 @@ int resolve_config(const Engine& E, int64_t N, int64_t Q, int D, int k, const kn
 {
     c->rerank = o.rerank ? 1 : 0;
     c->pilot = o.pilot != 0;
+    c->precision = o.precision;
+    if (o.precision == KNNS_PREC_BF16) {
+        // BF16 keys rank a shortlist of c*k; the exact re-rank picks the k
+        if (!o.rerank) return set_error(KNNS_ERR_INVALID, "BF16 precision needs the exact re-rank");
+        if (E.cc < 100) return set_error(KNNS_ERR_UNSUPPORTED, "BF16 precision needs sm_100+");
+        if (o.algo == KNNS_ALGO_SIMT) return set_error(KNNS_ERR_UNSUPPORTED, "BF16 precision runs on tensor cores");
+        const int dpb = (D + 63) & ~63;
+        if (dpb / 2 > kMaxDpTC) return set_error(KNNS_ERR_UNSUPPORTED, "BF16 precision needs D <= %d", 2 * kMaxDpTC);
+        const int cf = o.shortlist > 0 ? o.shortlist : 4;
+        c->kp = o.kp > 0 ? o.kp : std::max(32, round16(k * cf));
+        if (c->kp % 16 != 0 || c->kp < k || c->kp > kMaxKpTC)
+            return set_error(KNNS_ERR_UNSUPPORTED, "BF16 shortlist of %d entries (k=%d) outside [k, %d]", c->kp, k,
+                             kMaxKpTC);
+        c->algo = KNNS_ALGO_TC;
+        c->dp = kChunkK;  // TF32 operands unused
+        c->dpb = dpb;
+        c->stages = std::min(4, tc_max_stages(c->kp));
+        c->qtile = kTileQ;
+        const int64_t tiles = cdiv(N, kTileN);
+        int S = o.splits > 0 ? o.splits : auto_splits(cdiv(Q, kTileQ), tiles, E.sms, 64);
+        S = (int)std::max<int64_t>(1, std::min<int64_t>(S, tiles));
+        c->split_len = cdiv(tiles, S) * kTileN;
+        c->splits = (int)cdiv(N, c->split_len);
+        return KNNS_OK;
+    } else if (o.precision != KNNS_PREC_EXACT) {
+        return set_error(KNNS_ERR_INVALID, "unknown precision %d", o.precision);
+    }
     c->kp = o.kp > 0 ? o.kp : auto_kp(k, c->rerank);
     if (o.kp <= 0 && c->kp > 512 && k <= 512) c->kp = std::max(round16(k), 32);  // no margin at the limit
     if (c->kp % 16 != 0 || c->kp < k || c->kp < 32)
@@ -305,11 +332,13 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         if (rc) return rc;
         ws += E.qn.cap;
     }
+    const bool bf16_only = c.precision == KNNS_PREC_BF16;
     if (c.algo == KNNS_ALGO_TC) {
-        rc = E.hi.ensure((size_t)N * c.dp * sizeof(float));
-        if (rc) return rc;
-        rc = E.lo.ensure((size_t)N * c.dp * sizeof(float));
-        if (rc) return rc;
+        if (!bf16_only) {
+            rc = E.hi.ensure((size_t)N * c.dp * sizeof(float));
+            if (!rc) rc = E.lo.ensure((size_t)N * c.dp * sizeof(float));
+            if (rc) return rc;
+        }
         rc = E.bf.ensure((size_t)N * c.dpb * 2);
         if (rc) return rc;
         rc = E.loflags.ensure(((size_t)cdiv(N, 128) + 2) * sizeof(uint32_t));
@@ -339,12 +368,20 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         any_lo = flags + cdiv(N, 128);
         not_exact = any_lo + 1;
         KNN_CUDA(cudaMemsetAsync(any_lo, 0, 2 * sizeof(uint32_t), s));
-        // BF16 copy of the corpus and the exactness test of corpus and queries;
-        // the TF32 split then runs only for data that is not BF16-exact
-        KNN_CUDA(launch_bf16(corpus, N, ldc, D, c.dpb, E.bf.p, not_exact, s));
-        KNN_CUDA(launch_bf16(queries, Q, ldq, D, c.dpb, nullptr, not_exact, s));
-        KNN_CUDA(launch_split(corpus, N, ldc, D, c.dp, (float*)E.hi.p, (float*)E.lo.p, flags, any_lo, not_exact, s));
-        launches += 3;
+        if (bf16_only) {
+            // BF16 keys whatever the data: the "not exact" word stays 0 (the
+            // conversion reports into the unused any_lo word instead)
+            KNN_CUDA(launch_bf16(corpus, N, ldc, D, c.dpb, E.bf.p, any_lo, s));
+            launches += 1;
+        } else {
+            // BF16 copy of the corpus and the exactness test of corpus and queries;
+            // the TF32 split then runs only for data that is not BF16-exact
+            KNN_CUDA(launch_bf16(corpus, N, ldc, D, c.dpb, E.bf.p, not_exact, s));
+            KNN_CUDA(launch_bf16(queries, Q, ldq, D, c.dpb, nullptr, not_exact, s));
+            KNN_CUDA(launch_split(corpus, N, ldc, D, c.dp, (float*)E.hi.p, (float*)E.lo.p, flags, any_lo, not_exact,
+                                  s));
+            launches += 3;
+        }
     }
     if (tv[1]) KNN_CUDA(cudaEventRecord(tv[1], s));
 
@@ -354,8 +391,11 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         if (c.algo == KNNS_ALGO_TC) {
             TcArgs a;
             memset(&a, 0, sizeof(a));
-            int r = encode_rows(&a.tm_hi, (const float*)E.hi.p, nview, c.dp, stride * c.dp);
-            if (!r) r = encode_rows(&a.tm_lo, (const float*)E.lo.p, nview, c.dp, stride * c.dp);
+            int r = 0;
+            if (!bf16_only) {
+                r = encode_rows(&a.tm_hi, (const float*)E.hi.p, nview, c.dp, stride * c.dp);
+                if (!r) r = encode_rows(&a.tm_lo, (const float*)E.lo.p, nview, c.dp, stride * c.dp);
+            }
             if (!r) r = encode_rows_bf16(&a.tm_bf, E.bf.p, nview, c.dpb, stride * c.dpb);
             if (r) return r;
             a.not_exact = not_exact;
@@ -378,9 +418,12 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
             a.kp = kp;
             a.stages = stages;
             // both precisions are launched; the one that does not match the data returns at once
-            KNN_CUDA(launch_tc(a, splits, false, s));
+            if (!bf16_only) {
+                KNN_CUDA(launch_tc(a, splits, false, s));
+                ++launches;
+            }
             KNN_CUDA(launch_tc(a, splits, true, s));
-            launches += 2;
+            ++launches;
         } else {
             KNN_CUDA(launch_simt(corpus, nview, ldc * stride, cn_view, queries, Q, ldq, D, kp, c.qtile, split_len,
                                  splits, part, thr, s, redo));
@@ -542,6 +585,8 @@ void knns_default_options(knns_options* opt)
     opt->kp = 0;
     opt->timing = 0;
     opt->pilot = 1;
+    opt->precision = KNNS_PREC_EXACT;
+    opt->shortlist = 0;
 }
 
 int knns_search_device(const float* corpus, int64_t N, int64_t ldc, const float* queries, int64_t Q, int64_t ldq,

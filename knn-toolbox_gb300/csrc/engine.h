@@ -23,6 +23,7 @@ struct Config {
     int kp = 0;
     int rerank = 1;
     bool pilot = true;
+    int precision = 0;
     int splits = 1;
     int64_t split_len = 0;
     int qtile = 128;

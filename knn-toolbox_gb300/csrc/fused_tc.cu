@@ -484,8 +484,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
 
 cudaError_t launch_tc(const TcArgs& a, int splits, bool bf16, cudaStream_t st)
 {
-    if (a.stages < 1 || a.stages > kMaxStages || a.dp % kChunkK != 0 || a.dp > kMaxDpTC || a.kp % 16 != 0 ||
-        a.dpb % kBoxElemsBf16 != 0 || a.dpb / 2 > kMaxDpTC)
+    if (a.stages < 1 || a.stages > kMaxStages || a.dp % kChunkK != 0 || a.kp % 16 != 0 ||
+        a.dpb % kBoxElemsBf16 != 0 || a.dpb / 2 > kMaxDpTC || (!bf16 && a.dp > kMaxDpTC))
         return cudaErrorInvalidValue;
     const size_t smem = tc_smem_bytes(a.kp, a.stages);
     dim3 grid((unsigned)((a.Q + kTileQ - 1) / kTileQ), (unsigned)splits);

@@ -28,6 +28,7 @@ PKG = os.path.dirname(HERE)
 LIB_PATH = os.path.join(PKG, "_build", "libknngb300.so")
 
 ALGO_AUTO, ALGO_TC, ALGO_SIMT = 0, 1, 2
+PREC_EXACT, PREC_BF16 = 0, 1
 OK, ERR_INVALID, ERR_CUDA, ERR_UNSUPPORTED, ERR_DEVICE_TIMEOUT, ERR_NOMEM = range(6)
 
 # Every symbol include/knn_gb300.h and include/cuknns.h declare.
@@ -46,7 +47,7 @@ class KnnsError(RuntimeError):
 class Options(ctypes.Structure):
     _fields_ = [("algo", ctypes.c_int), ("splits", ctypes.c_int), ("rerank", ctypes.c_int),
                 ("kp", ctypes.c_int), ("timing", ctypes.c_int), ("pilot", ctypes.c_int),
-                ("reserved", ctypes.c_int * 2)]
+                ("precision", ctypes.c_int), ("shortlist", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -113,12 +114,14 @@ def _check(rc):
         raise KnnsError(rc, last_error())
 
 
-def options(algo=ALGO_AUTO, splits=0, rerank=True, kp=0, timing=False, pilot=True) -> Options:
+def options(algo=ALGO_AUTO, splits=0, rerank=True, kp=0, timing=False, pilot=True, precision=PREC_EXACT,
+            shortlist=0) -> Options:
     o = Options()
     lib().knns_default_options(ctypes.byref(o))
     o.algo, o.splits, o.rerank, o.kp = int(algo), int(splits), int(bool(rerank)), int(kp)
     o.timing = int(bool(timing))
     o.pilot = int(bool(pilot))
+    o.precision, o.shortlist = int(precision), int(shortlist)
     return o
 
 
@@ -142,7 +145,7 @@ def last_stats() -> dict:
 # --------------------------------------------------------------------------
 
 def search(corpus, queries, k, *, dist=None, idx=None, algo=ALGO_AUTO, splits=0, rerank=True, kp=0,
-           stream=None, check=True, timing=False, pilot=True):
+           stream=None, check=True, timing=False, pilot=True, precision=PREC_EXACT, shortlist=0):
     """kNN on CUDA tensors (float32, rows contiguous).  Returns (dist[Q,k] f32, idx[Q,k] i32)."""
     import torch
     assert corpus.is_cuda and queries.is_cuda, "search() takes device tensors"
@@ -156,7 +159,7 @@ def search(corpus, queries, k, *, dist=None, idx=None, algo=ALGO_AUTO, splits=0,
     if idx is None:
         idx = torch.empty((Q, k), dtype=torch.int32, device=corpus.device)
     s = torch.cuda.current_stream(corpus.device) if stream is None else stream
-    o = options(algo, splits, rerank, kp, timing, pilot)
+    o = options(algo, splits, rerank, kp, timing, pilot, precision, shortlist)
     rc = lib().knns_search_device(corpus.data_ptr(), N, corpus.stride(0), queries.data_ptr(), Q,
                                   queries.stride(0), D, k, dist.data_ptr(), idx.data_ptr(), ctypes.byref(o),
                                   ctypes.c_void_p(s.cuda_stream))

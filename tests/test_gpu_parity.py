@@ -290,3 +290,29 @@ def test_pilot_fixup_on_unrepresentative_sample(engine, oracle, algo):
     oracle.check_parity(X, Qs, k, d, i, ref_idx=oi, gap_rel=GAP, dist_rel=DIST_REL, dist_abs=1e-6)
     d0, i0, _ = run(engine, X, Qs, k, algo=algo, pilot=False)
     np.testing.assert_array_equal(i, i0)
+
+
+# ---------------------------------------------------------------- precision form: BF16 shortlist + exact re-rank
+@pytest.mark.parametrize("D,c", [(96, 4), (256, 2)])
+def test_bf16_shortlist_recall_and_exact_distances(engine, oracle, D, c):
+    import cuknns.synth as S
+    X, Qs = S.gauss_mixture(60000, D, seed=5, nq=120, centres=256)
+    k = 10
+    d, i, st = run(engine, X, Qs, k, precision=engine.PREC_BF16, shortlist=c)
+    assert st["algo"] == engine.ALGO_TC and st["kp"] >= c * k
+    ex = oracle.knn_f64(X, Qs, k)
+    rec = oracle.recall_at_k(i, ex[1])
+    assert rec >= 0.99, rec
+    # every returned distance is the exact distance of the returned index (re-rank in FP32)
+    got64 = oracle.pair_dist_f64(X, Qs, i)
+    assert (np.abs(d - got64) <= 1e-5 * got64 + 1e-6).all()
+    assert (np.diff(d, axis=1) >= 0).all()
+
+
+def test_bf16_shortlist_on_bf16_exact_data_is_exact(engine, oracle):
+    X, Qs = data_int(20000, 200, 64, 9)
+    k = 16
+    d, i, st = run(engine, X, Qs, k, precision=engine.PREC_BF16, shortlist=2)
+    od, oi = oracle.knn_gemm(X, Qs, k, kp=st["kp"], rerank=True)
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_array_equal(d, od)
