@@ -246,15 +246,17 @@ def run_gb300(args, w):
 
     prec = cuknns.PREC_BF16 if args.precision == "bf16" else cuknns.PREC_EXACT
 
+    scan_mode = {"auto": cuknns.SCAN_AUTO, "on": cuknns.SCAN_ON, "off": cuknns.SCAN_OFF}[args.scan]
+
     def step(timing=False):
         cuknns.search(c, q, k, dist=dist_out, idx=idx_out, stream=stream, check=False, timing=timing,
-                      precision=prec, shortlist=args.shortlist)
+                      precision=prec, shortlist=args.shortlist, scan=scan_mode, scan_boxes=args.scan_boxes)
 
     for _ in range(args.warmup):
         step()
     cuknns.lib().knns_check_device(None)
     st = cuknns.last_stats()
-    cuknns.timing_collect()  # drop anything recorded so far
+    cuknns.timing_collect5()  # drop anything recorded so far
 
     def barrier():
         if dist is not None:
@@ -271,7 +273,7 @@ def run_gb300(args, w):
         torch.cuda.synchronize()
     barrier()
     el_ms = e0.elapsed_time(e1)
-    prep_ms, fused_ms, select_ms, nt = cuknns.timing_collect()
+    prep_ms, seed_ms, fused_ms, select_ms, fix_ms, nt = cuknns.timing_collect5()
     rc = cuknns.lib().knns_check_device(None)
     if rc != 0:
         raise RuntimeError(cuknns.last_error())
@@ -302,15 +304,24 @@ def run_gb300(args, w):
     if e2e_steps:
         e2e = run_e2e(corpus_np, queries_np, k, Q, world, e2e_steps, barrier, dist, dev)
 
-    # ---- roofline of the dominant kernel (fused distance + shortlist)
+    # ---- roofline of the dominant kernel (the main fused distance pass)
     peaks, peak_kind = measured_peaks()
-    fused_avg_ms = fused_ms / max(1, nt)
-    kern = "tc_kernel" if st["algo"] == cuknns.ALGO_TC else "simt_kernel"
-    if st["algo"] == cuknns.ALGO_TC:
+    bf16_exact = bool(((corpus_np.view(np.uint32) & 0xFFFF) == 0).all() and
+                      ((queries_np.view(np.uint32) & 0xFFFF) == 0).all())
+    on_scan = bool(st["scan"]) and (args.precision == "bf16" or bf16_exact)
+    kern = "scan_kernel" if on_scan else ("tc_kernel" if st["algo"] == cuknns.ALGO_TC else "simt_kernel")
+    # shortlist kernels: the fused stage includes their pilot pass
+    fused_avg_ms = (fused_ms if on_scan else seed_ms + fused_ms) / max(1, nt)
+    if on_scan:
+        # the main pass alone is timed (seeding passes are their own stage); one BF16 product per pair
+        flops = 2.0 * N * Q * D
+        roof = {"bound": "tensor", "achieved": flops / (fused_avg_ms / 1e3) / 1e12, "peak": peaks["bf16_tflops"],
+                "unit": "TFLOP/s", "peak_source": f"{peak_kind} bf16 dense burst",
+                "mma_kind": "bf16 (kind::f16, M128 N256)", "products_per_useful_product": 1.0,
+                "flops_per_launch": flops, "padded_k": int(-(-D // 64) * 64)}
+    elif st["algo"] == cuknns.ALGO_TC:
         # executed tensor work of the fused stage (main pass + the 1/16-sample pilot pass)
         pilot_f = 1.0 + (1.0 / 16.0 if st["pilot"] else 0.0)
-        bf16_exact = bool(((corpus_np.view(np.uint32) & 0xFFFF) == 0).all() and
-                          ((queries_np.view(np.uint32) & 0xFFFF) == 0).all())
         if args.precision == "bf16" or bf16_exact:
             kind, products, peak = ("bf16 shortlist" if args.precision == "bf16" else "bf16 (data BF16-exact)",
                                     1.0, peaks["bf16_tflops"])
@@ -350,9 +361,11 @@ def run_gb300(args, w):
                        "l2": "inputs larger than L2 (512 MB corpus + 1 GB TF32 hi/lo copies)" if N * D * 4 > 129e6
                        else "working set within L2 (65,536 x 128 corpus)",
                        "algo": {1: "tcgen05", 2: "CUDA-core FP32"}[st["algo"]], "precision": args.precision,
-                       "pilot": st["pilot"], "splits": st["splits"],
-                       "shortlist": st["kp"], "stages": st["stages"]},
-            "stage_ms": {"prep": prep_ms / max(1, nt), "fused": fused_avg_ms, "select": select_ms / max(1, nt)},
+                       "pilot": st["pilot"], "splits": st["scan_splits"] if on_scan else st["splits"],
+                       "shortlist": st["kp"], "path": "threshold scan" if on_scan else "shortlist kernel",
+                       "scan_cap": st["scan_cap"], "scan_ring": st["scan_ring"], "stages": st["stages"]},
+            "stage_ms": {"prep": prep_ms / max(1, nt), "seed": seed_ms / max(1, nt), "fused": fused_ms / max(1, nt),
+                         "select": select_ms / max(1, nt), "fixup": fix_ms / max(1, nt)},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "accuracy": accuracy,
             "gpu_launches": st["launches"] * args.steps,
             "clocks": clk.summary()}
@@ -374,6 +387,9 @@ def main():
     ap.add_argument("--precision", default="exact", choices=["exact", "bf16"],
                     help="exact: FP32-accurate keys (plain form); bf16: BF16 shortlist + exact re-rank")
     ap.add_argument("--shortlist", type=int, default=0, help="bf16: shortlist factor c (0 = 4)")
+    ap.add_argument("--scan", default="auto", choices=["auto", "on", "off"],
+                    help="threshold-scan path for BF16 keys (auto: corpora of 131,072 rows and more)")
+    ap.add_argument("--scan-boxes", type=int, default=0, help="threshold scan: K boxes per ring slot (0 = auto)")
     ap.add_argument("--recall-queries", type=int, default=0,
                     help="measure recall@k and distance error against the FP64 oracle on this many queries")
     args = ap.parse_args()

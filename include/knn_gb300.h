@@ -41,6 +41,13 @@ extern "C" {
 #define KNNS_PREC_BF16 1  /* BF16 keys pick a shortlist of c*k per query, re-ranked by exact distance
                              (tensor cores, D <= 256, c*k <= 128) */
 
+/* threshold scan: for large corpora the BF16 tensor-core pass keeps no shortlist
+   on chip; per-query thresholds seeded from two corpus samples let it collect
+   only the keys that can still enter the top-kp (results are the same) */
+#define KNNS_SCAN_AUTO 0 /* used for BF16 keys when N >= 131072 */
+#define KNNS_SCAN_ON 1   /* used for BF16 keys when N >= 16384 */
+#define KNNS_SCAN_OFF 2  /* never used */
+
 typedef struct knns_options {
     int algo;        /* KNNS_ALGO_* */
     int splits;      /* corpus splits processed by independent CTAs; 0 = automatic */
@@ -52,6 +59,9 @@ typedef struct knns_options {
                         (large corpora only); results are identical either way */
     int precision;   /* KNNS_PREC_EXACT (default) or KNNS_PREC_BF16 */
     int shortlist;   /* KNNS_PREC_BF16: shortlist factor c, kp = c*k rounded up to 16 (0 = 4) */
+    int scan;        /* KNNS_SCAN_* (default AUTO) */
+    int scan_boxes;  /* threshold scan: 64-element K boxes per shared-memory ring slot (0 = automatic) */
+    int reserved[4];
 } knns_options;
 
 typedef struct knns_stats {
@@ -62,6 +72,10 @@ typedef struct knns_stats {
     int launches;    /* kernels launched by the call */
     int pilot;       /* 1 when the threshold-seeding pilot pass ran */
     int64_t workspace_bytes;
+    int scan;        /* 1 when the threshold-scan path was launched (it runs when the keys are BF16) */
+    int scan_splits; /* corpus splits of the main threshold scan */
+    int scan_cap;    /* candidate slots per (query, split half) of the main threshold scan */
+    int scan_ring;   /* ring slots x boxes per slot, as 100 * slots + boxes */
 } knns_stats;
 
 /* Fill *opt with the defaults (automatic algo, splits and shortlist, re-rank on, pilot on). */
@@ -105,6 +119,14 @@ int knns_last_stats(knns_stats *out);
  * include/cuknns.h:43-47.)
  */
 int knns_timing_collect(double ms[3], int *count);
+
+/*
+ * As knns_timing_collect, with five stages: ms[0] preparation, ms[1] threshold
+ * seeding (pilot passes and their selections), ms[2] the main fused distance
+ * kernel, ms[3] the main merge / selection / re-rank, ms[4] the fix-up of
+ * queries whose seeded threshold did not hold.  Resets the accumulator.
+ */
+int knns_timing_collect5(double ms[5], int *count);
 
 /*
  * Allocation-free search.  No counterpart in the reference: it exists for

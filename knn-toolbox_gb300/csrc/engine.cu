@@ -148,15 +148,17 @@ static int encode_rows(CUtensorMap* m, const float* base, int64_t rows, int64_t 
     return KNNS_OK;
 }
 
-// 2-D bf16 matrix [rows][cols] (rows `pitch` elements apart), box {64 cols (128 B), 128 rows}, 128B swizzle
-static int encode_rows_bf16(CUtensorMap* m, const void* base, int64_t rows, int64_t cols, int64_t pitch = 0)
+// 2-D bf16 matrix [rows][cols] (rows `pitch` elements apart), box {64 cols (128 B), box_rows rows},
+// 128B swizzle
+static int encode_rows_bf16(CUtensorMap* m, const void* base, int64_t rows, int64_t cols, int64_t pitch = 0,
+                            int box_rows = kTileN)
 {
     EncodeTiledFn fn;
     int rc = get_encode_fn(&fn);
     if (rc) return rc;
     cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)(pitch > 0 ? pitch : cols) * 2};
-    cuuint32_t box[2] = {64u, (cuuint32_t)kTileN};
+    cuuint32_t box[2] = {64u, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -267,6 +269,87 @@ int resolve_config(const Engine& E, int64_t N, int64_t Q, int D, int k, const kn
     return KNNS_OK;
 }
 
+// ---------------------------------------------------------------- threshold-scan plan
+// Seeding: the main scan needs, per query, a threshold T with at least kp keys
+// below it (then every top-kp candidate is collected) and few more.  Two
+// sample passes give it: P0 keys every key of a 1024-row sample and picks its
+// j0-th smallest as T0; P1 collects the keys below T0 over every 16th row and
+// picks the j1-th smallest as T1, the main pass's threshold.  With m = kp/16
+// (the expected sample rank of the final kp-th key) j1 = 2m + 4 sqrt(m) + 1
+// leaves a chance of roughly 1e-5 that fewer than kp keys fall below T1; such
+// queries (and any whose segments overflow) are found by the selection and
+// searched again without a threshold, so results never depend on the seeds.
+struct ScanPlan {
+    int bps = 0, ring = 0;
+    int64_t n0 = 0, s0 = 1, len0 = 0;
+    int j0 = 0, S0 = 1, cap0 = 0;
+    int64_t n1 = 0, s1 = 16, len1 = 0;
+    int j1 = 0, S1 = 1, cap1 = 0;
+    int64_t len = 0;
+    int S = 1, cap = 0;
+    int64_t fixA_rows = 0, fixA_len = 0, fixB_rows = 0, fixB_len = 0;
+    int fixA_S = 1, fixB_S = 1;
+    size_t cand_words = 0, cnt_words = 0, part_words = 0;
+};
+
+static int seg_cap(double per_seg, double sigmas)
+{
+    return round16((int)std::ceil(sigmas * per_seg + 8.0 * std::sqrt(per_seg) + 16.0));
+}
+
+static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, const knns_options& o, ScanPlan* P)
+{
+    if (scan_plan(dpb, o.scan_boxes, &P->bps, &P->ring) != 0)
+        return set_error(KNNS_ERR_UNSUPPORTED, "threshold scan: no ring geometry for %d BF16 columns with %d boxes per slot",
+                         dpb, o.scan_boxes);
+    const int64_t qt = cdiv(Q, kTileQ);
+    const double m = (double)kp / 16.0;
+    P->s1 = 16;
+    P->n1 = cdiv(N, P->s1);
+    P->j1 = (int)std::ceil(2.0 * m + 4.0 * std::sqrt(m)) + 1;
+    P->n0 = std::min<int64_t>(N, 1024);
+    P->s0 = std::max<int64_t>(1, N / P->n0);
+    const double m0 = (double)P->j1 * (double)P->n0 / (double)P->n1;
+    P->j0 = std::min<int>((int)P->n0, (int)std::ceil(2.0 * m0 + 4.0 * std::sqrt(m0)) + 1);
+    if (P->j1 > kCandMax / 2 || P->n1 < 4 * P->j1)
+        return set_error(KNNS_ERR_UNSUPPORTED, "threshold scan: shortlist of %d too long for N=%lld", kp, (long long)N);
+    // P0: two splits of at most two tiles; each half-warp segment sees <= 256 columns, all kept
+    const int64_t tiles0 = cdiv(P->n0, kScanTileN);
+    P->S0 = (int)std::min<int64_t>(2, tiles0);
+    P->len0 = cdiv(tiles0, P->S0) * kScanTileN;
+    P->S0 = (int)cdiv(P->n0, P->len0);
+    P->cap0 = (int)(P->len0 / 2);
+    // P1
+    const int64_t tiles1 = cdiv(P->n1, kScanTileN);
+    P->S1 = auto_splits(qt, tiles1, E.sms, 64);
+    P->len1 = cdiv(tiles1, P->S1) * kScanTileN;
+    P->S1 = (int)cdiv(P->n1, P->len1);
+    const double h1 = (double)P->n1 * P->j0 / (double)P->n0;
+    P->cap1 = std::min<int>((int)(P->len1 / 2), seg_cap(h1 / (2.0 * P->S1), 3.0));
+    // main pass
+    const int64_t tiles = cdiv(N, kScanTileN);
+    P->S = o.splits > 0 ? std::min<int>(o.splits, (int)tiles) : auto_splits(qt, tiles, E.sms, 64);
+    P->len = cdiv(tiles, P->S) * kScanTileN;
+    P->S = (int)cdiv(N, P->len);
+    const double hm = (double)P->j1 * P->s1;
+    P->cap = std::min<int>((int)(P->len / 2), seg_cap(hm / (2.0 * P->S), 2.0));
+    // fix-up of failed queries: up to 512 on a full wave, the rest (rare) on 8 splits
+    const int64_t tiles128 = cdiv(N, kTileN);
+    P->fixA_rows = std::min<int64_t>(Q, 4 * kTileQ);
+    P->fixA_S = (int)std::max<int64_t>(1, std::min<int64_t>(tiles128, E.sms / cdiv(P->fixA_rows, kTileQ)));
+    P->fixA_len = cdiv(tiles128, P->fixA_S) * kTileN;
+    P->fixA_S = (int)cdiv(N, P->fixA_len);
+    P->fixB_rows = Q - P->fixA_rows;
+    P->fixB_S = (int)std::min<int64_t>(tiles128, 8);
+    P->fixB_len = cdiv(tiles128, P->fixB_S) * kTileN;
+    P->fixB_S = (int)cdiv(N, P->fixB_len);
+    P->cand_words = std::max({(size_t)2 * P->S0 * Q * P->cap0, (size_t)2 * P->S1 * Q * P->cap1,
+                              (size_t)2 * P->S * Q * P->cap});
+    P->cnt_words = (size_t)2 * std::max({P->S0, P->S1, P->S}) * Q;
+    P->part_words = std::max((size_t)P->fixA_S * P->fixA_rows * kp, (size_t)P->fixB_S * P->fixB_rows * kp);
+    return KNNS_OK;
+}
+
 // ---------------------------------------------------------------- search
 int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const float* queries, int64_t Q, int64_t ldq,
                int D, int k, float* dist, int32_t* idx, float* idx_f, const knns_options& o, cudaStream_t s,
@@ -278,32 +361,50 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     if (N > 0x7fffffffLL) return set_error(KNNS_ERR_UNSUPPORTED, "corpus larger than 2^31-1 rows");
     if (ldc < D || ldq < D) return set_error(KNNS_ERR_INVALID, "row pitch smaller than D");
     if (!corpus || (!queries && Q > 0)) return set_error(KNNS_ERR_INVALID, "null input pointer");
+    if (o.scan < KNNS_SCAN_AUTO || o.scan > KNNS_SCAN_OFF) return set_error(KNNS_ERR_INVALID, "unknown scan mode %d", o.scan);
     Config c;
     int rc = resolve_config(E, N, Q, D, k, o, &c);
     if (rc) return rc;
     if (Q == 0) {
-        if (st) *st = knns_stats{c.algo, c.splits, c.kp, c.stages, 0, 0, 0};
+        if (st) *st = knns_stats{c.algo, c.splits, c.kp, c.stages, 0, 0, 0, 0, 0, 0, 0};
         return KNNS_OK;
     }
+    const bool bf16_only = c.precision == KNNS_PREC_BF16;
 
-    const int64_t n_pad = cdiv(N, 128) * 128;
+    // The threshold scan serves BF16 keys on large corpora: always in the BF16
+    // precision form, and in the exact form when the data turn out BF16-exact
+    // (decided on the device; the TF32 path then stands down and vice versa).
+    ScanPlan sp;
+    bool scan = false;
+    if (c.algo == KNNS_ALGO_TC && o.scan != KNNS_SCAN_OFF && E.cc >= 100 && c.dpb <= 256 && c.rerank) {
+        const int64_t min_n = o.scan == KNNS_SCAN_ON ? 16384 : 131072;
+        if (N >= min_n) {
+            rc = plan_scan(E, N, Q, c.dpb, c.kp, o, &sp);
+            if (rc) return rc;
+            scan = true;
+        }
+    }
+    const bool run_old = !(scan && bf16_only);  // the shortlist path is needed (possibly gated)
+
+    const int64_t n_pad = cdiv(N, kScanTileN) * kScanTileN;
     size_t ws = 0;
     rc = E.cn.ensure(n_pad * sizeof(float));
     if (rc) return rc;
     ws += E.cn.cap;
-    rc = E.part.ensure((size_t)c.splits * Q * c.kp * sizeof(uint64_t));
-    if (rc) return rc;
-    ws += E.part.cap;
     rc = E.thr.ensure(Q * sizeof(uint32_t));
     if (rc) return rc;
     ws += E.thr.cap;
-    // Threshold seeding: a pilot pass over every s-th corpus row gives each
-    // query the key of a conservatively high rank r of its sample shortlist;
-    // the main pass drops candidates above it from the first tile on.  Exact:
-    // a query whose merged shortlist ends up with fewer than min(kp, N)
-    // entries is redone (its whole query tile) without the seed.
+    if (run_old) {
+        rc = E.part.ensure((size_t)c.splits * Q * c.kp * sizeof(uint64_t));
+        if (rc) return rc;
+    }
+    // Threshold seeding of the shortlist path: a pilot pass over every s-th
+    // corpus row gives each query the key of a conservatively high rank r of
+    // its sample shortlist; the main pass drops candidates above it from the
+    // first tile on.  Exact: a query whose merged shortlist ends up with fewer
+    // than min(kp, N) entries is redone (its whole query tile) without the seed.
     const int sample_stride = 16;
-    const bool pilot = c.pilot && N >= (int64_t)sample_stride * 4096;
+    const bool pilot = run_old && c.pilot && N >= (int64_t)sample_stride * 4096;
     const int qt = (int)cdiv(Q, c.qtile);
     const int tile_n = c.algo == KNNS_ALGO_TC ? kTileN : kSimtTileN;
     int64_t ns = 0, ns_pad = 0, split_len1 = 0;
@@ -325,14 +426,13 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         if (!rc) rc = E.redo.ensure((size_t)qt * sizeof(uint32_t));
         if (!rc) rc = E.part.ensure((size_t)splits1 * Q * kp1 * sizeof(uint64_t));
         if (rc) return rc;
-        ws += E.cn_s.cap + E.thr2.cap + E.redo.cap;
+        ws += E.cn_s.cap + E.redo.cap;
     }
     if (!c.rerank) {
         rc = E.qn.ensure(Q * sizeof(float));
         if (rc) return rc;
         ws += E.qn.cap;
     }
-    const bool bf16_only = c.precision == KNNS_PREC_BF16;
     if (c.algo == KNNS_ALGO_TC) {
         if (!bf16_only) {
             rc = E.hi.ensure((size_t)N * c.dp * sizeof(float));
@@ -345,11 +445,30 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         if (rc) return rc;
         ws += E.hi.cap + E.lo.cap + E.bf.cap + E.loflags.cap;
     }
+    const int64_t n1_pad = scan ? cdiv(sp.n1, kScanTileN) * kScanTileN : 0;
+    const int64_t n0_pad = scan ? cdiv(sp.n0, kScanTileN) * kScanTileN : 0;
+    if (scan) {
+        rc = E.qbf.ensure((size_t)Q * c.dpb * 2);
+        if (!rc) rc = E.cand.ensure(sp.cand_words * sizeof(uint64_t));
+        if (!rc) rc = E.cnt.ensure(sp.cnt_words * sizeof(uint32_t));
+        if (!rc) rc = E.tq.ensure((size_t)2 * Q * sizeof(float));
+        if (!rc) rc = E.cnv.ensure((size_t)(n0_pad + n1_pad) * sizeof(float));
+        if (!rc) rc = E.fail.ensure((size_t)(Q + 1) * sizeof(uint32_t));
+        if (!rc) rc = E.part.ensure(sp.part_words * sizeof(uint64_t));
+        if (!rc) rc = E.thr2.ensure(Q * sizeof(uint32_t));
+        if (rc) return rc;
+        ws += E.qbf.cap + E.cand.cap + E.cnt.cap + E.tq.cap + E.cnv.cap + E.fail.cap;
+    }
+    ws += E.part.cap + E.thr2.cap;
 
     KNN_CUDA(cudaStreamWaitEvent(s, E.last_done, 0));
-    cudaEvent_t tv[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t tv[Engine::kTimingEvents] = {};
     if (o.timing && E.timing_slot(tv) != KNNS_OK) return KNNS_ERR_CUDA;
-    if (tv[0]) KNN_CUDA(cudaEventRecord(tv[0], s));
+    auto mark = [&](int i) -> int {
+        if (tv[i]) KNN_CUDA(cudaEventRecord(tv[i], s));
+        return KNNS_OK;
+    };
+    if ((rc = mark(0))) return rc;
     int launches = 0;
     float* cn = (float*)E.cn.p;
     KNN_CUDA(launch_norms(corpus, N, ldc, D, cn, n_pad, s));
@@ -372,20 +491,22 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
             // BF16 keys whatever the data: the "not exact" word stays 0 (the
             // conversion reports into the unused any_lo word instead)
             KNN_CUDA(launch_bf16(corpus, N, ldc, D, c.dpb, E.bf.p, any_lo, s));
-            launches += 1;
+            KNN_CUDA(launch_bf16(queries, Q, ldq, D, c.dpb, scan ? E.qbf.p : nullptr, any_lo, s));
+            launches += 2;
         } else {
             // BF16 copy of the corpus and the exactness test of corpus and queries;
             // the TF32 split then runs only for data that is not BF16-exact
             KNN_CUDA(launch_bf16(corpus, N, ldc, D, c.dpb, E.bf.p, not_exact, s));
-            KNN_CUDA(launch_bf16(queries, Q, ldq, D, c.dpb, nullptr, not_exact, s));
+            KNN_CUDA(launch_bf16(queries, Q, ldq, D, c.dpb, scan ? E.qbf.p : nullptr, not_exact, s));
             KNN_CUDA(launch_split(corpus, N, ldc, D, c.dp, (float*)E.hi.p, (float*)E.lo.p, flags, any_lo, not_exact,
                                   s));
             launches += 3;
         }
     }
-    if (tv[1]) KNN_CUDA(cudaEventRecord(tv[1], s));
+    if ((rc = mark(1))) return rc;
 
-    // One fused pass over a corpus view: rows 0, stride, 2*stride, ... (nview of them).
+    // One shortlist pass over a corpus view: rows 0, stride, 2*stride, ... (nview
+    // of them).  With the threshold scan on, the BF16 variant is left to the scan.
     auto fused_pass = [&](int64_t nview, int64_t stride, const float* cn_view, int kp, int stages, int splits,
                           int64_t split_len, uint32_t* thr, const uint32_t* redo, bool tile_flags) -> int {
         if (c.algo == KNNS_ALGO_TC) {
@@ -422,8 +543,10 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
                 KNN_CUDA(launch_tc(a, splits, false, s));
                 ++launches;
             }
-            KNN_CUDA(launch_tc(a, splits, true, s));
-            ++launches;
+            if (!scan) {
+                KNN_CUDA(launch_tc(a, splits, true, s));
+                ++launches;
+            }
         } else {
             KNN_CUDA(launch_simt(corpus, nview, ldc * stride, cn_view, queries, Q, ldq, D, kp, c.qtile, split_len,
                                  splits, part, thr, s, redo));
@@ -431,53 +554,192 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         }
         return KNNS_OK;
     };
+    // in the exact form with the scan on, the shortlist path's selections run only for TF32 data
+    const uint32_t* old_gate = scan ? not_exact : nullptr;
 
-    if (pilot) {
-        float* cn_s = (float*)E.cn_s.p;
-        KNN_CUDA(launch_gather_norms(cn, ns, sample_stride, cn_s, ns_pad, s));
-        KNN_CUDA(cudaMemsetAsync(thr_g, 0xFF, Q * sizeof(uint32_t), s));
-        rc = fused_pass(ns, sample_stride, cn_s, kp1, stages1, splits1, split_len1, thr_g, nullptr, false);
+    if (run_old) {
+        if (pilot) {
+            float* cn_s = (float*)E.cn_s.p;
+            KNN_CUDA(launch_gather_norms(cn, ns, sample_stride, cn_s, ns_pad, s));
+            KNN_CUDA(cudaMemsetAsync(thr_g, 0xFF, Q * sizeof(uint32_t), s));
+            rc = fused_pass(ns, sample_stride, cn_s, kp1, stages1, splits1, split_len1, thr_g, nullptr, false);
+            if (rc) return rc;
+            SelectExtra ex;
+            ex.thr_out = thr_g;
+            ex.thr_rank = rank;
+            ex.qtile = c.qtile;
+            ex.skip_if_zero = old_gate;
+            KNN_CUDA(launch_select(part, splits1, Q, kp1, std::min(kp1, (int)ns), corpus, ldc, queries, ldq, D, 0,
+                                   nullptr, nullptr, nullptr, nullptr, s, ex));
+            launches += 2;
+        } else {
+            KNN_CUDA(cudaMemsetAsync(thr_g, 0xFF, Q * sizeof(uint32_t), s));
+        }
+        rc = fused_pass(N, 1, cn, c.kp, c.stages, c.splits, c.split_len, thr_g, nullptr, true);
         if (rc) return rc;
         SelectExtra ex;
-        ex.thr_out = thr_g;
-        ex.thr_rank = rank;
         ex.qtile = c.qtile;
-        KNN_CUDA(launch_select(part, splits1, Q, kp1, std::min(kp1, (int)ns), corpus, ldc, queries, ldq, D, 0,
-                               nullptr, nullptr, nullptr, nullptr, s, ex));
-        launches += 2;
-    } else {
-        KNN_CUDA(cudaMemsetAsync(thr_g, 0xFF, Q * sizeof(uint32_t), s));
-    }
-    rc = fused_pass(N, 1, cn, c.kp, c.stages, c.splits, c.split_len, thr_g, nullptr, true);
-    if (rc) return rc;
-    if (tv[2]) KNN_CUDA(cudaEventRecord(tv[2], s));
-    SelectExtra ex;
-    ex.qtile = c.qtile;
-    uint32_t* redo = (uint32_t*)E.redo.p;
-    if (pilot) {
-        KNN_CUDA(cudaMemsetAsync(redo, 0, qt * sizeof(uint32_t), s));
-        ex.redo_out = redo;
-        ex.need = (int)std::min<int64_t>(c.kp, N);
-    }
-    KNN_CUDA(launch_select(part, c.splits, Q, c.kp, k, corpus, ldc, queries, ldq, D, c.rerank,
-                           c.rerank ? nullptr : (const float*)E.qn.p, dist, idx, idx_f, s, ex));
-    ++launches;
-    if (pilot) {
-        // fix-up: flagged query tiles again, unseeded (CTAs of other tiles return at once)
-        uint32_t* thr2 = (uint32_t*)E.thr2.p;
-        KNN_CUDA(cudaMemsetAsync(thr2, 0xFF, Q * sizeof(uint32_t), s));
-        rc = fused_pass(N, 1, cn, c.kp, c.stages, c.splits, c.split_len, thr2, redo, true);
-        if (rc) return rc;
-        SelectExtra ex2;
-        ex2.qtile = c.qtile;
-        ex2.redo_in = redo;
+        ex.skip_if_zero = old_gate;
+        uint32_t* redo = (uint32_t*)E.redo.p;
+        if (pilot) {
+            KNN_CUDA(cudaMemsetAsync(redo, 0, qt * sizeof(uint32_t), s));
+            ex.redo_out = redo;
+            ex.need = (int)std::min<int64_t>(c.kp, N);
+        }
         KNN_CUDA(launch_select(part, c.splits, Q, c.kp, k, corpus, ldc, queries, ldq, D, c.rerank,
-                               c.rerank ? nullptr : (const float*)E.qn.p, dist, idx, idx_f, s, ex2));
+                               c.rerank ? nullptr : (const float*)E.qn.p, dist, idx, idx_f, s, ex));
         ++launches;
+        if (pilot) {
+            // fix-up: flagged query tiles again, unseeded (CTAs of other tiles return at once)
+            uint32_t* thr2 = (uint32_t*)E.thr2.p;
+            KNN_CUDA(cudaMemsetAsync(thr2, 0xFF, Q * sizeof(uint32_t), s));
+            rc = fused_pass(N, 1, cn, c.kp, c.stages, c.splits, c.split_len, thr2, redo, true);
+            if (rc) return rc;
+            SelectExtra ex2;
+            ex2.qtile = c.qtile;
+            ex2.redo_in = redo;
+            ex2.skip_if_zero = old_gate;
+            KNN_CUDA(launch_select(part, c.splits, Q, c.kp, k, corpus, ldc, queries, ldq, D, c.rerank,
+                                   c.rerank ? nullptr : (const float*)E.qn.p, dist, idx, idx_f, s, ex2));
+            ++launches;
+        }
     }
-    if (tv[3]) KNN_CUDA(cudaEventRecord(tv[3], s));
+
+    if (!scan) {
+        for (int i = 2; i <= 5; ++i)
+            if ((rc = mark(i))) return rc;
+    } else {
+        // ---------------------------------------------------------------- threshold scan
+        // (runs when *scan_gate == 0: always in the BF16 form, for BF16-exact data in the exact form)
+        const uint32_t* scan_gate = bf16_only ? nullptr : not_exact;
+        float* T0 = (float*)E.tq.p;
+        float* T1 = T0 + Q;
+        float* cn0 = (float*)E.cnv.p;
+        float* cn1 = cn0 + n0_pad;
+        uint32_t* fail_cnt = (uint32_t*)E.fail.p;
+        int32_t* fail_idx = (int32_t*)E.fail.p + 1;
+        ScanArgs a;
+        memset(&a, 0, sizeof(a));
+        rc = encode_rows_bf16(&a.tm_q, E.qbf.p, Q, c.dpb, c.dpb, kTileQ);
+        if (rc) return rc;
+        a.skip_if = scan_gate;
+        a.cand = (uint64_t*)E.cand.p;
+        a.cnt = (uint32_t*)E.cnt.p;
+        a.err = (int*)E.err.p;
+        a.Q = Q;
+        a.dpb = c.dpb;
+        a.bps = sp.bps;
+        a.ring = sp.ring;
+        auto scan_pass = [&](int64_t nview, int64_t stride, const float* cn_view, const float* thr, int splits,
+                             int64_t split_len, int cap) -> int {
+            int r = encode_rows_bf16(&a.tm_c, E.bf.p, nview, c.dpb, stride * c.dpb, kScanTileN);
+            if (r) return r;
+            a.cn = cn_view;
+            a.thr = thr;
+            a.N = nview;
+            a.split_len = split_len;
+            a.cap = cap;
+            KNN_CUDA(launch_scan(a, splits, s));
+            ++launches;
+            return KNNS_OK;
+        };
+        CandSelect cs;
+        cs.cand = (const uint64_t*)E.cand.p;
+        cs.cnt = (const uint32_t*)E.cnt.p;
+        cs.Q = Q;
+        cs.skip_if = scan_gate;
+        cs.D = D;
+        // P0: every key of a 1024-row sample; T0 = key of rank j0
+        KNN_CUDA(launch_gather_norms(cn, sp.n0, sp.s0, cn0, n0_pad, s));
+        if ((rc = scan_pass(sp.n0, sp.s0, cn0, nullptr, sp.S0, sp.len0, sp.cap0))) return rc;
+        cs.nseg = 2 * sp.S0;
+        cs.cap = sp.cap0;
+        cs.thr_out = T0;
+        cs.thr_rank = sp.j0;
+        cs.thr_fallback = nullptr;
+        KNN_CUDA(launch_select_cand(cs, s));
+        // P1: keys below T0 over every 16th row; T1 = key of rank j1 (T0 when that fails)
+        KNN_CUDA(launch_gather_norms(cn, sp.n1, sp.s1, cn1, n1_pad, s));
+        if ((rc = scan_pass(sp.n1, sp.s1, cn1, T0, sp.S1, sp.len1, sp.cap1))) return rc;
+        cs.nseg = 2 * sp.S1;
+        cs.cap = sp.cap1;
+        cs.thr_out = T1;
+        cs.thr_rank = sp.j1;
+        cs.thr_fallback = T0;
+        KNN_CUDA(launch_select_cand(cs, s));
+        launches += 4;
+        if ((rc = mark(2))) return rc;
+        // main pass
+        if ((rc = scan_pass(N, 1, cn, T1, sp.S, sp.len, sp.cap))) return rc;
+        if ((rc = mark(3))) return rc;
+        KNN_CUDA(cudaMemsetAsync(fail_cnt, 0, sizeof(uint32_t), s));
+        cs.nseg = 2 * sp.S;
+        cs.cap = sp.cap;
+        cs.thr_out = nullptr;
+        cs.thr_fallback = nullptr;
+        cs.kp = c.kp;
+        cs.k = k;
+        cs.need = (int)std::min<int64_t>(c.kp, N);
+        cs.rerank = c.rerank;
+        cs.corpus = corpus;
+        cs.ldc = ldc;
+        cs.queries = queries;
+        cs.ldq = ldq;
+        cs.qn = c.rerank ? nullptr : (const float*)E.qn.p;
+        cs.out_dist = dist;
+        cs.out_idx = idx;
+        cs.out_idx_f = idx_f;
+        cs.fail_idx = fail_idx;
+        cs.fail_cnt = fail_cnt;
+        KNN_CUDA(launch_select_cand(cs, s));
+        ++launches;
+        if ((rc = mark(4))) return rc;
+        // fix-up: failed queries, compacted, through the shortlist kernel without a threshold
+        // (launches whose rows are all past the failure count return at once)
+        auto fix_pass = [&](int64_t qbase, int64_t rows, int splits, int64_t split_len) -> int {
+            if (rows <= 0) return KNNS_OK;
+            TcArgs t;
+            memset(&t, 0, sizeof(t));
+            int r = encode_rows_bf16(&t.tm_bf, E.bf.p, N, c.dpb, c.dpb);
+            if (r) return r;
+            uint32_t* thr2 = (uint32_t*)E.thr2.p;
+            KNN_CUDA(cudaMemsetAsync(thr2, 0xFF, rows * sizeof(uint32_t), s));
+            t.not_exact = not_exact;  // the BF16 variant runs when the data are BF16 (always in the BF16 form)
+            t.dpb = c.dpb;
+            t.cn = cn;
+            t.queries = queries;
+            t.Q = rows;
+            t.ldq = ldq;
+            t.N = N;
+            t.split_len = split_len;
+            t.part = part;
+            t.thr_g = thr2;
+            t.qmap = fail_idx;
+            t.qcount = fail_cnt;
+            t.qbase = qbase;
+            t.err = (int*)E.err.p;
+            t.D = D;
+            t.dp = kChunkK;
+            t.kp = c.kp;
+            t.stages = std::min(4, tc_max_stages(c.kp));
+            KNN_CUDA(launch_tc(t, splits, true, s));
+            SelectExtra ex;
+            ex.qmap = fail_idx;
+            ex.qcount = fail_cnt;
+            ex.qbase = qbase;
+            KNN_CUDA(launch_select(part, splits, rows, c.kp, k, corpus, ldc, queries, ldq, D, c.rerank,
+                                   c.rerank ? nullptr : (const float*)E.qn.p, dist, idx, idx_f, s, ex));
+            launches += 2;
+            return KNNS_OK;
+        };
+        if ((rc = fix_pass(0, sp.fixA_rows, sp.fixA_S, sp.fixA_len))) return rc;
+        if ((rc = fix_pass(sp.fixA_rows, sp.fixB_rows, sp.fixB_S, sp.fixB_len))) return rc;
+        if ((rc = mark(5))) return rc;
+    }
     KNN_CUDA(cudaEventRecord(E.last_done, s));
-    if (st) *st = knns_stats{c.algo, c.splits, c.kp, c.stages, launches, pilot ? 1 : 0, (int64_t)ws};
+    if (st)
+        *st = knns_stats{c.algo, c.splits, c.kp, c.stages, launches, (pilot || scan) ? 1 : 0, (int64_t)ws,
+                         scan ? 1 : 0, scan ? sp.S : 0, scan ? sp.cap : 0, scan ? 100 * sp.ring + sp.bps : 0};
     return KNNS_OK;
 }
 
@@ -530,15 +792,15 @@ int search_host(const float* corpus, int64_t N, const float* queries, int64_t Q,
     return KNNS_OK;
 }
 
-int Engine::timing_slot(cudaEvent_t out[4])
+int Engine::timing_slot(cudaEvent_t out[kTimingEvents])
 {
-    const size_t need = (size_t)(tcount + 1) * 4;
+    const size_t need = (size_t)(tcount + 1) * kTimingEvents;
     while (tev.size() < need) {
         cudaEvent_t e;
         KNN_CUDA(cudaEventCreate(&e));
         tev.push_back(e);
     }
-    for (int i = 0; i < 4; ++i) out[i] = tev[(size_t)tcount * 4 + i];
+    for (int i = 0; i < kTimingEvents; ++i) out[i] = tev[(size_t)tcount * kTimingEvents + i];
     ++tcount;
     return KNNS_OK;
 }
@@ -587,6 +849,8 @@ void knns_default_options(knns_options* opt)
     opt->pilot = 1;
     opt->precision = KNNS_PREC_EXACT;
     opt->shortlist = 0;
+    opt->scan = KNNS_SCAN_AUTO;
+    opt->scan_boxes = 0;
 }
 
 int knns_search_device(const float* corpus, int64_t N, int64_t ldc, const float* queries, int64_t Q, int64_t ldq,
@@ -640,19 +904,18 @@ int knns_last_stats(knns_stats* out)
 
 int knns_version(void) { return 100; }
 
-int knns_timing_collect(double ms[3], int* count)
+static int timing_collect(double ms[Engine::kTimingEvents - 1], int* count)
 {
-    clear_error();
-    if (!ms) return set_error(KNNS_ERR_INVALID, "null output");
     Engine* E = nullptr;
     int rc = get_engine(&E);
     if (rc) return rc;
     std::lock_guard<std::mutex> lk(E->mu);
-    ms[0] = ms[1] = ms[2] = 0.0;
+    const int ne = Engine::kTimingEvents;
+    for (int j = 0; j < ne - 1; ++j) ms[j] = 0.0;
     for (int i = 0; i < E->tcount; ++i) {
-        cudaEvent_t* ev = &E->tev[(size_t)i * 4];
-        KNN_CUDA(cudaEventSynchronize(ev[3]));
-        for (int j = 0; j < 3; ++j) {
+        cudaEvent_t* ev = &E->tev[(size_t)i * ne];
+        KNN_CUDA(cudaEventSynchronize(ev[ne - 1]));
+        for (int j = 0; j < ne - 1; ++j) {
             float t = 0.f;
             KNN_CUDA(cudaEventElapsedTime(&t, ev[j], ev[j + 1]));
             ms[j] += t;
@@ -661,6 +924,26 @@ int knns_timing_collect(double ms[3], int* count)
     if (count) *count = E->tcount;
     E->tcount = 0;
     return KNNS_OK;
+}
+
+int knns_timing_collect(double ms[3], int* count)
+{
+    clear_error();
+    if (!ms) return set_error(KNNS_ERR_INVALID, "null output");
+    double m5[5];
+    int rc = timing_collect(m5, count);
+    if (rc) return rc;
+    ms[0] = m5[0];
+    ms[1] = m5[1] + m5[2];
+    ms[2] = m5[3] + m5[4];
+    return KNNS_OK;
+}
+
+int knns_timing_collect5(double ms[5], int* count)
+{
+    clear_error();
+    if (!ms) return set_error(KNNS_ERR_INVALID, "null output");
+    return timing_collect(ms, count);
 }
 
 int knns_debug_tc_dot_tile(const float* corpus, int64_t N, const float* queries, int64_t Q, int D, float* dump)

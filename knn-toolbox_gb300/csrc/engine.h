@@ -39,11 +39,17 @@ struct Engine {
     std::mutex mu;
     cudaEvent_t last_done = nullptr;
     DevBuf cn, qn, part, hi, lo, bf, err, thr, loflags, cn_s, thr2, redo;
+    // threshold-scan path: BF16 queries, candidate segments and counts, seeded
+    // thresholds, sample norms, failed-query list
+    DevBuf qbf, cand, cnt, tq, cnv, fail;
     DevBuf in_corpus, in_queries, out_dist, out_idx;
-    // stage timing: 4 events per timed search (start, after prep, after fused, end)
+    // stage timing: kTimingEvents events per timed search (start, after prep,
+    // after threshold seeding, after the main fused kernel, after the main
+    // selection, end)
+    static constexpr int kTimingEvents = 6;
     std::vector<cudaEvent_t> tev;
     int tcount = 0;
-    int timing_slot(cudaEvent_t out[4]);
+    int timing_slot(cudaEvent_t out[kTimingEvents]);
     cudaStream_t host_stream();
     cudaEvent_t t0();
     cudaEvent_t t1();

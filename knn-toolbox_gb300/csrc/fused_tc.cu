@@ -159,6 +159,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
     extern __shared__ __align__(1024) unsigned char sm[];
     // redo pass: only flagged query tiles run
     if (a.tile_redo != nullptr && a.tile_redo[blockIdx.x] == 0u) return;
+    // compacted-query mode: rows past the listed queries accept nothing; empty tiles return
+    int64_t qvalid = a.Q;
+    if (a.qcount != nullptr) {
+        qvalid = min(a.Q, (int64_t)*a.qcount - a.qbase);
+        if ((int64_t)blockIdx.x * kTileQ >= qvalid) return;
+    }
     // only the variant that matches the data runs
     if (a.not_exact != nullptr) {
         if ((*a.not_exact != 0u) == kBF16) return;
@@ -361,7 +367,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
         float* srow = s.keystage + ((warp - 2) * 32 + lane) * kStagePitch;
 
         // A operand: this thread's query row into TMEM (BF16 pairs, or TF32 hi/lo)
-        const float* qrow = a.queries + (q < a.Q ? q : 0) * a.ldq;
+        const bool qok = q < qvalid;
+        const int64_t qsrc = !qok ? 0 : (a.qmap != nullptr ? (int64_t)a.qmap[a.qbase + q] : q);
+        const float* qrow = a.queries + qsrc * a.ldq;
         uint32_t any_lo = 0;
         if (kBF16) {
             for (int bx = 0; bx < nbox_bf; ++bx) {
@@ -369,8 +377,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
 #pragma unroll
                 for (int u = 0; u < 32; ++u) {
                     const int d0 = bx * kBoxElemsBf16 + 2 * u;
-                    const float x0 = (q < a.Q && d0 < a.D) ? __ldg(qrow + d0) : 0.f;
-                    const float x1 = (q < a.Q && d0 + 1 < a.D) ? __ldg(qrow + d0 + 1) : 0.f;
+                    const float x0 = (qok && d0 < a.D) ? __ldg(qrow + d0) : 0.f;
+                    const float x1 = (qok && d0 + 1 < a.D) ? __ldg(qrow + d0 + 1) : 0.f;
                     // lower K index in the low half of the 32-bit column
                     const uint32_t lo16 = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(x0));
                     const uint32_t hi16 = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(x1));
@@ -385,7 +393,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
 #pragma unroll
             for (int u = 0; u < 32; ++u) {
                 const int d = c * kChunkK + u;
-                const float x = (q < a.Q && d < a.D) ? __ldg(qrow + d) : 0.f;
+                const float x = (qok && d < a.D) ? __ldg(qrow + d) : 0.f;
                 hi[u] = tf32_rne_dev(x);
                 lo[u] = tf32_rne_dev(__fsub_rn(x, hi[u]));
                 any_lo |= (lo[u] != 0.f) ? 1u : 0u;
@@ -400,8 +408,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
         ptx::mbar_arrive(s.aready);
 
         // padding rows of the last query tile accept nothing
-        LaneState st{0, q < a.Q ? __int_as_float(0x7f800000) : -__int_as_float(0x7f800000)};
-        uint32_t* thr_g = q < a.Q ? a.thr_g : nullptr;
+        LaneState st{0, qok ? __int_as_float(0x7f800000) : -__int_as_float(0x7f800000)};
+        uint32_t* thr_g = qok ? a.thr_g : nullptr;
         uint32_t g_pending = thr_g ? __ldcg(thr_g + q) : 0xFFFFFFFFu;
         const bool dump = a.dump != nullptr && blockIdx.x == 0 && blockIdx.y == 0;
         for (int t = 0; t < ntiles; ++t) {
@@ -477,7 +485,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
         ptx::tmem_dealloc(tmem, kTmemCols);
     }
 
-    const int64_t nq = min((int64_t)kTileQ, a.Q - q0);
+    const int64_t nq = min((int64_t)kTileQ, qvalid - q0);
     uint64_t* out = a.part + ((size_t)blockIdx.y * a.Q + q0) * a.kp;
     for (int64_t i = tid; i < nq * a.kp; i += kTcThreads) out[i] = s.list[i];
 }

@@ -62,6 +62,11 @@ struct TcArgs {
     const uint32_t* corpus_any_lo;  // 1 when any corpus tile has a low part (null: assume so)
     const uint32_t* not_exact;      // 0 when corpus and queries are BF16-exact (null: TF32 path only)
     const uint32_t* tile_redo;      // optional: a CTA runs only when tile_redo[blockIdx.x] != 0
+    // optional compacted-query mode: row r of this launch (r < Q) is query qmap[qbase + r],
+    // present only when qbase + r < *qcount; part / thr_g rows are indexed by r
+    const int32_t* qmap;
+    const uint32_t* qcount;
+    int64_t qbase;
     float* dump;              // optional: raw dot tile of CTA (0,0), tile 0, [128][128]
     int* err;                 // device error word
     int D;
@@ -76,6 +81,35 @@ int tc_max_stages(int kp);
 // *a.not_exact selects it (BF16: inputs exact in BF16; TF32: otherwise).
 cudaError_t launch_tc(const TcArgs& a, int splits, bool bf16, cudaStream_t s);
 
+// Tensor-core BF16 threshold scan (csrc/scan_bf16.cu): 128 queries x 256-row
+// corpus tiles; every key strictly below the query's threshold is appended to
+// the query's segment cand[(split*2 + half)][q][0..cap) (in increasing corpus
+// index); cnt[(split*2 + half)][q] = keys found (may exceed cap: overflow).
+constexpr int kScanTileN = 256;
+constexpr int kScanMaxRing = 8;
+constexpr size_t kScanSmemLimit = 232448;
+struct ScanArgs {
+    CUtensorMap tm_c;          // corpus bf16 [N][dpb] (view), box {64, 256}, 128B swizzle
+    CUtensorMap tm_q;          // queries bf16 [Q][dpb], box {64, 128}, 128B swizzle
+    const float* cn;           // [>= roundup(N, 256)] corpus norms of the view, +inf padding
+    const float* thr;          // [Q] thresholds (null: +inf, every key collected)
+    const uint32_t* skip_if;   // optional: the kernel returns at once when *skip_if != 0
+    uint64_t* cand;            // [splits*2][Q][cap]
+    uint32_t* cnt;             // [splits*2][Q]
+    int* err;                  // device error word
+    int64_t Q;
+    int64_t N;
+    int64_t split_len;         // multiple of 256
+    int cap;
+    int dpb;                   // D rounded up to 64, <= 256
+    int bps;                   // K-boxes per ring slot (divides dpb/64)
+    int ring;                  // ring slots
+};
+size_t scan_smem_bytes(int dpb, int bps, int ring);
+// Ring geometry for dpb (want_bps = 0: automatic).  Returns 0 on success.
+int scan_plan(int dpb, int want_bps, int* bps, int* ring);
+cudaError_t launch_scan(const ScanArgs& a, int splits, cudaStream_t s);
+
 // Merge of the per-split shortlists, optional exact re-rank, final top-k.
 // Extra modes (all optional):
 //  * thr_out: instead of results, write the order-mapped key of the merged
@@ -83,6 +117,9 @@ cudaError_t launch_tc(const TcArgs& a, int splits, bool bf16, cudaStream_t s);
 //  * redo_out / need: when the merged shortlist holds fewer than `need` real
 //    entries, set redo_out[q / qtile] = 1 and write no result for q;
 //  * redo_in: process only queries whose tile has redo_in[q / qtile] != 0.
+//  * skip_if_zero: the kernel does nothing when *skip_if_zero == 0 (device-side path choice);
+//  * qmap / qcount / qbase: compacted rows, as for TcArgs: part row r is query
+//    qmap[qbase + r], present when qbase + r < *qcount; results go to that query's row.
 struct SelectExtra {
     uint32_t* thr_out = nullptr;
     int thr_rank = 0;
@@ -90,12 +127,55 @@ struct SelectExtra {
     int need = 0;
     const uint32_t* redo_in = nullptr;
     int qtile = 128;
+    const uint32_t* skip_if_zero = nullptr;
+    const int32_t* qmap = nullptr;
+    const uint32_t* qcount = nullptr;
+    int64_t qbase = 0;
 };
 size_t select_smem_bytes(int kp, int D, int rerank);
 cudaError_t launch_select(const uint64_t* part, int splits, int64_t Q, int kp, int k,
                           const float* corpus, int64_t ldc, const float* queries, int64_t ldq,
                           int D, int rerank, const float* qn, float* out_dist, int32_t* out_idx,
                           float* out_idx_f, cudaStream_t s, const SelectExtra& ex = SelectExtra());
+
+// Selection over the threshold scan's candidate segments (one warp per query).
+// The candidates of query q are the first min(cnt, cap) words of its nseg
+// segments; total = sum of cnt (the number of keys below the threshold).
+//  * thr_out (threshold mode): thr_out[q] = the next float above the key of
+//    rank thr_rank (1-based) when total >= thr_rank, no segment overflowed and
+//    total <= kCandMax; otherwise thr_out[q] = thr_fallback[q] (+inf if null);
+//  * result mode: the kp smallest (key, index) words form the shortlist, then
+//    re-rank / output as launch_select.  A query whose candidates cannot be
+//    trusted (overflow, total < need, total > kCandMax) is appended to
+//    fail_idx (count in *fail_cnt) and gets no result.
+constexpr int kCandMax = 2048;
+struct CandSelect {
+    const uint64_t* cand = nullptr;
+    const uint32_t* cnt = nullptr;
+    int nseg = 0;
+    int cap = 0;
+    int64_t Q = 0;
+    const uint32_t* skip_if = nullptr;  // the kernel does nothing when *skip_if != 0
+    float* thr_out = nullptr;
+    int thr_rank = 0;
+    const float* thr_fallback = nullptr;
+    int kp = 0;
+    int k = 0;
+    int need = 0;
+    int rerank = 1;
+    const float* corpus = nullptr;
+    int64_t ldc = 0;
+    const float* queries = nullptr;
+    int64_t ldq = 0;
+    int D = 0;
+    const float* qn = nullptr;
+    float* out_dist = nullptr;
+    int32_t* out_idx = nullptr;
+    float* out_idx_f = nullptr;
+    int32_t* fail_idx = nullptr;
+    uint32_t* fail_cnt = nullptr;
+};
+cudaError_t launch_select_cand(const CandSelect& c, cudaStream_t s);
 
 // out[i] = src[i * stride] for i < n, +inf for n <= i < n_pad (norms of a strided corpus sample).
 cudaError_t launch_gather_norms(const float* src, int64_t n, int64_t stride, float* out, int64_t n_pad,

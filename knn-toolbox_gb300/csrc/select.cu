@@ -1,4 +1,5 @@
-// select.cu -- merge of the per-split shortlists, exact re-rank, final top-k.
+// select.cu -- merge of the per-split shortlists (or of the threshold scan's
+// candidate segments), exact re-rank, final top-k.
 //
 // Replaces the reference's cross-chunk host merge (mergeResBitonic,
 // src/cuknnBitonic.cu:381-417; mergeResHeap, src/cuknnHeap.cu:26-62) and the
@@ -27,56 +28,19 @@ __host__ __device__ inline int pow2_at_least(int x)
     while (p < x) p <<= 1;
     return p;
 }
-}  // namespace
 
-__global__ void __launch_bounds__(kSelWarps * 32)
-select_kernel(const uint64_t* __restrict__ part, int splits, int64_t Q, int kp, int k,
-              const float* __restrict__ corpus, int64_t ldc, const float* __restrict__ queries,
-              int64_t ldq, int D, int rerank, const float* __restrict__ qn,
-              float* __restrict__ out_dist, int32_t* __restrict__ out_idx, float* __restrict__ out_idx_f,
-              const SelectExtra ex)
+// cur[0..kp) holds the query's shortlist sorted by (key, index) (sentinels at
+// the end); cur has room for pow2_at_least(kp) words.  Writes the k results of
+// query q (re-ranked by exact distance, or key + ||q||^2).
+__device__ __forceinline__ void finish_query(uint64_t* cur, int kp, int k, int64_t q, int rerank,
+                                             const float* __restrict__ corpus, int64_t ldc,
+                                             const float* __restrict__ queries, int64_t ldq, int D,
+                                             const float* __restrict__ qn, float* qv, float* out_dist,
+                                             int32_t* out_idx, float* out_idx_f)
 {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int P = pow2_at_least(kp);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // per warp: cur[P], nxt[P], other[kp], query vector[D]
-    size_t per_warp_words = (size_t)3 * P;
-    uint64_t* cur = reinterpret_cast<uint64_t*>(smem) + warp * per_warp_words;
-    uint64_t* nxt = cur + P;
-    uint64_t* oth = nxt + P;
-    float* qv = reinterpret_cast<float*>(reinterpret_cast<uint64_t*>(smem) + kSelWarps * per_warp_words) +
-                (size_t)warp * ((D + 3) & ~3);
-
-    const int64_t q = (int64_t)blockIdx.x * kSelWarps + warp;
-    if (q >= Q) return;
-    if (ex.redo_in != nullptr && ex.redo_in[q / ex.qtile] == 0u) return;
-
-    for (int j = lane; j < kp; j += 32) cur[j] = part[(size_t)q * kp + j];
-    __syncwarp();
-    for (int s = 1; s < splits; ++s) {
-        const uint64_t* src = part + ((size_t)s * Q + q) * kp;
-        for (int j = lane; j < kp; j += 32) oth[j] = src[j];
-        __syncwarp();
-        warp_merge_lists(cur, oth, nxt, kp);
-        uint64_t* t = cur; cur = nxt; nxt = t;
-        __syncwarp();
-    }
-
-    if (ex.thr_out != nullptr) {
-        // threshold extraction: key of the thr_rank-th entry
-        if (lane == 0) {
-            const uint64_t w = cur[ex.thr_rank - 1];
-            ex.thr_out[q] = w == kSentinel ? 0xFFFFFFFFu : (uint32_t)(w >> 32);
-        }
-        return;
-    }
-    if (ex.redo_out != nullptr && ex.need > 0 && cur[ex.need - 1] == kSentinel) {
-        // fewer entries than required passed a seeded threshold: this query's tile is redone
-        if (lane == 0) ex.redo_out[q / ex.qtile] = 1u;
-        return;
-    }
-
+    const int lane = threadIdx.x & 31;
     if (rerank) {
+        const int P = pow2_at_least(kp);
         const float* qrow = queries + q * ldq;
         for (int d = lane; d < D; d += 32) qv[d] = __ldg(qrow + d);
         __syncwarp();
@@ -113,6 +77,277 @@ select_kernel(const uint64_t* __restrict__ part, int splits, int64_t Q, int kp, 
         }
     }
 }
+}  // namespace
+
+__global__ void __launch_bounds__(kSelWarps * 32)
+select_kernel(const uint64_t* __restrict__ part, int splits, int64_t Q, int kp, int k,
+              const float* __restrict__ corpus, int64_t ldc, const float* __restrict__ queries,
+              int64_t ldq, int D, int rerank, const float* __restrict__ qn,
+              float* __restrict__ out_dist, int32_t* __restrict__ out_idx, float* __restrict__ out_idx_f,
+              const SelectExtra ex)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    if (ex.skip_if_zero != nullptr && *ex.skip_if_zero == 0u) return;
+    const int P = pow2_at_least(kp);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // per warp: cur[P], nxt[P], other[kp], query vector[D]
+    size_t per_warp_words = (size_t)3 * P;
+    uint64_t* cur = reinterpret_cast<uint64_t*>(smem) + warp * per_warp_words;
+    uint64_t* nxt = cur + P;
+    uint64_t* oth = nxt + P;
+    float* qv = reinterpret_cast<float*>(reinterpret_cast<uint64_t*>(smem) + kSelWarps * per_warp_words) +
+                (size_t)warp * ((D + 3) & ~3);
+
+    const int64_t q = (int64_t)blockIdx.x * kSelWarps + warp;  // row of `part`
+    if (q >= Q) return;
+    if (ex.redo_in != nullptr && ex.redo_in[q / ex.qtile] == 0u) return;
+    int64_t qout = q;  // query whose results this row holds
+    if (ex.qcount != nullptr) {
+        if (ex.qbase + q >= (int64_t)*ex.qcount) return;
+        qout = ex.qmap[ex.qbase + q];
+    }
+
+    for (int j = lane; j < kp; j += 32) cur[j] = part[(size_t)q * kp + j];
+    __syncwarp();
+    for (int s = 1; s < splits; ++s) {
+        const uint64_t* src = part + ((size_t)s * Q + q) * kp;
+        for (int j = lane; j < kp; j += 32) oth[j] = src[j];
+        __syncwarp();
+        warp_merge_lists(cur, oth, nxt, kp);
+        uint64_t* t = cur; cur = nxt; nxt = t;
+        __syncwarp();
+    }
+
+    if (ex.thr_out != nullptr) {
+        // threshold extraction: key of the thr_rank-th entry
+        if (lane == 0) {
+            const uint64_t w = cur[ex.thr_rank - 1];
+            ex.thr_out[q] = w == kSentinel ? 0xFFFFFFFFu : (uint32_t)(w >> 32);
+        }
+        return;
+    }
+    if (ex.redo_out != nullptr && ex.need > 0 && cur[ex.need - 1] == kSentinel) {
+        // fewer entries than required passed a seeded threshold: this query's tile is redone
+        if (lane == 0) ex.redo_out[q / ex.qtile] = 1u;
+        return;
+    }
+    finish_query(cur, kp, k, qout, rerank, corpus, ldc, queries, ldq, D, qn, qv, out_dist, out_idx, out_idx_f);
+}
+
+// ---------------------------------------------------------------- threshold-scan selection
+namespace {
+// rows of candidate vectors staged per re-rank batch: [rows][D + 1] floats
+__host__ __device__ inline int cand_stage_rows(int D) { return D <= 128 ? 32 : 16; }
+
+__host__ __device__ inline size_t cand_warp_bytes(int D)
+{
+    const size_t sel = (size_t)kCandMax * 8;
+    const size_t rr = (size_t)kMaxKpTC * 8 + (size_t)cand_stage_rows(D) * (D + 1) * 4;
+    const size_t w = sel > rr ? sel : rr;
+    return (w + 15) & ~(size_t)15;
+}
+
+// number of words w[0..n) (shared memory) not above x, summed over the warp
+__device__ __forceinline__ uint32_t count_not_above_u64(const uint64_t* w, int n, uint64_t x)
+{
+    const int lane = threadIdx.x & 31;
+    uint32_t c = 0;
+    for (int e = lane; e < n; e += 32) c += w[e] <= x ? 1u : 0u;
+    return __reduce_add_sync(0xffffffffu, c);
+}
+
+__device__ __forceinline__ uint32_t count_key_not_above(const uint64_t* w, int n, uint32_t x)
+{
+    const int lane = threadIdx.x & 31;
+    uint32_t c = 0;
+    for (int e = lane; e < n; e += 32) c += (uint32_t)(w[e] >> 32) <= x ? 1u : 0u;
+    return __reduce_add_sync(0xffffffffu, c);
+}
+
+// Exact distances of cur[0..kp) (direct difference, oracle order: eight partial
+// sums over d mod 8, fixed final tree), candidate rows staged in shared memory
+// with coalesced loads; lane j of a batch computes candidate b0 + j.
+__device__ __forceinline__ void rerank_staged(uint64_t* cur, int kp, const float* __restrict__ corpus, int64_t ldc,
+                                              const float* qv, int D, float* rows)
+{
+    const int lane = threadIdx.x & 31;
+    const int RB = cand_stage_rows(D);
+    const int pitch = D + 1;
+    for (int b0 = 0; b0 < kp; b0 += RB) {
+        const int nb = min(RB, kp - b0);
+        for (int r = 0; r < nb; ++r) {
+            const uint64_t w = cur[b0 + r];
+            if (w == kSentinel) continue;
+            const float* src = corpus + (int64_t)unpack_idx(w) * ldc;
+            for (int d = lane; d < D; d += 32) rows[r * pitch + d] = __ldg(src + d);
+        }
+        __syncwarp();
+        if (lane < nb) {
+            const uint64_t w = cur[b0 + lane];
+            if (w != kSentinel) {
+                const float* c = rows + lane * pitch;
+                float p[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                int d = 0;
+                for (; d + 8 <= D; d += 8) {
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const float t = __fsub_rn(qv[d + u], c[d + u]);
+                        p[u] = __fmaf_rn(t, t, p[u]);
+                    }
+                }
+                for (; d < D; ++d) {
+                    const float t = __fsub_rn(qv[d], c[d]);
+                    p[d & 7] = __fmaf_rn(t, t, p[d & 7]);
+                }
+                const float dist = __fadd_rn(__fadd_rn(__fadd_rn(p[0], p[1]), __fadd_rn(p[2], p[3])),
+                                             __fadd_rn(__fadd_rn(p[4], p[5]), __fadd_rn(p[6], p[7])));
+                cur[b0 + lane] = pack_key(dist, unpack_idx(w));
+            }
+        }
+        __syncwarp();
+    }
+}
+}  // namespace
+
+// One warp per query over the threshold scan's segments.
+__global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandSelect c)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    if (c.skip_if != nullptr && *c.skip_if != 0u) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t wb = cand_warp_bytes(c.D);
+    uint64_t* buf = reinterpret_cast<uint64_t*>(smem + (size_t)warp * wb);
+    float* qv = reinterpret_cast<float*>(smem + (size_t)kSelWarps * wb) + (size_t)warp * ((c.D + 3) & ~3);
+    const int64_t q = (int64_t)blockIdx.x * kSelWarps + warp;
+    if (q >= c.Q) return;
+
+    // per-lane segments s = lane, lane + 32, ...: stored and found counts
+    uint32_t stored = 0, found = 0;
+    bool over = false;
+    for (int s = lane; s < c.nseg; s += 32) {
+        const uint32_t n = __ldg(c.cnt + (size_t)s * c.Q + q);
+        found += n;
+        over |= n > (uint32_t)c.cap;
+        stored += min(n, (uint32_t)c.cap);
+    }
+    const uint32_t total = __reduce_add_sync(0xffffffffu, stored);
+    const uint32_t found_all = __reduce_add_sync(0xffffffffu, found);
+    const bool overflow = __any_sync(0xffffffffu, over);
+
+    const bool thr_mode = c.thr_out != nullptr;
+    const uint32_t need = thr_mode ? (uint32_t)c.thr_rank : (uint32_t)c.need;
+    if (overflow || found_all < need || total > (uint32_t)kCandMax) {
+        if (lane == 0) {
+            if (thr_mode) {
+                c.thr_out[q] = c.thr_fallback ? c.thr_fallback[q] : __int_as_float(0x7f800000);
+            } else {
+                const uint32_t pos = atomicAdd(c.fail_cnt, 1u);
+                c.fail_idx[pos] = (int32_t)q;
+            }
+        }
+        return;
+    }
+
+    // gather, segment by segment (eight at a time so that their loads overlap)
+    uint32_t base = 0;
+    for (int s0 = 0; s0 < c.nseg; s0 += 8) {
+        uint32_t n8[8];
+        uint64_t v8[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int s = s0 + u;
+            n8[u] = s < c.nseg ? min(__ldg(c.cnt + (size_t)s * c.Q + q), (uint32_t)c.cap) : 0u;
+            v8[u] = (uint32_t)lane < n8[u] ? __ldg(c.cand + ((size_t)s * c.Q + q) * c.cap + lane) : 0ull;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if ((uint32_t)lane < n8[u]) buf[base + lane] = v8[u];
+            if (n8[u] > 32u) {
+                // segments holding more than 32 candidates (every segment of the 1024-row sample pass)
+                const uint64_t* src = c.cand + ((size_t)(s0 + u) * c.Q + q) * c.cap;
+                uint64_t t8[7];
+#pragma unroll
+                for (int t = 0; t < 7; ++t) {
+                    const uint32_t i = 32u * (t + 1) + lane;
+                    t8[t] = i < n8[u] ? __ldg(src + i) : 0ull;
+                }
+#pragma unroll
+                for (int t = 0; t < 7; ++t) {
+                    const uint32_t i = 32u * (t + 1) + lane;
+                    if (i < n8[u]) buf[base + i] = t8[t];
+                }
+                for (uint32_t i = 256u + lane; i < n8[u]; i += 32) buf[base + i] = __ldg(src + i);
+            }
+            base += n8[u];
+        }
+    }
+    __syncwarp();
+    const int n = (int)total;
+
+    if (thr_mode) {
+        // smallest key x with at least thr_rank keys not above it (bitwise binary search)
+        uint32_t x = 0;
+        for (int bit = 31; bit >= 0; --bit) {
+            const uint32_t y = x | ((1u << bit) - 1u);  // x with the lower bits set
+            if (count_key_not_above(buf, n, y) < (uint32_t)c.thr_rank) x |= 1u << bit;
+        }
+        if (lane == 0) {
+            const float key = ord2f(x);
+            // strictly above the key of rank thr_rank: that key itself passes a "< T" test
+            c.thr_out[q] = key < __int_as_float(0x7f800000) ? nextafterf(key, __int_as_float(0x7f800000)) : key;
+        }
+        return;
+    }
+
+    // the kp-th smallest (key, index) word W (words are distinct: indices are)
+    const int kp = c.kp;
+    uint64_t W = kSentinel;
+    if (n > kp) {
+        uint64_t x = 0;
+        for (int bit = 63; bit >= 0; --bit) {
+            const uint64_t y = x | ((1ull << bit) - 1ull);
+            if (count_not_above_u64(buf, n, y) < (uint32_t)kp) x |= 1ull << bit;
+        }
+        W = x;
+    }
+    // compact the words not above W (at most kp of them) to the front, then sort them
+    const int P = pow2_at_least(kp);
+    uint64_t* cur = buf;  // in place: the compacted prefix never overtakes the read position
+    uint32_t m = 0;
+    for (int e0 = 0; e0 < n; e0 += 32) {
+        const int e = e0 + lane;
+        const uint64_t w = e < n ? buf[e] : kSentinel;
+        const bool keep = e < n && w <= W;
+        const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+        __syncwarp();
+        if (keep) cur[m + __popc(bal & ((1u << lane) - 1u))] = w;
+        m += __popc(bal);
+        __syncwarp();
+    }
+    for (int j = (int)m + lane; j < P; j += 32) cur[j] = kSentinel;
+    __syncwarp();
+    warp_sort_smem(cur, P);
+
+    if (c.rerank) {
+        const float* qrow = c.queries + q * c.ldq;
+        for (int d = lane; d < c.D; d += 32) qv[d] = __ldg(qrow + d);
+        __syncwarp();
+        rerank_staged(cur, kp, c.corpus, c.ldc, qv, c.D, reinterpret_cast<float*>(buf + kMaxKpTC));
+        warp_sort_smem(cur, P);
+        for (int j = lane; j < c.k; j += 32) {
+            const uint64_t w = cur[j];
+            const bool ok = w != kSentinel;
+            const float dv = ok ? unpack_key(w) : __int_as_float(0x7f800000);
+            const int32_t iv = ok ? (int32_t)unpack_idx(w) : -1;
+            if (c.out_dist) c.out_dist[q * c.k + j] = dv;
+            if (c.out_idx) c.out_idx[q * c.k + j] = iv;
+            if (c.out_idx_f) c.out_idx_f[q * c.k + j] = (float)iv;
+        }
+    } else {
+        finish_query(cur, kp, c.k, q, 0, c.corpus, c.ldc, c.queries, c.ldq, c.D, c.qn, qv, c.out_dist, c.out_idx,
+                     c.out_idx_f);
+    }
+}
 
 size_t select_smem_bytes(int kp, int D, int rerank)
 {
@@ -132,6 +367,22 @@ cudaError_t launch_select(const uint64_t* part, int splits, int64_t Q, int kp, i
     unsigned blocks = (unsigned)((Q + kSelWarps - 1) / kSelWarps);
     select_kernel<<<blocks, kSelWarps * 32, smem, s>>>(part, splits, Q, kp, k, corpus, ldc, queries, ldq, D,
                                                        rerank, qn, out_dist, out_idx, out_idx_f, ex);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_select_cand(const CandSelect& c, cudaStream_t s)
+{
+    if (c.Q <= 0) return cudaSuccess;
+    if (c.nseg < 1 || c.cap < 1 || (c.thr_out == nullptr && (c.kp < 1 || c.kp > kCandMax || c.k > c.kp ||
+                                                              c.fail_idx == nullptr || c.fail_cnt == nullptr)) ||
+        (c.thr_out != nullptr && (c.thr_rank < 1 || c.thr_rank > kCandMax)))
+        return cudaErrorInvalidValue;
+    if (c.thr_out == nullptr && c.kp > kMaxKpTC) return cudaErrorInvalidValue;
+    const size_t smem = (size_t)kSelWarps * cand_warp_bytes(c.D) + (size_t)kSelWarps * ((c.D + 3) & ~3) * 4;
+    cudaError_t e = cudaFuncSetAttribute(select_cand_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    unsigned blocks = (unsigned)((c.Q + kSelWarps - 1) / kSelWarps);
+    select_cand_kernel<<<blocks, kSelWarps * 32, smem, s>>>(c);
     return cudaGetLastError();
 }
 

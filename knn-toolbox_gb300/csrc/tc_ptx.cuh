@@ -127,6 +127,18 @@ __device__ __forceinline__ void mma_bf16_ts(uint32_t d_tmem, uint32_t a_tmem, ui
         : "memory");
 }
 
+// D[tmem] (+)= A[smem desc] * B[smem desc]^T, kind::f16 (BF16 operands, FP32 accumulate), cta_group::1
+__device__ __forceinline__ void mma_bf16_ss(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                            uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
 // Arrive on an mbarrier once all previously issued tcgen05 async ops of this thread complete.
 __device__ __forceinline__ void mma_commit(uint64_t* bar)
 {
@@ -220,6 +232,25 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N)
            | (2u << 10)                    // B format tf32
            | ((uint32_t)(N >> 3) << 17)    // N / 8
            | ((uint32_t)(M >> 4) << 24);   // M / 16
+}
+
+// ---------------------------------------------------------------- packed / 3-input FP32 (sm_100+)
+// (o0, o1) = (a0 * m + c0, a1 * m + c1), each one IEEE fma with round-to-nearest
+__device__ __forceinline__ void fma2(float& o0, float& o1, float a0, float a1, float m, float c0, float c1)
+{
+    uint64_t a, mm, c, r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(a) : "f"(a0), "f"(a1));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(mm) : "f"(m), "f"(m));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(c) : "f"(c0), "f"(c1));
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(mm), "l"(c));
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(o0), "=f"(o1) : "l"(r));
+}
+
+__device__ __forceinline__ float fmin3(float a, float b, float c)
+{
+    float m;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(m) : "f"(a), "f"(b), "f"(c));
+    return m;
 }
 
 }  // namespace ptx

@@ -29,12 +29,13 @@ LIB_PATH = os.path.join(PKG, "_build", "libknngb300.so")
 
 ALGO_AUTO, ALGO_TC, ALGO_SIMT = 0, 1, 2
 PREC_EXACT, PREC_BF16 = 0, 1
+SCAN_AUTO, SCAN_ON, SCAN_OFF = 0, 1, 2
 OK, ERR_INVALID, ERR_CUDA, ERR_UNSUPPORTED, ERR_DEVICE_TIMEOUT, ERR_NOMEM = range(6)
 
 # Every symbol include/knn_gb300.h and include/cuknns.h declare.
 EXPORTED = ["knns_default_options", "knns_search_device", "knns_search_host", "knns_check_device",
             "knns_last_error", "knns_last_stats", "knns_version", "knns_debug_tc_dot_tile",
-            "knns_timing_collect", "knns_search_device_noalloc",
+            "knns_timing_collect", "knns_timing_collect5", "knns_search_device_noalloc",
             "gpuknnsBitonic", "gpuknnsHeap", "knnsplan", "knnsexecute"]
 
 
@@ -47,13 +48,15 @@ class KnnsError(RuntimeError):
 class Options(ctypes.Structure):
     _fields_ = [("algo", ctypes.c_int), ("splits", ctypes.c_int), ("rerank", ctypes.c_int),
                 ("kp", ctypes.c_int), ("timing", ctypes.c_int), ("pilot", ctypes.c_int),
-                ("precision", ctypes.c_int), ("shortlist", ctypes.c_int)]
+                ("precision", ctypes.c_int), ("shortlist", ctypes.c_int), ("scan", ctypes.c_int),
+                ("scan_boxes", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
 
 
 class Stats(ctypes.Structure):
     _fields_ = [("algo", ctypes.c_int), ("splits", ctypes.c_int), ("kp", ctypes.c_int),
                 ("stages", ctypes.c_int), ("launches", ctypes.c_int), ("pilot", ctypes.c_int),
-                ("workspace_bytes", ctypes.c_int64)]
+                ("workspace_bytes", ctypes.c_int64), ("scan", ctypes.c_int), ("scan_splits", ctypes.c_int),
+                ("scan_cap", ctypes.c_int), ("scan_ring", ctypes.c_int)]
 
 
 KNNPTR2FUNCTION = ctypes.CFUNCTYPE(ctypes.c_double, *([ctypes.POINTER(ctypes.c_float)] * 4),
@@ -92,6 +95,7 @@ def lib():
     L.knns_last_stats.argtypes = [ctypes.POINTER(Stats)]
     L.knns_debug_tc_dot_tile.argtypes = [vp, i64, vp, i64, ci, vp]
     L.knns_timing_collect.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
+    L.knns_timing_collect5.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
     L.knns_search_device_noalloc.argtypes = [vp, i64, i64, vp, i64, i64, ci, ci, vp, vp, vp]
     L.gpuknnsBitonic.argtypes = [fp, fp, fp, fp, ci, ci, ci, ci, ci]
     L.gpuknnsBitonic.restype = ctypes.c_double
@@ -115,13 +119,14 @@ def _check(rc):
 
 
 def options(algo=ALGO_AUTO, splits=0, rerank=True, kp=0, timing=False, pilot=True, precision=PREC_EXACT,
-            shortlist=0) -> Options:
+            shortlist=0, scan=SCAN_AUTO, scan_boxes=0) -> Options:
     o = Options()
     lib().knns_default_options(ctypes.byref(o))
     o.algo, o.splits, o.rerank, o.kp = int(algo), int(splits), int(bool(rerank)), int(kp)
     o.timing = int(bool(timing))
     o.pilot = int(bool(pilot))
     o.precision, o.shortlist = int(precision), int(shortlist)
+    o.scan, o.scan_boxes = int(scan), int(scan_boxes)
     return o
 
 
@@ -133,11 +138,20 @@ def timing_collect():
     return ms[0], ms[1], ms[2], n.value
 
 
+def timing_collect5():
+    """Per-stage milliseconds: (prep, seeding, fused, select, fixup, count) summed since the last call."""
+    ms = (ctypes.c_double * 5)()
+    n = ctypes.c_int(0)
+    _check(lib().knns_timing_collect5(ms, ctypes.byref(n)))
+    return ms[0], ms[1], ms[2], ms[3], ms[4], n.value
+
+
 def last_stats() -> dict:
     s = Stats()
     _check(lib().knns_last_stats(ctypes.byref(s)))
     return {"algo": s.algo, "splits": s.splits, "kp": s.kp, "stages": s.stages, "launches": s.launches,
-            "pilot": s.pilot, "workspace_bytes": s.workspace_bytes}
+            "pilot": s.pilot, "workspace_bytes": s.workspace_bytes, "scan": s.scan, "scan_splits": s.scan_splits,
+            "scan_cap": s.scan_cap, "scan_ring": s.scan_ring}
 
 
 # --------------------------------------------------------------------------
@@ -145,7 +159,8 @@ def last_stats() -> dict:
 # --------------------------------------------------------------------------
 
 def search(corpus, queries, k, *, dist=None, idx=None, algo=ALGO_AUTO, splits=0, rerank=True, kp=0,
-           stream=None, check=True, timing=False, pilot=True, precision=PREC_EXACT, shortlist=0):
+           stream=None, check=True, timing=False, pilot=True, precision=PREC_EXACT, shortlist=0, scan=SCAN_AUTO,
+           scan_boxes=0):
     """kNN on CUDA tensors (float32, rows contiguous).  Returns (dist[Q,k] f32, idx[Q,k] i32)."""
     import torch
     assert corpus.is_cuda and queries.is_cuda, "search() takes device tensors"
@@ -159,7 +174,7 @@ def search(corpus, queries, k, *, dist=None, idx=None, algo=ALGO_AUTO, splits=0,
     if idx is None:
         idx = torch.empty((Q, k), dtype=torch.int32, device=corpus.device)
     s = torch.cuda.current_stream(corpus.device) if stream is None else stream
-    o = options(algo, splits, rerank, kp, timing, pilot, precision, shortlist)
+    o = options(algo, splits, rerank, kp, timing, pilot, precision, shortlist, scan, scan_boxes)
     rc = lib().knns_search_device(corpus.data_ptr(), N, corpus.stride(0), queries.data_ptr(), Q,
                                   queries.stride(0), D, k, dist.data_ptr(), idx.data_ptr(), ctypes.byref(o),
                                   ctypes.c_void_p(s.cuda_stream))

@@ -1,0 +1,133 @@
+"""Threshold-scan path (BF16 tensor cores, seeded per-query thresholds, candidate
+segments, fix-up of failed queries) against the oracle and against the
+shortlist path.  Bars as in test_gpu_parity.py: bit-exact where the arithmetic
+is exact (integer data), otherwise indices identical except where the FP64
+distances of competing candidates differ by < 1e-6 relative, distances within
+1e-5 relative of FP64; the BF16 precision form is held to recall@k >= 0.99 with
+exact distances for the returned indices.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GAP = 1e-6
+DIST_REL = 1e-5
+
+
+def run(engine, X, Qs, k, **kw):
+    import torch
+    c = torch.from_numpy(np.ascontiguousarray(X)).cuda()
+    q = torch.from_numpy(np.ascontiguousarray(Qs)).cuda()
+    d, i = engine.search(c, q, k, **kw)
+    return d.cpu().numpy(), i.cpu().numpy(), engine.last_stats()
+
+
+def ints(n, q, d, seed, hi=256):
+    rng = np.random.default_rng(seed)
+    return (rng.integers(0, hi, (n, d)).astype(np.float32), rng.integers(0, hi, (q, d)).astype(np.float32))
+
+
+def test_auto_scan_matches_shortlist_path_and_oracle(engine, oracle):
+    import cuknns.synth as S
+    X, Qs = S.int_descriptor(150_000, 128, seed=8, nq=300)
+    k = 100
+    d, i, st = run(engine, X, Qs, k)
+    assert st["scan"] == 1
+    d0, i0, st0 = run(engine, X, Qs, k, scan=engine.SCAN_OFF)
+    assert st0["scan"] == 0
+    np.testing.assert_array_equal(i, i0)
+    np.testing.assert_array_equal(d, d0)
+    sub = np.arange(0, 300, 7)
+    od, oi = oracle.knn_gemm(X, Qs[sub], k, kp=st["kp"], rerank=True)
+    np.testing.assert_array_equal(i[sub], oi)
+    np.testing.assert_array_equal(d[sub], od)
+
+
+@pytest.mark.parametrize("N,Q,D,k", [(20000, 300, 128, 16), (20011, 130, 64, 10), (16384, 1, 128, 100),
+                                     (30000, 257, 96, 32), (25000, 64, 40, 1)])
+def test_forced_scan_integer_data_bit_exact(engine, oracle, N, Q, D, k):
+    X, Qs = ints(N, Q, D, N + D)
+    d, i, st = run(engine, X, Qs, k, scan=engine.SCAN_ON)
+    assert st["scan"] == 1
+    od, oi = oracle.knn_gemm(X, Qs, k, kp=st["kp"], rerank=True)
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_array_equal(d, od)
+
+
+@pytest.mark.parametrize("boxes", [1, 2])
+def test_ring_geometry_does_not_change_results(engine, oracle, boxes):
+    X, Qs = ints(40000, 200, 128, 31)
+    k = 20
+    d, i, st = run(engine, X, Qs, k, scan=engine.SCAN_ON, scan_boxes=boxes)
+    assert st["scan_ring"] % 100 == boxes
+    od, oi = oracle.knn_gemm(X, Qs, k, kp=st["kp"], rerank=True)
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_array_equal(d, od)
+
+
+@pytest.mark.parametrize("Q", [40, 600])
+def test_duplicate_rows_overflow_and_fixup(engine, oracle, Q):
+    # Each query equals 2,000 corpus rows: every segment overflows, every query
+    # fails the scan and is searched again by the fix-up (600 > 512 queries
+    # also exercises the second fix-up launch).  Ties go to the lower index.
+    rng = np.random.default_rng(5)
+    base = rng.integers(0, 64, (10, 64)).astype(np.float32)
+    X = np.repeat(base, 2000, axis=0)
+    rng.shuffle(X)
+    Qs = base[rng.integers(0, 10, Q)]
+    k = 16
+    d, i, st = run(engine, X, Qs, k, scan=engine.SCAN_ON)
+    assert st["scan"] == 1
+    od, oi = oracle.knn_gemm(X, Qs, k, kp=st["kp"], rerank=True)
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_array_equal(d, od)
+
+
+def test_unrepresentative_sample_fixup(engine, oracle):
+    # Only every 16th row (the seeding sample) lies near the queries, so the
+    # seeded threshold admits fewer than kp rows and the fix-up must take over.
+    rng = np.random.default_rng(78)
+    N, D, Q, k = 16 * 8192, 64, 150, 10
+    Qs = rng.integers(0, 32, (Q, D)).astype(np.float32)
+    X = rng.integers(200, 256, (N, D)).astype(np.float32)
+    near = np.arange(0, N, 16)
+    X[near] = Qs[rng.integers(0, Q, near.size)] + rng.integers(0, 2, (near.size, D)).astype(np.float32)
+    d, i, st = run(engine, X, Qs, k)
+    assert st["scan"] == 1
+    od, oi = oracle.knn_gemm(X, Qs, k, kp=st["kp"], rerank=True)
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_array_equal(d, od)
+
+
+def test_exact_form_on_fp32_data_stays_on_tf32(engine, oracle):
+    # The scan is launched but stands down on the device: data not BF16-exact.
+    import cuknns.synth as S
+    X, Qs = S.uniform(140_000, 128, seed=12, nq=200)
+    k = 16
+    d, i, st = run(engine, X, Qs, k)
+    assert st["scan"] == 1
+    od, oi = oracle.knn_gemm(X, Qs, k, kp=st["kp"], rerank=True)
+    oracle.check_parity(X, Qs, k, d, i, ref_idx=oi, gap_rel=GAP, dist_rel=DIST_REL)
+    d0, i0, _ = run(engine, X, Qs, k, scan=engine.SCAN_OFF)
+    np.testing.assert_array_equal(i, i0)
+    np.testing.assert_array_equal(d, d0)
+
+
+@pytest.mark.parametrize("D,c", [(96, 4), (200, 2), (256, 4)])
+def test_bf16_precision_form_on_scan(engine, oracle, D, c):
+    import cuknns.synth as S
+    X, Qs = S.gauss_mixture(150_000, D, seed=6, nq=150, centres=512)
+    k = 10
+    d, i, st = run(engine, X, Qs, k, precision=engine.PREC_BF16, shortlist=c)
+    assert st["scan"] == 1 and st["kp"] >= c * k
+    ex = oracle.knn_f64(X, Qs, k)
+    rec = oracle.recall_at_k(i, ex[1])
+    assert rec >= 0.99, rec
+    got64 = oracle.pair_dist_f64(X, Qs, i)
+    assert (np.abs(d - got64) <= DIST_REL * got64 + 1e-6).all()
+    assert (np.diff(d, axis=1) >= 0).all()
+    # the shortlist path ranks by the same BF16 keys (its MMA shape differs, so
+    # FP32 accumulation may differ in the last bit on near-ties)
+    d0, i0, _ = run(engine, X, Qs, k, precision=engine.PREC_BF16, shortlist=c, scan=engine.SCAN_OFF)
+    assert (i == i0).mean() >= 0.999
