@@ -39,6 +39,9 @@ WORKLOADS = {
     "mix4m": dict(desc="Gaussian mixture corpus 4,000,000 x 96 (1,024 centres N(0,1), sigma 0.15, rows "
                        "L2-normalised), 10,000 queries, k=10, seed 2",
                   gen="gauss_mixture", N=4_000_000, D=96, Q=10_000, k=10, seed=2),
+    # profiling cut of int1m: full corpus (same candidate density per corpus row), a quarter of the queries
+    "int1m_q2500": dict(desc="int-descriptor corpus 1,000,000 x 128, 2,500 queries, k=100, seed 1",
+                        gen="int_descriptor", N=1_000_000, D=128, Q=2_500, k=100, seed=1),
     # profiling-sized cut of int1m (corpus still larger than L2) for ncu captures
     "int256k": dict(desc="int-descriptor corpus 262,144 x 128, 10,000 queries, k=100, seed 1",
                     gen="int_descriptor", N=262_144, D=128, Q=10_000, k=100, seed=1),

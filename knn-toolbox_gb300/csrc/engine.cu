@@ -271,25 +271,34 @@ int resolve_config(const Engine& E, int64_t N, int64_t Q, int D, int k, const kn
 
 // ---------------------------------------------------------------- threshold-scan plan
 // Seeding: the main scan needs, per query, a threshold T with at least kp keys
-// below it (then every top-kp candidate is collected) and few more.  Two
-// sample passes give it: P0 keys every key of a 1024-row sample and picks its
-// j0-th smallest as T0; P1 collects the keys below T0 over every 16th row and
-// picks the j1-th smallest as T1, the main pass's threshold.  With m = kp/16
-// (the expected sample rank of the final kp-th key) j1 = 2m + 4 sqrt(m) + 1
-// leaves a chance of roughly 1e-5 that fewer than kp keys fall below T1; such
-// queries (and any whose segments overflow) are found by the selection and
-// searched again without a threshold, so results never depend on the seeds.
+// below it (then every top-kp candidate is collected) and few more.  Nested
+// corpus samples give it, coarse to fine: level l keeps every stride_l-th row
+// (stride 16 for the finest level, 16x more per coarser level, the coarsest
+// small enough to keep every key).  Each level collects the keys below the
+// previous level's threshold and picks the key of rank j_l as its own.  With
+// m = j_next / 16 (the expected rank, in this level's sample, of the key of
+// rank j_next in the next one; m = kp / 16 for the finest level)
+// j = 2m + 4 sqrt(m) + 1 leaves a chance of roughly 1e-5 that fewer than j_next
+// keys fall below the threshold at the next level.  Queries for which that
+// happens in the main pass (and any whose segments overflow) are found by the
+// selection and searched again without a threshold, so results never depend
+// on the seeds.
+constexpr int kMaxSeedLevels = 6;
+
+struct ScanLevel {
+    int64_t n = 0, stride = 1, len = 0, n_pad = 0;
+    int j = 0, S = 1, cap = 0;
+};
+
 struct ScanPlan {
     int bps = 0, ring = 0;
-    int64_t n0 = 0, s0 = 1, len0 = 0;
-    int j0 = 0, S0 = 1, cap0 = 0;
-    int64_t n1 = 0, s1 = 16, len1 = 0;
-    int j1 = 0, S1 = 1, cap1 = 0;
+    int levels = 0;
+    ScanLevel lv[kMaxSeedLevels];
     int64_t len = 0;
     int S = 1, cap = 0;
     int64_t fixA_rows = 0, fixA_len = 0, fixB_rows = 0, fixB_len = 0;
     int fixA_S = 1, fixB_S = 1;
-    size_t cand_words = 0, cnt_words = 0, part_words = 0;
+    size_t cand_words = 0, cnt_words = 0, part_words = 0, norm_words = 0;
 };
 
 static int seg_cap(double per_seg, double sigmas)
@@ -297,42 +306,72 @@ static int seg_cap(double per_seg, double sigmas)
     return round16((int)std::ceil(sigmas * per_seg + 8.0 * std::sqrt(per_seg) + 16.0));
 }
 
+static int seed_rank(double m) { return (int)std::ceil(2.0 * m + 4.0 * std::sqrt(m)) + 1; }
+
 static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, const knns_options& o, ScanPlan* P)
 {
     if (scan_plan(dpb, o.scan_boxes, &P->bps, &P->ring) != 0)
         return set_error(KNNS_ERR_UNSUPPORTED, "threshold scan: no ring geometry for %d BF16 columns with %d boxes per slot",
                          dpb, o.scan_boxes);
     const int64_t qt = cdiv(Q, kTileQ);
-    const double m = (double)kp / 16.0;
-    P->s1 = 16;
-    P->n1 = cdiv(N, P->s1);
-    P->j1 = (int)std::ceil(2.0 * m + 4.0 * std::sqrt(m)) + 1;
-    P->n0 = std::min<int64_t>(N, 1024);
-    P->s0 = std::max<int64_t>(1, N / P->n0);
-    const double m0 = (double)P->j1 * (double)P->n0 / (double)P->n1;
-    P->j0 = std::min<int>((int)P->n0, (int)std::ceil(2.0 * m0 + 4.0 * std::sqrt(m0)) + 1);
-    if (P->j1 > kCandMax / 2 || P->n1 < 4 * P->j1)
+    const int tn = scan_tile_rows(dpb);
+    // levels, finest first: strides 16, 256, ... until the sample fits the selector whole
+    int64_t st[kMaxSeedLevels];
+    int L = 0;
+    for (int64_t stride = 16;; stride *= 16) {
+        if (L == kMaxSeedLevels) return set_error(KNNS_ERR_UNSUPPORTED, "threshold scan: corpus too large to seed");
+        st[L++] = stride;
+        if (cdiv(N, stride) <= kCandMax / 2) break;
+    }
+    P->levels = L;
+    // level index 0 = coarsest
+    for (int l = 0; l < L; ++l) {
+        ScanLevel& v = P->lv[l];
+        v.stride = st[L - 1 - l];
+        v.n = cdiv(N, v.stride);
+        v.n_pad = cdiv(v.n, kScanTileN) * kScanTileN + kScanTileN;  // >= one tile past the view
+    }
+    // ranks, finest to coarsest
+    double m = (double)kp / 16.0;
+    for (int l = L - 1; l >= 0; --l) {
+        ScanLevel& v = P->lv[l];
+        v.j = std::min<int>((int)v.n, seed_rank(m));
+        if (l > 0) m = (double)v.j * (double)P->lv[l - 1].n / (double)v.n;
+    }
+    if (P->lv[L - 1].j > kCandMax / 2 || P->lv[L - 1].n < 4 * P->lv[L - 1].j)
         return set_error(KNNS_ERR_UNSUPPORTED, "threshold scan: shortlist of %d too long for N=%lld", kp, (long long)N);
-    // P0: two splits of at most two tiles; each half-warp segment sees <= 256 columns, all kept
-    const int64_t tiles0 = cdiv(P->n0, kScanTileN);
-    P->S0 = (int)std::min<int64_t>(2, tiles0);
-    P->len0 = cdiv(tiles0, P->S0) * kScanTileN;
-    P->S0 = (int)cdiv(P->n0, P->len0);
-    P->cap0 = (int)(P->len0 / 2);
-    // P1
-    const int64_t tiles1 = cdiv(P->n1, kScanTileN);
-    P->S1 = auto_splits(qt, tiles1, E.sms, 64);
-    P->len1 = cdiv(tiles1, P->S1) * kScanTileN;
-    P->S1 = (int)cdiv(P->n1, P->len1);
-    const double h1 = (double)P->n1 * P->j0 / (double)P->n0;
-    P->cap1 = std::min<int>((int)(P->len1 / 2), seg_cap(h1 / (2.0 * P->S1), 3.0));
+    P->cand_words = 0;
+    P->cnt_words = 0;
+    P->norm_words = 0;
+    for (int l = 0; l < L; ++l) {
+        ScanLevel& v = P->lv[l];
+        const int64_t tiles = cdiv(v.n, tn);
+        if (l == 0) {
+            // every key kept: at most two splits, each segment holds all its columns
+            v.S = (int)std::min<int64_t>(2, tiles);
+            v.len = cdiv(tiles, v.S) * tn;
+            v.S = (int)cdiv(v.n, v.len);
+            v.cap = (int)(v.len / kScanParts);
+        } else {
+            v.S = auto_splits(qt, tiles, E.sms, 64);
+            v.len = cdiv(tiles, v.S) * tn;
+            v.S = (int)cdiv(v.n, v.len);
+            const double hits = (double)P->lv[l - 1].j * (double)v.n / (double)P->lv[l - 1].n;
+            v.cap = std::min<int>((int)(v.len / kScanParts), seg_cap(hits / ((double)kScanParts * v.S), 3.0));
+        }
+        P->cand_words = std::max(P->cand_words, (size_t)kScanParts * v.S * Q * v.cap);
+        P->cnt_words = std::max(P->cnt_words, (size_t)kScanParts * v.S * Q);
+        P->norm_words += (size_t)v.n_pad;
+    }
     // main pass
-    const int64_t tiles = cdiv(N, kScanTileN);
+    const int64_t tiles = cdiv(N, tn);
     P->S = o.splits > 0 ? std::min<int>(o.splits, (int)tiles) : auto_splits(qt, tiles, E.sms, 64);
-    P->len = cdiv(tiles, P->S) * kScanTileN;
+    P->len = cdiv(tiles, P->S) * tn;
     P->S = (int)cdiv(N, P->len);
-    const double hm = (double)P->j1 * P->s1;
-    P->cap = std::min<int>((int)(P->len / 2), seg_cap(hm / (2.0 * P->S), 2.0));
+    const double hm = (double)P->lv[L - 1].j * (double)P->lv[L - 1].stride;
+    P->cap = std::min<int>((int)(P->len / kScanParts), seg_cap(hm / ((double)kScanParts * P->S), 2.0));
+    P->cand_words = std::max(P->cand_words, (size_t)kScanParts * P->S * Q * P->cap);
+    P->cnt_words = std::max(P->cnt_words, (size_t)kScanParts * P->S * Q);
     // fix-up of failed queries: up to 512 on a full wave, the rest (rare) on 8 splits
     const int64_t tiles128 = cdiv(N, kTileN);
     P->fixA_rows = std::min<int64_t>(Q, 4 * kTileQ);
@@ -343,9 +382,6 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
     P->fixB_S = (int)std::min<int64_t>(tiles128, 8);
     P->fixB_len = cdiv(tiles128, P->fixB_S) * kTileN;
     P->fixB_S = (int)cdiv(N, P->fixB_len);
-    P->cand_words = std::max({(size_t)2 * P->S0 * Q * P->cap0, (size_t)2 * P->S1 * Q * P->cap1,
-                              (size_t)2 * P->S * Q * P->cap});
-    P->cnt_words = (size_t)2 * std::max({P->S0, P->S1, P->S}) * Q;
     P->part_words = std::max((size_t)P->fixA_S * P->fixA_rows * kp, (size_t)P->fixB_S * P->fixB_rows * kp);
     return KNNS_OK;
 }
@@ -386,7 +422,8 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     }
     const bool run_old = !(scan && bf16_only);  // the shortlist path is needed (possibly gated)
 
-    const int64_t n_pad = cdiv(N, kScanTileN) * kScanTileN;
+    // norms padded with +inf at least one tile (of any kernel) past the corpus
+    const int64_t n_pad = cdiv(N, kScanTileN) * kScanTileN + kScanTileN;
     size_t ws = 0;
     rc = E.cn.ensure(n_pad * sizeof(float));
     if (rc) return rc;
@@ -445,14 +482,12 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         if (rc) return rc;
         ws += E.hi.cap + E.lo.cap + E.bf.cap + E.loflags.cap;
     }
-    const int64_t n1_pad = scan ? cdiv(sp.n1, kScanTileN) * kScanTileN : 0;
-    const int64_t n0_pad = scan ? cdiv(sp.n0, kScanTileN) * kScanTileN : 0;
     if (scan) {
         rc = E.qbf.ensure((size_t)Q * c.dpb * 2);
         if (!rc) rc = E.cand.ensure(sp.cand_words * sizeof(uint64_t));
         if (!rc) rc = E.cnt.ensure(sp.cnt_words * sizeof(uint32_t));
         if (!rc) rc = E.tq.ensure((size_t)2 * Q * sizeof(float));
-        if (!rc) rc = E.cnv.ensure((size_t)(n0_pad + n1_pad) * sizeof(float));
+        if (!rc) rc = E.cnv.ensure(sp.norm_words * sizeof(float));
         if (!rc) rc = E.fail.ensure((size_t)(Q + 1) * sizeof(uint32_t));
         if (!rc) rc = E.part.ensure(sp.part_words * sizeof(uint64_t));
         if (!rc) rc = E.thr2.ensure(Q * sizeof(uint32_t));
@@ -471,12 +506,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     if ((rc = mark(0))) return rc;
     int launches = 0;
     float* cn = (float*)E.cn.p;
-    KNN_CUDA(launch_norms(corpus, N, ldc, D, cn, n_pad, s));
-    ++launches;
-    if (!c.rerank) {
-        KNN_CUDA(launch_norms(queries, Q, ldq, D, (float*)E.qn.p, Q, s));
-        ++launches;
-    }
+    float* qn = c.rerank ? nullptr : (float*)E.qn.p;
     uint64_t* part = (uint64_t*)E.part.p;
     uint32_t* thr_g = (uint32_t*)E.thr.p;
     uint32_t* flags = nullptr;
@@ -487,20 +517,25 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         any_lo = flags + cdiv(N, 128);
         not_exact = any_lo + 1;
         KNN_CUDA(cudaMemsetAsync(any_lo, 0, 2 * sizeof(uint32_t), s));
-        if (bf16_only) {
-            // BF16 keys whatever the data: the "not exact" word stays 0 (the
-            // conversion reports into the unused any_lo word instead)
-            KNN_CUDA(launch_bf16(corpus, N, ldc, D, c.dpb, E.bf.p, any_lo, s));
-            KNN_CUDA(launch_bf16(queries, Q, ldq, D, c.dpb, scan ? E.qbf.p : nullptr, any_lo, s));
-            launches += 2;
-        } else {
-            // BF16 copy of the corpus and the exactness test of corpus and queries;
-            // the TF32 split then runs only for data that is not BF16-exact
-            KNN_CUDA(launch_bf16(corpus, N, ldc, D, c.dpb, E.bf.p, not_exact, s));
-            KNN_CUDA(launch_bf16(queries, Q, ldq, D, c.dpb, scan ? E.qbf.p : nullptr, not_exact, s));
+        // one pass per input: BF16 copy, exactness test, norms.  In the BF16 form the
+        // keys are BF16 whatever the data: the "not exact" word stays 0 (the test
+        // reports into the unused any_lo word instead).
+        uint32_t* exact_word = bf16_only ? any_lo : not_exact;
+        KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, c.dpb, E.bf.p, cn, n_pad, exact_word, s));
+        KNN_CUDA(launch_prep_rows(queries, Q, ldq, D, c.dpb, scan ? E.qbf.p : nullptr, qn, Q, exact_word, s));
+        launches += 2;
+        if (!bf16_only) {
+            // the TF32 split runs only for data that is not BF16-exact
             KNN_CUDA(launch_split(corpus, N, ldc, D, c.dp, (float*)E.hi.p, (float*)E.lo.p, flags, any_lo, not_exact,
                                   s));
-            launches += 3;
+            ++launches;
+        }
+    } else {
+        KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, 0, nullptr, cn, n_pad, nullptr, s));
+        ++launches;
+        if (qn) {
+            KNN_CUDA(launch_prep_rows(queries, Q, ldq, D, 0, nullptr, qn, Q, nullptr, s));
+            ++launches;
         }
     }
     if ((rc = mark(1))) return rc;
@@ -612,27 +647,24 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         // ---------------------------------------------------------------- threshold scan
         // (runs when *scan_gate == 0: always in the BF16 form, for BF16-exact data in the exact form)
         const uint32_t* scan_gate = bf16_only ? nullptr : not_exact;
-        float* T0 = (float*)E.tq.p;
-        float* T1 = T0 + Q;
-        float* cn0 = (float*)E.cnv.p;
-        float* cn1 = cn0 + n0_pad;
+        float* Tbuf[2] = {(float*)E.tq.p, (float*)E.tq.p + Q};
         uint32_t* fail_cnt = (uint32_t*)E.fail.p;
         int32_t* fail_idx = (int32_t*)E.fail.p + 1;
         ScanArgs a;
         memset(&a, 0, sizeof(a));
-        rc = encode_rows_bf16(&a.tm_q, E.qbf.p, Q, c.dpb, c.dpb, kTileQ);
-        if (rc) return rc;
+        a.qbf = E.qbf.p;
         a.skip_if = scan_gate;
         a.cand = (uint64_t*)E.cand.p;
         a.cnt = (uint32_t*)E.cnt.p;
         a.err = (int*)E.err.p;
         a.Q = Q;
         a.dpb = c.dpb;
+        a.ksteps = (D + 15) / 16;
         a.bps = sp.bps;
         a.ring = sp.ring;
         auto scan_pass = [&](int64_t nview, int64_t stride, const float* cn_view, const float* thr, int splits,
                              int64_t split_len, int cap) -> int {
-            int r = encode_rows_bf16(&a.tm_c, E.bf.p, nview, c.dpb, stride * c.dpb, kScanTileN);
+            int r = encode_rows_bf16(&a.tm_c, E.bf.p, nview, c.dpb, stride * c.dpb, scan_box_rows(c.dpb));
             if (r) return r;
             a.cn = cn_view;
             a.thr = thr;
@@ -649,31 +681,30 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         cs.Q = Q;
         cs.skip_if = scan_gate;
         cs.D = D;
-        // P0: every key of a 1024-row sample; T0 = key of rank j0
-        KNN_CUDA(launch_gather_norms(cn, sp.n0, sp.s0, cn0, n0_pad, s));
-        if ((rc = scan_pass(sp.n0, sp.s0, cn0, nullptr, sp.S0, sp.len0, sp.cap0))) return rc;
-        cs.nseg = 2 * sp.S0;
-        cs.cap = sp.cap0;
-        cs.thr_out = T0;
-        cs.thr_rank = sp.j0;
-        cs.thr_fallback = nullptr;
-        KNN_CUDA(launch_select_cand(cs, s));
-        // P1: keys below T0 over every 16th row; T1 = key of rank j1 (T0 when that fails)
-        KNN_CUDA(launch_gather_norms(cn, sp.n1, sp.s1, cn1, n1_pad, s));
-        if ((rc = scan_pass(sp.n1, sp.s1, cn1, T0, sp.S1, sp.len1, sp.cap1))) return rc;
-        cs.nseg = 2 * sp.S1;
-        cs.cap = sp.cap1;
-        cs.thr_out = T1;
-        cs.thr_rank = sp.j1;
-        cs.thr_fallback = T0;
-        KNN_CUDA(launch_select_cand(cs, s));
-        launches += 4;
+        // seeding, coarse to fine: level l keeps the keys below the previous level's
+        // threshold (the coarsest keeps every key) and yields the key of rank j_l
+        float* cnv = (float*)E.cnv.p;
+        const float* T = nullptr;
+        for (int l = 0; l < sp.levels; ++l) {
+            const ScanLevel& v = sp.lv[l];
+            KNN_CUDA(launch_gather_norms(cn, v.n, v.stride, cnv, v.n_pad, s));
+            if ((rc = scan_pass(v.n, v.stride, cnv, T, v.S, v.len, v.cap))) return rc;
+            cs.nseg = kScanParts * v.S;
+            cs.cap = v.cap;
+            cs.thr_out = Tbuf[l & 1];
+            cs.thr_rank = v.j;
+            cs.thr_fallback = T;  // a level that fails keeps the previous threshold
+            KNN_CUDA(launch_select_cand(cs, s));
+            launches += 3;
+            T = Tbuf[l & 1];
+            cnv += v.n_pad;
+        }
         if ((rc = mark(2))) return rc;
         // main pass
-        if ((rc = scan_pass(N, 1, cn, T1, sp.S, sp.len, sp.cap))) return rc;
+        if ((rc = scan_pass(N, 1, cn, T, sp.S, sp.len, sp.cap))) return rc;
         if ((rc = mark(3))) return rc;
         KNN_CUDA(cudaMemsetAsync(fail_cnt, 0, sizeof(uint32_t), s));
-        cs.nseg = 2 * sp.S;
+        cs.nseg = kScanParts * sp.S;
         cs.cap = sp.cap;
         cs.thr_out = nullptr;
         cs.thr_fallback = nullptr;

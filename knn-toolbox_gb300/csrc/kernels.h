@@ -37,6 +37,14 @@ cudaError_t launch_split(const float* x, int64_t n, int64_t ld, int D, int dp, f
 cudaError_t launch_bf16(const float* x, int64_t n, int64_t ld, int D, int dpb, void* out, uint32_t* not_exact,
                         cudaStream_t s);
 
+// One pass over a row-major matrix: optional BF16 copy out[n][dpb] (dpb = 0: none)
+// with the exactness flag, optional norms[0..n_pad) (+inf padding), same
+// conventions as launch_norms / launch_bf16.  Rows wider than kPrepMaxD fall
+// back to those two kernels.
+constexpr int kPrepMaxD = 383;
+cudaError_t launch_prep_rows(const float* x, int64_t n, int64_t ld, int D, int dpb, void* out, float* norms,
+                             int64_t n_pad, uint32_t* not_exact, cudaStream_t s);
+
 // CUDA-core FP32 fused distance + shortlist.  qpb in {32, 128}.
 size_t simt_smem_bytes(int qpb, int kp);
 // tile_redo (optional): a CTA runs only when tile_redo[blockIdx.x] != 0.
@@ -83,28 +91,36 @@ cudaError_t launch_tc(const TcArgs& a, int splits, bool bf16, cudaStream_t s);
 
 // Tensor-core BF16 threshold scan (csrc/scan_bf16.cu): 128 queries x 256-row
 // corpus tiles; every key strictly below the query's threshold is appended to
-// the query's segment cand[(split*2 + half)][q][0..cap) (in increasing corpus
-// index); cnt[(split*2 + half)][q] = keys found (may exceed cap: overflow).
+// the query's segment cand[(split*kScanParts + part)][q][0..cap) (part = the
+// tile's 64-column quarter; in increasing corpus index), as (raw float bits of
+// the key) << 32 | index; cnt[(split*kScanParts + part)][q] = keys found (may
+// exceed cap: overflow).
 constexpr int kScanTileN = 256;
+constexpr int kScanParts = 4;
 constexpr int kScanMaxRing = 8;
 constexpr size_t kScanSmemLimit = 232448;
 struct ScanArgs {
-    CUtensorMap tm_c;          // corpus bf16 [N][dpb] (view), box {64, 256}, 128B swizzle
-    CUtensorMap tm_q;          // queries bf16 [Q][dpb], box {64, 128}, 128B swizzle
-    const float* cn;           // [>= roundup(N, 256)] corpus norms of the view, +inf padding
+    CUtensorMap tm_c;          // corpus bf16 [N][dpb] (view), box {64, scan_box_rows(dpb)}, 128B swizzle
+    const void* qbf;           // queries bf16 [Q][dpb]
+    const float* cn;           // [>= N + scan_tile_rows(dpb)] corpus norms of the view, +inf padding
     const float* thr;          // [Q] thresholds (null: +inf, every key collected)
     const uint32_t* skip_if;   // optional: the kernel returns at once when *skip_if != 0
-    uint64_t* cand;            // [splits*2][Q][cap]
-    uint32_t* cnt;             // [splits*2][Q]
+    uint64_t* cand;            // [splits*kScanParts][Q][cap]
+    uint32_t* cnt;             // [splits*kScanParts][Q]
     int* err;                  // device error word
     int64_t Q;
     int64_t N;
-    int64_t split_len;         // multiple of 256
+    int64_t split_len;         // multiple of scan_tile_rows(dpb)
     int cap;
     int dpb;                   // D rounded up to 64, <= 256
+    int ksteps;                // MMA K steps of 16 holding data: ceil(D / 16)
     int bps;                   // K-boxes per ring slot (divides dpb/64)
     int ring;                  // ring slots
 };
+// corpus rows per tile (MMA N): 224 for dpb <= 128, 192 for dpb <= 256
+int scan_tile_rows(int dpb);
+// rows of the corpus tensor map's box: the share of a tile one CTA of a cluster loads
+int scan_box_rows(int dpb);
 size_t scan_smem_bytes(int dpb, int bps, int ring);
 // Ring geometry for dpb (want_bps = 0: automatic).  Returns 0 on success.
 int scan_plan(int dpb, int want_bps, int* bps, int* ring);

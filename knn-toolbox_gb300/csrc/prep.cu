@@ -5,6 +5,7 @@
 // row norm is the float rounding of a double sum taken in d order (exact for
 // the integer-valued data of the 1M x 128 workload and within one rounding of
 // exact otherwise); the same convention is used by the CPU oracle.
+#include <algorithm>
 #include <cstdint>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -109,6 +110,101 @@ __global__ void gather_norms_kernel(const float* __restrict__ src, int64_t n, in
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_pad) return;
     out[i] = i < n ? src[i * stride] : __int_as_float(0x7f800000);
+}
+
+// Fused preparation of a row-major matrix in one coalesced read: rows staged in
+// shared memory ([rows][pitch], pitch odd: conflict-free per-row walks), then
+//  * BF16 copy into out[n][dpb] (zero padded) and the "not exactly
+//    representable" flag (*not_exact |= 1), when out / not_exact are given;
+//  * row norms into norms[0..n_pad) (+inf for n <= i < n_pad), when given:
+//    the float rounding of the double sum of x_d^2 in d order.  A row of
+//    integers whose float sum stays below 2^24 is summed in float: every
+//    partial sum is then an exact integer, so the result is the same value.
+template <int kRows>
+__global__ void __launch_bounds__(256) prep_rows_kernel(const float* __restrict__ x, int64_t n, int64_t ld, int D,
+                                                        int dpb, __nv_bfloat16* __restrict__ out,
+                                                        float* __restrict__ norms, int64_t n_pad,
+                                                        uint32_t* __restrict__ not_exact)
+{
+    extern __shared__ float tile[];
+    const int pitch = D | 1;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t r0 = (int64_t)blockIdx.x * kRows;
+    const int rows = (int)max((int64_t)0, min((int64_t)kRows, n - r0));
+    for (int r = warp; r < rows; r += 8) {
+        const float* src = x + (r0 + r) * ld;
+        for (int c = lane; c < D; c += 32) tile[r * pitch + c] = __ldg(src + c);
+    }
+    __syncthreads();
+    if (out != nullptr || not_exact != nullptr) {
+        int bad = 0;
+        for (int r = warp; r < rows; r += 8) {
+            for (int c = 2 * lane; c < dpb; c += 64) {
+                const float v0 = c < D ? tile[r * pitch + c] : 0.f;
+                const float v1 = c + 1 < D ? tile[r * pitch + c + 1] : 0.f;
+                const __nv_bfloat162 b = __floats2bfloat162_rn(v0, v1);
+                if (out) *reinterpret_cast<__nv_bfloat162*>(out + (r0 + r) * dpb + c) = b;
+                bad |= !(__low2float(b) == v0) | !(__high2float(b) == v1);
+            }
+        }
+        bad = __syncthreads_or(bad);
+        if (threadIdx.x == 0 && bad && not_exact) atomicOr(not_exact, 1u);
+    }
+    if (norms != nullptr && threadIdx.x < kRows) {
+        const int64_t i = r0 + threadIdx.x;
+        if (i < n) {
+            const float* row = tile + threadIdx.x * pitch;
+            float s32 = 0.f;
+            bool ints = true;
+            for (int d = 0; d < D; ++d) {
+                const float v = row[d];
+                ints &= v == rintf(v);
+                s32 = __fmaf_rn(v, v, s32);
+            }
+            if (!(ints && s32 < 16777216.f)) {
+                double acc = 0.0;
+                for (int d = 0; d < D; ++d) {
+                    const double v = (double)row[d];
+                    acc = __fma_rn(v, v, acc);
+                }
+                s32 = __double2float_rn(acc);
+            }
+            norms[i] = s32;
+        } else if (i < n_pad) {
+            norms[i] = __int_as_float(0x7f800000);
+        }
+    }
+}
+
+cudaError_t launch_prep_rows(const float* x, int64_t n, int64_t ld, int D, int dpb, void* out, float* norms,
+                             int64_t n_pad, uint32_t* not_exact, cudaStream_t s)
+{
+    const int64_t rows = std::max(n, norms ? n_pad : n);
+    if (rows <= 0) return cudaSuccess;
+    const int pitch = D | 1;
+    if (D > kPrepMaxD) {
+        // wide rows: separate passes
+        cudaError_t e = cudaSuccess;
+        if (norms) e = launch_norms(x, n, ld, D, norms, n_pad, s);
+        if (e == cudaSuccess && (out || not_exact)) e = launch_bf16(x, n, ld, D, dpb, out, not_exact, s);
+        return e;
+    }
+    if (D <= 128) {
+        const size_t smem = (size_t)128 * pitch * 4;
+        cudaError_t e = cudaFuncSetAttribute(prep_rows_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        prep_rows_kernel<128><<<(unsigned)((rows + 127) / 128), 256, smem, s>>>(
+            x, n, ld, D, dpb, static_cast<__nv_bfloat16*>(out), norms, n_pad, not_exact);
+    } else {
+        const size_t smem = (size_t)64 * pitch * 4;
+        cudaError_t e = cudaFuncSetAttribute(prep_rows_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        prep_rows_kernel<64><<<(unsigned)((rows + 63) / 64), 256, smem, s>>>(
+            x, n, ld, D, dpb, static_cast<__nv_bfloat16*>(out), norms, n_pad, not_exact);
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t launch_gather_norms(const float* src, int64_t n, int64_t stride, float* out, int64_t n_pad,

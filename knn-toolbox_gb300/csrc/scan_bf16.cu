@@ -5,32 +5,40 @@
 // (cublasSgemm in pdist_NT, include/utils.h:957-985, followed by
 // bitonic_shared / relloc, src/cuknnBitonic.cu:45-254), restructured for
 // large corpora: instead of keeping a sorted shortlist per query in shared
-// memory, each query carries a threshold T (seeded from a sample of the
-// corpus, see engine.cu) and every key strictly below T is appended to the
+// memory, each query carries a threshold T (seeded from samples of the
+// corpus by the engine) and every key strictly below T is appended to the
 // query's candidate segment in global memory.  The final top-kp is chosen
 // from the segments by select_cand_kernel.  Keys are the reference's ranking
 // key ||c||^2 - 2 q.c (demo/knn.m:5), q.c from BF16 operands with FP32
 // accumulation (exact products), the norm added with one FP32 fma.
 //
-// Tile: 128 queries (MMA M, TMEM lanes) x 256 corpus rows (MMA N).
-// Warp roles (320 threads):
-//   warp 0      producer: the CTA's queries (A, BF16, K-major, 128-byte
-//               swizzle) once, then per tile the corpus norms (1-D bulk copy)
-//               and the corpus K-boxes (2-D TMA, 64 bf16 x 256 rows) into a
-//               ring of slots;
-//   warp 1      TMEM owner (512 columns = two 256-column FP32 accumulators)
-//               and single-thread MMA issuer (tcgen05.mma kind::f16, A and B
-//               from shared memory);
-//   warps 2..9  epilogue: thread = query (TMEM lane); warps 2..5 read the
-//               tile's columns 0..127, warps 6..9 columns 128..255; per
-//               32-column chunk: one tcgen05.ld, 16 packed fma, the minima of
-//               four 8-column groups, one vote; only the groups holding a key
-//               below the lane's threshold are appended, out of line.
+// Tile: 128 queries (MMA M, TMEM lanes) x TN corpus rows (MMA N), TN = 224
+// for up to 128 BF16 columns, 192 for up to 256.  Tensor memory holds two
+// TN-column FP32 accumulators and the A operand (this CTA's queries) in the
+// remaining dpb/2 columns, so shared memory carries only the corpus tiles
+// (a ring of whole tiles where three fit) and their norms.
+// Clusters of two CTAs (neighbouring query tiles, same corpus split) share
+// every corpus tile: each CTA loads half of each box's rows with a multicast
+// TMA into both, and each MMA commit releases the slot in both.
+// Warp roles (576 threads):
+//   warp 0      producer: per tile its half of the corpus K-boxes (2-D TMA
+//               multicast, 64 bf16 x TN/2 rows, 128-byte swizzle) and the
+//               corpus norms (1-D bulk copy);
+//   warp 1      TMEM owner (512 columns) and single-thread MMA issuer
+//               (tcgen05.mma kind::f16, A from TMEM, B from shared memory);
+//   warps 2..17 epilogue: thread = query (TMEM lane); warps 2..5 first write
+//               the queries into TMEM; warps 2+4p..5+4p (p = 0..3) read a
+//               quarter of each tile's columns as a 32-column chunk and a
+//               tail (16 + 8 columns for TN = 224, 16 for 192): per chunk
+//               tcgen05.ld, packed fma, the minima of its 8-column groups,
+//               one vote; only groups holding a key below some lane's
+//               threshold are appended.
 // Every mbarrier wait is bounded; on timeout the kernel records an error code
 // in the device error word and winds down without hanging the GPU.
 #include <algorithm>
 #include <cstdint>
 #include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include "common.cuh"
 #include "kernels.h"
@@ -39,20 +47,22 @@
 namespace knn {
 
 namespace {
-constexpr int kScanThreads = 320;
-constexpr uint32_t kBoxA = kTileQ * 128u;      // 64 bf16 x 128 query rows (16 KB)
-constexpr uint32_t kBoxB = kScanTileN * 128u;  // 64 bf16 x 256 corpus rows (32 KB)
-constexpr int kNormSlots = 4;
-constexpr uint32_t kNormBytes = kNormSlots * kScanTileN * 4u;
+constexpr int kEpiWarps = 4 * kScanParts;  // 4 TMEM lane quarters x kScanParts column ranges
+constexpr int kScanThreads = 32 * (2 + kEpiWarps);
+constexpr int kNormSlots = 8;
+// CTAs per cluster: the cluster's CTAs work on neighbouring query tiles of the
+// same corpus split; each TMA-loads 1/kCluster of every corpus box's rows and
+// multicasts it to all of them, so L2 delivers each tile once per cluster.
+constexpr int kCluster = 2;
+constexpr uint16_t kClusterMask = (1u << kCluster) - 1u;
 constexpr uint32_t kCtrlBytes = 512;
-constexpr int kRowPitch = 36;  // staged keys: [8 warps][32 lanes][36 floats] (conflict-free 16-byte stores)
-constexpr uint32_t kStageBytes = 8u * 32u * kRowPitch * 4u;
 constexpr uint32_t kTmemCols = 512;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
-constexpr uint32_t kIdesc = ptx::idesc_bf16(kTileQ, kScanTileN);
+
+__host__ __device__ constexpr uint32_t box_bytes(int tn) { return (uint32_t)tn * 128u; }  // 64 bf16 x tn rows
+__host__ __device__ constexpr uint32_t norm_bytes(int tn) { return (uint32_t)kNormSlots * tn * 4u; }
 
 struct ScanSmem {
-    unsigned char* a;
     unsigned char* ring;
     float* norms;
     uint64_t* full;    // [kScanMaxRing]
@@ -65,7 +75,6 @@ struct ScanSmem {
     uint64_t* drain;
     uint32_t* tmem_holder;
     volatile int* abort;
-    float* stage;      // [8][32][kRowPitch]
 };
 
 __device__ __forceinline__ bool scan_wait(const ScanArgs& a, const ScanSmem& s, uint64_t* bar, uint32_t parity,
@@ -78,90 +87,64 @@ __device__ __forceinline__ bool scan_wait(const ScanArgs& a, const ScanSmem& s, 
     return false;
 }
 
-// Out of line (one copy of the code): append the keys below T of the flagged
-// 8-column groups of one lane's staged 32-key row, in increasing corpus index.
-static __device__ __noinline__ uint32_t offer_groups(const float* row, uint32_t gm, float T, uint32_t base,
-                                                     uint64_t* out, uint32_t cap, uint32_t cnt)
-{
-    while (gm) {
-        const int g = __ffs(gm) - 1;
-        gm &= gm - 1;
-        const float4 lo = *reinterpret_cast<const float4*>(row + 8 * g);
-        const float4 hi = *reinterpret_cast<const float4*>(row + 8 * g + 4);
-        const float k8[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-        const uint32_t b = base + 8u * (uint32_t)g;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const bool h = k8[j] < T;
-            if (h && cnt < cap) out[cnt] = pack_key(k8[j], b + (uint32_t)j);
-            cnt += h ? 1u : 0u;
-        }
-    }
-    return cnt;
-}
-
 // Minimum of 8 keys (four min instructions).
 __device__ __forceinline__ float min8(const float* k)
 {
     return fminf(ptx::fmin3(ptx::fmin3(k[0], k[1], k[2]), ptx::fmin3(k[3], k[4], k[5]), k[6]), k[7]);
 }
 
-// One 32-column chunk of one lane: keys = ||c||^2 - 2 q.c, the minimum of each
-// 8-column group, one warp vote; when some lane has a group with a key below
-// its threshold, the keys are staged in the lane's shared-memory row and the
-// flagged groups are appended out of line.
-__device__ __forceinline__ void scan_chunk(const float (&v)[32], const float* nrm, float T, uint32_t base,
-                                           uint64_t* out, uint32_t cap, uint32_t& cnt, float* srow)
+// Keys ||c||^2 - 2 q.c of a W-column chunk and the mask of its 8-column groups
+// that hold a key below the lane's threshold.
+template <int W>
+__device__ __forceinline__ uint32_t chunk_keys(const float (&v)[W], const float* nrm, float T, float (&key)[W])
 {
-    float key[32];
     const float4* n4 = reinterpret_cast<const float4*>(nrm);
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
+    for (int u = 0; u < W / 4; ++u) {
         const float4 c = n4[u];
         ptx::fma2(key[4 * u], key[4 * u + 1], v[4 * u], v[4 * u + 1], -2.0f, c.x, c.y);
         ptx::fma2(key[4 * u + 2], key[4 * u + 3], v[4 * u + 2], v[4 * u + 3], -2.0f, c.z, c.w);
     }
-    const uint32_t gm = (min8(key) < T ? 1u : 0u) | (min8(key + 8) < T ? 2u : 0u) |
-                        (min8(key + 16) < T ? 4u : 0u) | (min8(key + 24) < T ? 8u : 0u);
-    if (__any_sync(0xffffffffu, gm != 0u)) {
-        if (gm != 0u) {
-            float4* s4 = reinterpret_cast<float4*>(srow);
+    uint32_t gm = 0;
 #pragma unroll
-            for (int u = 0; u < 8; ++u) s4[u] = make_float4(key[4 * u], key[4 * u + 1], key[4 * u + 2], key[4 * u + 3]);
-            cnt = offer_groups(srow, gm, T, base, out, cap, cnt);
+    for (int g = 0; g < W / 8; ++g) gm |= (min8(key + 8 * g) < T ? 1u : 0u) << g;
+    return gm;
+}
+
+// Append the keys below T of the flagged groups, in increasing corpus index.
+// Words hold the raw key bits above the index; the selection maps them to
+// ordered keys.
+template <int W>
+__device__ __forceinline__ void chunk_append(const float (&key)[W], uint32_t gm, float T, uint32_t base,
+                                             uint64_t* out, uint32_t cap, uint32_t& cnt)
+{
+#pragma unroll
+    for (int g = 0; g < W / 8; ++g) {
+        if ((gm >> g) & 1u) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const float k = key[8 * g + j];
+                const bool h = k < T;
+                if (h && cnt < cap)
+                    out[cnt] = ((uint64_t)__float_as_uint(k) << 32) | (uint64_t)(base + (uint32_t)(8 * g + j));
+                cnt += h ? 1u : 0u;
+            }
         }
     }
 }
-}  // namespace
 
-size_t scan_smem_bytes(int dpb, int bps, int ring)
+template <int TN>
+__global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads, 1)
+    scan_kernel(const __grid_constant__ ScanArgs a)
 {
-    return (size_t)(dpb / 64) * kBoxA + (size_t)ring * bps * kBoxB + kNormBytes + kCtrlBytes + kStageBytes;
-}
+    constexpr int TW = TN / kScanParts - 32;  // tail columns per epilogue part (24 or 16)
+    constexpr uint32_t kBoxB = box_bytes(TN);
+    constexpr uint32_t kIdesc = ptx::idesc_bf16(kTileQ, TN);
+    constexpr uint32_t kACol = 2u * TN;  // A operand columns [kACol, kACol + dpb/2)
+    constexpr int kPieceRows = TN / kCluster;  // rows of every box this CTA loads for the cluster
+    static_assert(kPieceRows % 8 == 0, "pieces of whole 8-row swizzle atoms");
+    static_assert(TW == 24 || TW == 16, "tail chunk of 16 or 24 columns");
 
-int scan_plan(int dpb, int want_bps, int* bps, int* ring)
-{
-    const int nbox = dpb / 64;
-    if (dpb % 64 != 0 || nbox < 1 || nbox > 4) return -1;
-    const size_t fixed = (size_t)nbox * kBoxA + kNormBytes + kCtrlBytes + kStageBytes;
-    auto slots = [&](int b) { return (int)std::min<size_t>(kScanMaxRing, (kScanSmemLimit - fixed) / ((size_t)b * kBoxB)); };
-    int b = 0;
-    if (want_bps > 0) {
-        if (nbox % want_bps != 0 || slots(want_bps) < 2) return -1;
-        b = want_bps;
-    } else {
-        // whole-tile slots (one commit per tile) when two fit, else pairs of boxes, else single boxes
-        for (int cand : {nbox, 2, 1})
-            if (cand <= nbox && nbox % cand == 0 && slots(cand) >= 2) { b = cand; break; }
-    }
-    if (b == 0) return -1;
-    *bps = b;
-    *ring = slots(b);
-    return 0;
-}
-
-__global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const __grid_constant__ ScanArgs a)
-{
     extern __shared__ __align__(1024) unsigned char sm[];
     // device-side path choice: the kernel runs only when *skip_if == 0
     if (a.skip_if != nullptr && *a.skip_if != 0u) return;
@@ -177,10 +160,9 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const __grid_cons
     const int slots_per_tile = nbox / bps;
 
     ScanSmem s;
-    s.a = sm;
-    s.ring = sm + (size_t)nbox * kBoxA;
+    s.ring = sm;
     s.norms = reinterpret_cast<float*>(s.ring + (size_t)R * slot_bytes);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(s.norms) + kNormBytes);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(s.norms) + norm_bytes(TN));
     s.full = bars;
     s.empty = bars + kScanMaxRing;
     s.accf = bars + 2 * kScanMaxRing;
@@ -192,33 +174,31 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const __grid_cons
     uint32_t* words = reinterpret_cast<uint32_t*>(s.drain + 1);
     s.tmem_holder = words;
     s.abort = reinterpret_cast<volatile int*>(words + 1);
-    s.stage = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(bars) + kCtrlBytes);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int64_t q0 = (int64_t)blockIdx.x * kTileQ;
     const int64_t n_begin = (int64_t)blockIdx.y * a.split_len;
     const int64_t n_end = min(a.N, n_begin + a.split_len);
-    const int ntiles = n_end > n_begin ? (int)((n_end - n_begin + kScanTileN - 1) / kScanTileN) : 0;
+    const int ntiles = n_end > n_begin ? (int)((n_end - n_begin + TN - 1) / TN) : 0;
 
     if (tid == 0) {
         for (int i = 0; i < R; ++i) {
             ptx::mbar_init(&s.full[i], 1);
-            ptx::mbar_init(&s.empty[i], 1);
+            ptx::mbar_init(&s.empty[i], kCluster);  // one MMA commit from every CTA of the cluster
         }
         for (int b = 0; b < 2; ++b) {
             ptx::mbar_init(&s.accf[b], 1);
-            ptx::mbar_init(&s.acce[b], 8);
+            ptx::mbar_init(&s.acce[b], kEpiWarps);
         }
         for (int b = 0; b < kNormSlots; ++b) {
             ptx::mbar_init(&s.nfull[b], 1);
-            ptx::mbar_init(&s.nempty[b], 8);
+            ptx::mbar_init(&s.nempty[b], kEpiWarps);
         }
-        ptx::mbar_init(s.aready, 1);
+        ptx::mbar_init(s.aready, 4);
         ptx::mbar_init(s.drain, 1);
         *s.abort = 0;
         ptx::fence_mbar_init();
         ptx::tma_prefetch_desc(&a.tm_c);
-        ptx::tma_prefetch_desc(&a.tm_q);
     }
     if (warp == 1) {
         ptx::tmem_alloc(s.tmem_holder, kTmemCols);
@@ -228,38 +208,40 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const __grid_cons
     __syncthreads();
     ptx::tc_fence_after();
     const uint32_t tmem = *s.tmem_holder;
+    // every CTA's barriers are initialised before any multicast copy or commit reaches them
+    ptx::cluster_sync();
+    const uint32_t crank = ptx::cluster_ctarank();
 
     if (warp == 0) {
         // ------------------------------------------------------------ producer
         if (lane == 0) {
-            // this CTA's queries: rows q0.. of the BF16 query copy (rows past Q read as zeros)
-            ptx::mbar_arrive_expect_tx(s.aready, (uint32_t)nbox * kBoxA);
-            for (int bx = 0; bx < nbox; ++bx)
-                ptx::tma_load_2d(s.a + (size_t)bx * kBoxA, &a.tm_q, s.aready, bx * 64, (int)q0);
             int it = 0;
             bool ok = true;
             for (int t = 0; t < ntiles && ok; ++t) {
-                const int64_t n0 = n_begin + (int64_t)t * kScanTileN;
-                const int ns = t % kNormSlots;
-                if (!scan_wait(a, s, &s.nempty[ns], ((uint32_t)(t / kNormSlots) & 1u) ^ 1u, kDevTimeoutProducer)) {
-                    ok = false;
-                    break;
-                }
-                // norms array padded with +inf to a multiple of 256 rows
-                ptx::mbar_arrive_expect_tx(&s.nfull[ns], kScanTileN * 4u);
-                ptx::bulk_load(s.norms + ns * kScanTileN, a.cn + n0, kScanTileN * 4u, &s.nfull[ns]);
+                const int64_t n0 = n_begin + (int64_t)t * TN;
                 for (int c = 0; c < slots_per_tile; ++c, ++it) {
                     const int st = it % R;
                     const uint32_t ph = (uint32_t)(it / R) & 1u;
                     if (!scan_wait(a, s, &s.empty[st], ph ^ 1u, kDevTimeoutProducer)) { ok = false; break; }
                     unsigned char* dst = s.ring + (size_t)st * slot_bytes;
+                    // this CTA's piece of every box, multicast: the slot fills when all pieces land
                     ptx::mbar_arrive_expect_tx(&s.full[st], slot_bytes);
                     for (int bx = 0; bx < bps; ++bx)
-                        ptx::tma_load_2d(dst + (size_t)bx * kBoxB, &a.tm_c, &s.full[st], (c * bps + bx) * 64, (int)n0);
+                        ptx::tma_load_2d_mc(dst + (size_t)bx * kBoxB + crank * (kPieceRows * 128u), &a.tm_c, &s.full[st],
+                                            (c * bps + bx) * 64, (int)(n0 + crank * kPieceRows), kClusterMask);
                 }
+                if (!ok) break;
+                // norms (needed by the epilogue only, after the MMAs); the array is padded
+                // with +inf at least one tile past the view
+                const int ns = t % kNormSlots;
+                if (!scan_wait(a, s, &s.nempty[ns], ((uint32_t)(t / kNormSlots) & 1u) ^ 1u, kDevTimeoutProducer)) {
+                    ok = false;
+                    break;
+                }
+                ptx::mbar_arrive_expect_tx(&s.nfull[ns], TN * 4u);
+                ptx::bulk_load(s.norms + ns * TN, a.cn + n0, TN * 4u, &s.nfull[ns]);
             }
             // let copies already issued land before the CTA winds down
-            ptx::mbar_wait(s.aready, 0, kTimeoutNs);
             if (!ok) {
                 const int first = it - R > 0 ? it - R : 0;
                 for (int j = first; j < it; ++j) ptx::mbar_wait(&s.full[j % R], (uint32_t)(j / R) & 1u, kTimeoutNs);
@@ -270,14 +252,14 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const __grid_cons
         if (lane == 0) {
             bool ok = scan_wait(a, s, s.aready, 0, kDevTimeoutAload);
             ptx::tc_fence_after();
-            const uint32_t a_base = ptx::smem_u32(s.a);
+            const uint32_t a_tmem = tmem + kACol;
             int it = 0;
             for (int t = 0; t < ntiles && ok; ++t) {
                 const int b = t & 1;
                 const uint32_t use = (uint32_t)(t >> 1);
                 if (!scan_wait(a, s, &s.acce[b], (use & 1u) ^ 1u, kDevTimeoutMma)) { ok = false; break; }
                 ptx::tc_fence_after();
-                const uint32_t d_tmem = tmem + (uint32_t)b * kScanTileN;
+                const uint32_t d_tmem = tmem + (uint32_t)b * TN;
                 for (int c = 0; c < slots_per_tile; ++c, ++it) {
                     const int st = it % R;
                     const uint32_t ph = (uint32_t)(it / R) & 1u;
@@ -285,15 +267,17 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const __grid_cons
                     ptx::tc_fence_after();
                     const uint32_t b_base = ptx::smem_u32(s.ring + (size_t)st * slot_bytes);
                     for (int bx = 0; bx < bps; ++bx) {
-                        const uint32_t box = (uint32_t)(c * bps + bx);
-#pragma unroll
-                        for (int kk = 0; kk < 4; ++kk) {
-                            const uint64_t da = ptx::desc_sw128_kmajor(a_base + box * kBoxA + kk * 32);
+                        const int box = c * bps + bx;
+                        // K steps of 16 past the last data column hold zeros on both sides: skipped
+                        const int kn = min(4, a.ksteps - 4 * box);
+                        for (int kk = 0; kk < kn; ++kk) {
                             const uint64_t db = ptx::desc_sw128_kmajor(b_base + bx * kBoxB + kk * 32);
-                            ptx::mma_bf16_ss(d_tmem, da, db, kIdesc, (box | (uint32_t)kk) != 0u);
+                            ptx::mma_bf16_ts(d_tmem, a_tmem + (uint32_t)(box * 32 + kk * 8), db, kIdesc,
+                                             (box | kk) != 0);
                         }
                     }
-                    ptx::mma_commit(&s.empty[st]);
+                    // the slot is free once every CTA of the cluster has consumed it
+                    ptx::mma_commit_mc(&s.empty[st], kClusterMask);
                 }
                 if (!ok) break;
                 ptx::mma_commit(&s.accf[b]);
@@ -306,18 +290,32 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const __grid_cons
         // ------------------------------------------------------------ epilogue
         const int ew = warp - 2;
         const int quad = warp & 3;  // TMEM lane quarter this warp may access
-        const int half = ew >> 2;   // columns [128*half, 128*half + 128) of each tile
+        const int part = ew >> 2;   // one quarter of each tile's columns (see below)
         const int row = quad * 32 + lane;
         const int64_t q = q0 + row;
         const bool valid = q < a.Q;
         const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
+        if (part == 0) {
+            // A operand: this lane's query (BF16 pairs, lower K index in the low half) into TMEM
+            const uint32_t* qrow = reinterpret_cast<const uint32_t*>(a.qbf) + (valid ? q : 0) * (a.dpb / 2);
+            for (int bx = 0; bx < nbox; ++bx) {
+                float w[32];
+#pragma unroll
+                for (int u = 0; u < 32; ++u) w[u] = valid ? __uint_as_float(__ldg(qrow + bx * 32 + u)) : 0.f;
+                __syncwarp();
+                ptx::tmem_st32(tmem + lane_base + kACol + (uint32_t)(bx * 32), w);
+            }
+            ptx::tmem_wait_st();
+            ptx::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(s.aready);
+        }
         // padding lanes of the last query tile collect nothing
         const float T = valid ? (a.thr ? __ldg(a.thr + q) : __int_as_float(0x7f800000)) : -__int_as_float(0x7f800000);
-        const size_t seg = (size_t)blockIdx.y * 2 + half;
+        const size_t seg = (size_t)blockIdx.y * kScanParts + part;
         uint64_t* out = a.cand + (seg * (size_t)a.Q + (size_t)(valid ? q : 0)) * (size_t)a.cap;
         uint32_t cnt = 0;
         const uint32_t cap = (uint32_t)a.cap;
-        float* srow = s.stage + (size_t)(ew * 32 + lane) * kRowPitch;
         for (int t = 0; t < ntiles; ++t) {
             const int b = t & 1;
             const uint32_t use = (uint32_t)(t >> 1);
@@ -327,31 +325,36 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const __grid_cons
                             scan_wait(a, s, &s.nfull[ns], (uint32_t)(t / kNormSlots) & 1u, kDevTimeoutEpilogue);
             if (!__all_sync(0xffffffffu, ok)) break;
             ptx::tc_fence_after();
-            const float* nrm = s.norms + ns * kScanTileN + half * 128;
-            const uint32_t tb = tmem + (uint32_t)b * kScanTileN + (uint32_t)(half * 128) + lane_base;
-            const uint32_t nb = (uint32_t)(n_begin + (int64_t)t * kScanTileN + half * 128);
-            // four 32-column chunks; the next chunk's TMEM load overlaps this chunk's work
-            float va[32], vb[32];
+            // this part's columns, every TMEM load at a multiple of its own width:
+            // [32p, 32p+32) then the tail [128+16p, 128+16p+16) and, for TN = 224, [192+8p, 192+8p+8)
+            const float* nrm = s.norms + ns * TN;
+            const uint32_t tb = tmem + (uint32_t)b * TN + lane_base;
+            const uint32_t nb = (uint32_t)(n_begin + (int64_t)t * TN);
+            const int c32 = 32 * part, c16 = 128 + 16 * part, c8 = 192 + 8 * part;
+            float va[32], v16[16], v8[8];
             __syncwarp();
-            ptx::tmem_ld32(tb, va);
+            ptx::tmem_ld32(tb + (uint32_t)c32, va);
             ptx::tmem_wait_ld_regs(va);
             __syncwarp();
-            ptx::tmem_ld32(tb + 32u, vb);
-            scan_chunk(va, nrm, T, nb, out, cap, cnt, srow);
-            ptx::tmem_wait_ld_regs(vb);
-            __syncwarp();
-            ptx::tmem_ld32(tb + 64u, va);
-            scan_chunk(vb, nrm + 32, T, nb + 32u, out, cap, cnt, srow);
-            ptx::tmem_wait_ld_regs(va);
-            __syncwarp();
-            ptx::tmem_ld32(tb + 96u, vb);
-            scan_chunk(va, nrm + 64, T, nb + 64u, out, cap, cnt, srow);
-            ptx::tmem_wait_ld_regs(vb);
-            // accumulator b fully read: the MMA may overwrite it while the last chunk is tested
+            ptx::tmem_ld16(tb + (uint32_t)c16, v16);
+            if (TW == 24) ptx::tmem_ld8(tb + (uint32_t)c8, v8);
+            float key[32];
+            const uint32_t ga = chunk_keys<32>(va, nrm + c32, T, key);
+            ptx::tmem_wait_ld();
+            ptx::tie_regs(v16);
+            if (TW == 24) ptx::tie_regs(v8);
+            // accumulator b fully read: the MMA may overwrite it while the keys are tested
             ptx::tc_fence_before();
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&s.acce[b]);
-            scan_chunk(vb, nrm + 96, T, nb + 96u, out, cap, cnt, srow);
+            if (__any_sync(0xffffffffu, ga != 0u)) chunk_append<32>(key, ga, T, nb + (uint32_t)c32, out, cap, cnt);
+            float k16[16], k8[8];
+            const uint32_t g16 = chunk_keys<16>(v16, nrm + c16, T, k16);
+            const uint32_t g8 = TW == 24 ? chunk_keys<8>(v8, nrm + c8, T, k8) : 0u;
+            if (__any_sync(0xffffffffu, (g16 | g8) != 0u)) {
+                chunk_append<16>(k16, g16, T, nb + (uint32_t)c16, out, cap, cnt);
+                if (TW == 24) chunk_append<8>(k8, g8, T, nb + (uint32_t)c8, out, cap, cnt);
+            }
             // norm slot ns fully read
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&s.nempty[ns]);
@@ -366,21 +369,71 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const __grid_cons
         __syncwarp();
         ptx::tmem_dealloc(tmem, kTmemCols);
     }
+    // no CTA leaves while another may still multicast into it or arrive on its barriers
+    ptx::cluster_sync();
+}
+}  // namespace
+
+int scan_tile_rows(int dpb) { return dpb <= 128 ? 224 : 192; }
+
+int scan_box_rows(int dpb) { return scan_tile_rows(dpb) / kCluster; }
+
+size_t scan_smem_bytes(int dpb, int bps, int ring)
+{
+    const int tn = scan_tile_rows(dpb);
+    return (size_t)ring * bps * box_bytes(tn) + norm_bytes(tn) + kCtrlBytes;
+}
+
+int scan_plan(int dpb, int want_bps, int* bps, int* ring)
+{
+    const int nbox = dpb / 64;
+    if (dpb % 64 != 0 || nbox < 1 || nbox > 4) return -1;
+    const int tn = scan_tile_rows(dpb);
+    const size_t fixed = norm_bytes(tn) + kCtrlBytes;
+    auto slots = [&](int b) {
+        return (int)std::min<size_t>(kScanMaxRing, (kScanSmemLimit - fixed) / ((size_t)b * box_bytes(tn)));
+    };
+    int b = 0;
+    if (want_bps > 0) {
+        if (nbox % want_bps != 0 || slots(want_bps) < 2) return -1;
+        b = want_bps;
+    } else {
+        // whole-tile slots (one commit per tile) when three fit, else the largest divisor with two
+        for (int cand : {nbox, 2, 1})
+            if (cand <= nbox && nbox % cand == 0 && slots(cand) >= 3) { b = cand; break; }
+        if (b == 0)
+            for (int cand : {nbox, 2, 1})
+                if (cand <= nbox && nbox % cand == 0 && slots(cand) >= 2) { b = cand; break; }
+    }
+    if (b == 0) return -1;
+    *bps = b;
+    *ring = slots(b);
+    return 0;
 }
 
 cudaError_t launch_scan(const ScanArgs& a, int splits, cudaStream_t st)
 {
     const int nbox = a.dpb / 64;
+    const int tn = scan_tile_rows(a.dpb);
     if (a.dpb % 64 != 0 || nbox < 1 || nbox > 4 || a.bps < 1 || nbox % a.bps != 0 || a.ring < 2 ||
-        a.ring > kScanMaxRing || a.split_len % kScanTileN != 0 || a.cap < 1 || splits < 1)
+        a.ring > kScanMaxRing || a.split_len % tn != 0 || a.cap < 1 || splits < 1 || a.qbf == nullptr)
         return cudaErrorInvalidValue;
     const size_t smem = scan_smem_bytes(a.dpb, a.bps, a.ring);
     if (smem > kScanSmemLimit) return cudaErrorInvalidValue;
     if (a.Q <= 0) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(scan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    dim3 grid((unsigned)((a.Q + kTileQ - 1) / kTileQ), (unsigned)splits);
-    scan_kernel<<<grid, kScanThreads, smem, st>>>(a);
+    // whole clusters: a padding query tile (all rows past Q) still loads its share of the corpus
+    const int64_t qt = (a.Q + kTileQ - 1) / kTileQ;
+    dim3 grid((unsigned)((qt + kCluster - 1) / kCluster * kCluster), (unsigned)splits);
+    cudaError_t e;
+    if (tn == 224) {
+        e = cudaFuncSetAttribute(scan_kernel<224>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        scan_kernel<224><<<grid, kScanThreads, smem, st>>>(a);
+    } else {
+        e = cudaFuncSetAttribute(scan_kernel<192>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        scan_kernel<192><<<grid, kScanThreads, smem, st>>>(a);
+    }
     return cudaGetLastError();
 }
 

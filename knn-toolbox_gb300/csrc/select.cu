@@ -147,6 +147,12 @@ __host__ __device__ inline size_t cand_warp_bytes(int D)
     return (w + 15) & ~(size_t)15;
 }
 
+// scan word (raw float bits of the key << 32 | index) -> ordered word (pack_key)
+__device__ __forceinline__ uint64_t raw_to_ordered(uint64_t w)
+{
+    return pack_key(__uint_as_float((uint32_t)(w >> 32)), (uint32_t)w);
+}
+
 // number of words w[0..n) (shared memory) not above x, summed over the warp
 __device__ __forceinline__ uint32_t count_not_above_u64(const uint64_t* w, int n, uint64_t x)
 {
@@ -257,7 +263,8 @@ __global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandS
         for (int u = 0; u < 8; ++u) {
             const int s = s0 + u;
             n8[u] = s < c.nseg ? min(__ldg(c.cnt + (size_t)s * c.Q + q), (uint32_t)c.cap) : 0u;
-            v8[u] = (uint32_t)lane < n8[u] ? __ldg(c.cand + ((size_t)s * c.Q + q) * c.cap + lane) : 0ull;
+            v8[u] = (uint32_t)lane < n8[u] ? raw_to_ordered(__ldg(c.cand + ((size_t)s * c.Q + q) * c.cap + lane))
+                                           : 0ull;
         }
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
@@ -269,14 +276,14 @@ __global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandS
 #pragma unroll
                 for (int t = 0; t < 7; ++t) {
                     const uint32_t i = 32u * (t + 1) + lane;
-                    t8[t] = i < n8[u] ? __ldg(src + i) : 0ull;
+                    t8[t] = i < n8[u] ? raw_to_ordered(__ldg(src + i)) : 0ull;
                 }
 #pragma unroll
                 for (int t = 0; t < 7; ++t) {
                     const uint32_t i = 32u * (t + 1) + lane;
                     if (i < n8[u]) buf[base + i] = t8[t];
                 }
-                for (uint32_t i = 256u + lane; i < n8[u]; i += 32) buf[base + i] = __ldg(src + i);
+                for (uint32_t i = 256u + lane; i < n8[u]; i += 32) buf[base + i] = raw_to_ordered(__ldg(src + i));
             }
             base += n8[u];
         }
