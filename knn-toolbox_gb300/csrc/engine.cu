@@ -353,7 +353,7 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
             v.S = (int)cdiv(v.n, v.len);
             v.cap = (int)(v.len / kScanParts);
         } else {
-            v.S = auto_splits(qt, tiles, E.sms, 64);
+            v.S = auto_splits(qt, tiles, E.sms, kScanMaxSegs / kScanParts);
             v.len = cdiv(tiles, v.S) * tn;
             v.S = (int)cdiv(v.n, v.len);
             const double hits = (double)P->lv[l - 1].j * (double)v.n / (double)P->lv[l - 1].n;
@@ -365,7 +365,9 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
     }
     // main pass
     const int64_t tiles = cdiv(N, tn);
-    P->S = o.splits > 0 ? std::min<int>(o.splits, (int)tiles) : auto_splits(qt, tiles, E.sms, 64);
+    const int max_splits = kScanMaxSegs / kScanParts;
+    P->S = o.splits > 0 ? std::min<int>(std::min(o.splits, max_splits), (int)tiles)
+                        : auto_splits(qt, tiles, E.sms, max_splits);
     P->len = cdiv(tiles, P->S) * tn;
     P->S = (int)cdiv(N, P->len);
     const double hm = (double)P->lv[L - 1].j * (double)P->lv[L - 1].stride;
@@ -465,7 +467,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         if (rc) return rc;
         ws += E.cn_s.cap + E.redo.cap;
     }
-    if (!c.rerank) {
+    if (!c.rerank || scan) {
         rc = E.qn.ensure(Q * sizeof(float));
         if (rc) return rc;
         ws += E.qn.cap;
@@ -478,7 +480,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         }
         rc = E.bf.ensure((size_t)N * c.dpb * 2);
         if (rc) return rc;
-        rc = E.loflags.ensure(((size_t)cdiv(N, 128) + 2) * sizeof(uint32_t));
+        rc = E.loflags.ensure(((size_t)cdiv(N, 128) + 4) * sizeof(uint32_t));
         if (rc) return rc;
         ws += E.hi.cap + E.lo.cap + E.bf.cap + E.loflags.cap;
     }
@@ -506,7 +508,8 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     if ((rc = mark(0))) return rc;
     int launches = 0;
     float* cn = (float*)E.cn.p;
-    float* qn = c.rerank ? nullptr : (float*)E.qn.p;
+    float* qn = (!c.rerank || scan) ? (float*)E.qn.p : nullptr;
+    uint32_t* int_stats = nullptr;  // integrality / magnitude of corpus and queries (scan path)
     uint64_t* part = (uint64_t*)E.part.p;
     uint32_t* thr_g = (uint32_t*)E.thr.p;
     uint32_t* flags = nullptr;
@@ -516,13 +519,15 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         flags = (uint32_t*)E.loflags.p;
         any_lo = flags + cdiv(N, 128);
         not_exact = any_lo + 1;
-        KNN_CUDA(cudaMemsetAsync(any_lo, 0, 2 * sizeof(uint32_t), s));
+        int_stats = scan ? any_lo + 2 : nullptr;
+        KNN_CUDA(cudaMemsetAsync(any_lo, 0, 4 * sizeof(uint32_t), s));
         // one pass per input: BF16 copy, exactness test, norms.  In the BF16 form the
         // keys are BF16 whatever the data: the "not exact" word stays 0 (the test
         // reports into the unused any_lo word instead).
         uint32_t* exact_word = bf16_only ? any_lo : not_exact;
-        KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, c.dpb, E.bf.p, cn, n_pad, exact_word, s));
-        KNN_CUDA(launch_prep_rows(queries, Q, ldq, D, c.dpb, scan ? E.qbf.p : nullptr, qn, Q, exact_word, s));
+        KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, c.dpb, E.bf.p, cn, n_pad, exact_word, s, int_stats));
+        KNN_CUDA(launch_prep_rows(queries, Q, ldq, D, c.dpb, scan ? E.qbf.p : nullptr, qn, Q, exact_word, s,
+                                  int_stats));
         launches += 2;
         if (!bf16_only) {
             // the TF32 split runs only for data that is not BF16-exact
@@ -716,7 +721,9 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         cs.ldc = ldc;
         cs.queries = queries;
         cs.ldq = ldq;
-        cs.qn = c.rerank ? nullptr : (const float*)E.qn.p;
+        cs.qn = qn;
+        cs.int_stats = int_stats;
+        cs.bf16_inexact = bf16_only ? any_lo : not_exact;
         cs.out_dist = dist;
         cs.out_idx = idx;
         cs.out_idx_f = idx_f;

@@ -42,8 +42,10 @@ cudaError_t launch_bf16(const float* x, int64_t n, int64_t ld, int D, int dpb, v
 // conventions as launch_norms / launch_bf16.  Rows wider than kPrepMaxD fall
 // back to those two kernels.
 constexpr int kPrepMaxD = 383;
+// int_stats (optional, 2 words, zeroed by the caller): [0] |= 1 when some value is not an
+// integer, [1] = max |x| as float bits.
 cudaError_t launch_prep_rows(const float* x, int64_t n, int64_t ld, int D, int dpb, void* out, float* norms,
-                             int64_t n_pad, uint32_t* not_exact, cudaStream_t s);
+                             int64_t n_pad, uint32_t* not_exact, cudaStream_t s, uint32_t* int_stats = nullptr);
 
 // CUDA-core FP32 fused distance + shortlist.  qpb in {32, 128}.
 size_t simt_smem_bytes(int qpb, int kp);
@@ -165,6 +167,7 @@ cudaError_t launch_select(const uint64_t* part, int splits, int64_t Q, int kp, i
 //    trusted (overflow, total < need, total > kCandMax) is appended to
 //    fail_idx (count in *fail_cnt) and gets no result.
 constexpr int kCandMax = 2048;
+constexpr int kScanMaxSegs = 128;  // candidate segments per query (splits x kScanParts)
 struct CandSelect {
     const uint64_t* cand = nullptr;
     const uint32_t* cnt = nullptr;
@@ -190,6 +193,11 @@ struct CandSelect {
     float* out_idx_f = nullptr;
     int32_t* fail_idx = nullptr;
     uint32_t* fail_cnt = nullptr;
+    // exact-key test (optional): keys and distances are exact integers when every corpus and
+    // query value is an integer, 2 * D * max|x|^2 < 2^24 and the BF16 copies are exact; the
+    // re-rank is then skipped (distance = key + qn[q], the same value it would compute)
+    const uint32_t* int_stats = nullptr;  // [0] not-integer flag, [1] max|x| bits (corpus and queries)
+    const uint32_t* bf16_inexact = nullptr;
 };
 cudaError_t launch_select_cand(const CandSelect& c, cudaStream_t s);
 

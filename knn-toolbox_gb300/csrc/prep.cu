@@ -124,7 +124,8 @@ template <int kRows>
 __global__ void __launch_bounds__(256) prep_rows_kernel(const float* __restrict__ x, int64_t n, int64_t ld, int D,
                                                         int dpb, __nv_bfloat16* __restrict__ out,
                                                         float* __restrict__ norms, int64_t n_pad,
-                                                        uint32_t* __restrict__ not_exact)
+                                                        uint32_t* __restrict__ not_exact,
+                                                        uint32_t* __restrict__ int_stats)
 {
     extern __shared__ float tile[];
     const int pitch = D | 1;
@@ -136,6 +137,23 @@ __global__ void __launch_bounds__(256) prep_rows_kernel(const float* __restrict_
         for (int c = lane; c < D; c += 32) tile[r * pitch + c] = __ldg(src + c);
     }
     __syncthreads();
+    if (int_stats != nullptr) {
+        // integrality and magnitude of the data: int_stats[0] |= 1 when some value is not an
+        // integer, int_stats[1] = max(|x|) as float bits (non-negative floats order as integers)
+        int frac = 0;
+        float mx = 0.f;
+        for (int r = warp; r < rows; r += 8)
+            for (int c = lane; c < D; c += 32) {
+                const float v = tile[r * pitch + c];
+                frac |= !(v == rintf(v));
+                mx = fmaxf(mx, fabsf(v));
+            }
+        frac = __syncthreads_or(frac);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) atomicMax(int_stats + 1, __float_as_uint(mx));
+        if (threadIdx.x == 0 && frac) atomicOr(int_stats, 1u);
+    }
     if (out != nullptr || not_exact != nullptr) {
         int bad = 0;
         for (int r = warp; r < rows; r += 8) {
@@ -177,7 +195,7 @@ __global__ void __launch_bounds__(256) prep_rows_kernel(const float* __restrict_
 }
 
 cudaError_t launch_prep_rows(const float* x, int64_t n, int64_t ld, int D, int dpb, void* out, float* norms,
-                             int64_t n_pad, uint32_t* not_exact, cudaStream_t s)
+                             int64_t n_pad, uint32_t* not_exact, cudaStream_t s, uint32_t* int_stats)
 {
     const int64_t rows = std::max(n, norms ? n_pad : n);
     if (rows <= 0) return cudaSuccess;
@@ -187,6 +205,7 @@ cudaError_t launch_prep_rows(const float* x, int64_t n, int64_t ld, int D, int d
         cudaError_t e = cudaSuccess;
         if (norms) e = launch_norms(x, n, ld, D, norms, n_pad, s);
         if (e == cudaSuccess && (out || not_exact)) e = launch_bf16(x, n, ld, D, dpb, out, not_exact, s);
+        if (e == cudaSuccess && int_stats) e = cudaMemsetAsync(int_stats, 0xFF, sizeof(uint32_t), s);  // unknown
         return e;
     }
     if (D <= 128) {
@@ -195,14 +214,14 @@ cudaError_t launch_prep_rows(const float* x, int64_t n, int64_t ld, int D, int d
                                              (int)smem);
         if (e != cudaSuccess) return e;
         prep_rows_kernel<128><<<(unsigned)((rows + 127) / 128), 256, smem, s>>>(
-            x, n, ld, D, dpb, static_cast<__nv_bfloat16*>(out), norms, n_pad, not_exact);
+            x, n, ld, D, dpb, static_cast<__nv_bfloat16*>(out), norms, n_pad, not_exact, int_stats);
     } else {
         const size_t smem = (size_t)64 * pitch * 4;
         cudaError_t e = cudaFuncSetAttribute(prep_rows_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
         prep_rows_kernel<64><<<(unsigned)((rows + 63) / 64), 256, smem, s>>>(
-            x, n, ld, D, dpb, static_cast<__nv_bfloat16*>(out), norms, n_pad, not_exact);
+            x, n, ld, D, dpb, static_cast<__nv_bfloat16*>(out), norms, n_pad, not_exact, int_stats);
     }
     return cudaGetLastError();
 }

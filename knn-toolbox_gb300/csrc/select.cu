@@ -139,10 +139,13 @@ namespace {
 // rows of candidate vectors staged per re-rank batch: [rows][D + 1] floats
 __host__ __device__ inline int cand_stage_rows(int D) { return D <= 128 ? 32 : 16; }
 
-__host__ __device__ inline size_t cand_warp_bytes(int D)
+// candidate words a warp can hold: threshold mode (seeding passes) and result mode
+constexpr int kCandThrMax = 1024;
+
+__host__ __device__ inline size_t cand_warp_bytes(int D, bool thr_mode, bool rerank)
 {
-    const size_t sel = (size_t)kCandMax * 8;
-    const size_t rr = (size_t)kMaxKpTC * 8 + (size_t)cand_stage_rows(D) * (D + 1) * 4;
+    const size_t sel = (size_t)(thr_mode ? kCandThrMax : kCandMax) * 8;
+    const size_t rr = rerank && !thr_mode ? (size_t)kMaxKpTC * 8 + (size_t)cand_stage_rows(D) * (D + 1) * 4 : 0;
     const size_t w = sel > rr ? sel : rr;
     return (w + 15) & ~(size_t)15;
 }
@@ -171,8 +174,9 @@ __device__ __forceinline__ uint32_t count_key_not_above(const uint64_t* w, int n
 }
 
 // Exact distances of cur[0..kp) (direct difference, oracle order: eight partial
-// sums over d mod 8, fixed final tree), candidate rows staged in shared memory
-// with coalesced loads; lane j of a batch computes candidate b0 + j.
+// sums over d mod 8, fixed final tree).  Candidate rows are staged in shared
+// memory ([rows][D + 1]: conflict-free per-lane walks) four rows at a time with
+// coalesced loads; lane j of a batch computes candidate b0 + j.
 __device__ __forceinline__ void rerank_staged(uint64_t* cur, int kp, const float* __restrict__ corpus, int64_t ldc,
                                               const float* qv, int D, float* rows)
 {
@@ -181,11 +185,30 @@ __device__ __forceinline__ void rerank_staged(uint64_t* cur, int kp, const float
     const int pitch = D + 1;
     for (int b0 = 0; b0 < kp; b0 += RB) {
         const int nb = min(RB, kp - b0);
-        for (int r = 0; r < nb; ++r) {
-            const uint64_t w = cur[b0 + r];
-            if (w == kSentinel) continue;
-            const float* src = corpus + (int64_t)unpack_idx(w) * ldc;
-            for (int d = lane; d < D; d += 32) rows[r * pitch + d] = __ldg(src + d);
+        for (int r0 = 0; r0 < nb; r0 += 4) {
+            const float* src[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint64_t w = r0 + u < nb ? cur[b0 + r0 + u] : kSentinel;
+                src[u] = w == kSentinel ? nullptr : corpus + (int64_t)unpack_idx(w) * ldc;
+            }
+            for (int d0 = 0; d0 < D; d0 += 64) {
+                float v[8];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int d = d0 + 32 * h + lane;
+                        v[2 * u + h] = (src[u] != nullptr && d < D) ? __ldg(src[u] + d) : 0.f;
+                    }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int d = d0 + 32 * h + lane;
+                        if (d < D) rows[(r0 + u) * pitch + d] = v[2 * u + h];
+                    }
+            }
         }
         __syncwarp();
         if (lane < nb) {
@@ -216,35 +239,41 @@ __device__ __forceinline__ void rerank_staged(uint64_t* cur, int kp, const float
 }  // namespace
 
 // One warp per query over the threshold scan's segments.
+template <bool kThr>
 __global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandSelect c)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     if (c.skip_if != nullptr && *c.skip_if != 0u) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const size_t wb = cand_warp_bytes(c.D);
+    const size_t wb = cand_warp_bytes(c.D, kThr, c.rerank != 0);
+    const int buf_max = kThr ? kCandThrMax : kCandMax;
     uint64_t* buf = reinterpret_cast<uint64_t*>(smem + (size_t)warp * wb);
     float* qv = reinterpret_cast<float*>(smem + (size_t)kSelWarps * wb) + (size_t)warp * ((c.D + 3) & ~3);
     const int64_t q = (int64_t)blockIdx.x * kSelWarps + warp;
     if (q >= c.Q) return;
 
-    // per-lane segments s = lane, lane + 32, ...: stored and found counts
+    // segments s = lane + 32 r: their counts, all loaded at once
+    constexpr int kSegPerLane = kScanMaxSegs / 32;
+    uint32_t n4[kSegPerLane];
     uint32_t stored = 0, found = 0;
     bool over = false;
-    for (int s = lane; s < c.nseg; s += 32) {
-        const uint32_t n = __ldg(c.cnt + (size_t)s * c.Q + q);
+#pragma unroll
+    for (int r = 0; r < kSegPerLane; ++r) {
+        const int s = lane + 32 * r;
+        const uint32_t n = s < c.nseg ? __ldg(c.cnt + (size_t)s * c.Q + q) : 0u;
         found += n;
         over |= n > (uint32_t)c.cap;
-        stored += min(n, (uint32_t)c.cap);
+        n4[r] = min(n, (uint32_t)c.cap);
+        stored += n4[r];
     }
     const uint32_t total = __reduce_add_sync(0xffffffffu, stored);
     const uint32_t found_all = __reduce_add_sync(0xffffffffu, found);
     const bool overflow = __any_sync(0xffffffffu, over);
 
-    const bool thr_mode = c.thr_out != nullptr;
-    const uint32_t need = thr_mode ? (uint32_t)c.thr_rank : (uint32_t)c.need;
-    if (overflow || found_all < need || total > (uint32_t)kCandMax) {
+    const uint32_t need = kThr ? (uint32_t)c.thr_rank : (uint32_t)c.need;
+    if (overflow || found_all < need || total > (uint32_t)buf_max) {
         if (lane == 0) {
-            if (thr_mode) {
+            if (kThr) {
                 c.thr_out[q] = c.thr_fallback ? c.thr_fallback[q] : __int_as_float(0x7f800000);
             } else {
                 const uint32_t pos = atomicAdd(c.fail_cnt, 1u);
@@ -254,44 +283,33 @@ __global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandS
         return;
     }
 
-    // gather, segment by segment (eight at a time so that their loads overlap)
+    // gather: each lane copies its own segments (segment-major prefix over r, then lanes)
     uint32_t base = 0;
-    for (int s0 = 0; s0 < c.nseg; s0 += 8) {
-        uint32_t n8[8];
-        uint64_t v8[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const int s = s0 + u;
-            n8[u] = s < c.nseg ? min(__ldg(c.cnt + (size_t)s * c.Q + q), (uint32_t)c.cap) : 0u;
-            v8[u] = (uint32_t)lane < n8[u] ? raw_to_ordered(__ldg(c.cand + ((size_t)s * c.Q + q) * c.cap + lane))
-                                           : 0ull;
+    for (int r = 0; r < kSegPerLane; ++r) {
+        uint32_t pre = n4[r];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, pre, o);
+            if (lane >= o) pre += v;
         }
+        const uint32_t tot_r = __shfl_sync(0xffffffffu, pre, 31);
+        const uint32_t my = base + pre - n4[r];
+        const uint64_t* src = c.cand + ((size_t)(lane + 32 * r) * c.Q + q) * c.cap;
+        for (uint32_t i0 = 0; i0 < n4[r]; i0 += 8) {
+            uint64_t v[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            if ((uint32_t)lane < n8[u]) buf[base + lane] = v8[u];
-            if (n8[u] > 32u) {
-                // segments holding more than 32 candidates (every segment of the 1024-row sample pass)
-                const uint64_t* src = c.cand + ((size_t)(s0 + u) * c.Q + q) * c.cap;
-                uint64_t t8[7];
+            for (int u = 0; u < 8; ++u) v[u] = i0 + u < n4[r] ? __ldg(src + i0 + u) : 0ull;
 #pragma unroll
-                for (int t = 0; t < 7; ++t) {
-                    const uint32_t i = 32u * (t + 1) + lane;
-                    t8[t] = i < n8[u] ? raw_to_ordered(__ldg(src + i)) : 0ull;
-                }
-#pragma unroll
-                for (int t = 0; t < 7; ++t) {
-                    const uint32_t i = 32u * (t + 1) + lane;
-                    if (i < n8[u]) buf[base + i] = t8[t];
-                }
-                for (uint32_t i = 256u + lane; i < n8[u]; i += 32) buf[base + i] = raw_to_ordered(__ldg(src + i));
-            }
-            base += n8[u];
+            for (int u = 0; u < 8; ++u)
+                if (i0 + u < n4[r]) buf[my + i0 + u] = raw_to_ordered(v[u]);
         }
+        base += tot_r;
     }
     __syncwarp();
     const int n = (int)total;
 
-    if (thr_mode) {
+    if (kThr) {
         // smallest key x with at least thr_rank keys not above it (bitwise binary search)
         uint32_t x = 0;
         for (int bit = 31; bit >= 0; --bit) {
@@ -335,7 +353,14 @@ __global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandS
     __syncwarp();
     warp_sort_smem(cur, P);
 
-    if (c.rerank) {
+    // exact integer keys: the ranking by key is the ranking by distance, distance = key + ||q||^2
+    bool exact = false;
+    if (c.int_stats != nullptr && c.qn != nullptr) {
+        const float mx = __uint_as_float(__ldg(c.int_stats + 1));
+        exact = __ldg(c.int_stats) == 0u && (c.bf16_inexact == nullptr || __ldg(c.bf16_inexact) == 0u) &&
+                2.0 * (double)c.D * (double)mx * (double)mx < 16777216.0;
+    }
+    if (c.rerank && !exact) {
         const float* qrow = c.queries + q * c.ldq;
         for (int d = lane; d < c.D; d += 32) qv[d] = __ldg(qrow + d);
         __syncwarp();
@@ -380,16 +405,25 @@ cudaError_t launch_select(const uint64_t* part, int splits, int64_t Q, int kp, i
 cudaError_t launch_select_cand(const CandSelect& c, cudaStream_t s)
 {
     if (c.Q <= 0) return cudaSuccess;
-    if (c.nseg < 1 || c.cap < 1 || (c.thr_out == nullptr && (c.kp < 1 || c.kp > kCandMax || c.k > c.kp ||
-                                                              c.fail_idx == nullptr || c.fail_cnt == nullptr)) ||
-        (c.thr_out != nullptr && (c.thr_rank < 1 || c.thr_rank > kCandMax)))
+    const bool thr = c.thr_out != nullptr;
+    if (c.nseg < 1 || c.nseg > kScanMaxSegs || c.cap < 1 ||
+        (!thr && (c.kp < 1 || c.kp > kMaxKpTC || c.k > c.kp || c.fail_idx == nullptr || c.fail_cnt == nullptr ||
+                  (!c.rerank && c.qn == nullptr))) ||
+        (thr && (c.thr_rank < 1 || c.thr_rank > kCandThrMax)))
         return cudaErrorInvalidValue;
-    if (c.thr_out == nullptr && c.kp > kMaxKpTC) return cudaErrorInvalidValue;
-    const size_t smem = (size_t)kSelWarps * cand_warp_bytes(c.D) + (size_t)kSelWarps * ((c.D + 3) & ~3) * 4;
-    cudaError_t e = cudaFuncSetAttribute(select_cand_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    unsigned blocks = (unsigned)((c.Q + kSelWarps - 1) / kSelWarps);
-    select_cand_kernel<<<blocks, kSelWarps * 32, smem, s>>>(c);
+    const size_t smem = (size_t)kSelWarps * cand_warp_bytes(c.D, thr, c.rerank != 0) +
+                        (size_t)kSelWarps * ((c.D + 3) & ~3) * 4;
+    const unsigned blocks = (unsigned)((c.Q + kSelWarps - 1) / kSelWarps);
+    cudaError_t e;
+    if (thr) {
+        e = cudaFuncSetAttribute(select_cand_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        select_cand_kernel<true><<<blocks, kSelWarps * 32, smem, s>>>(c);
+    } else {
+        e = cudaFuncSetAttribute(select_cand_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        select_cand_kernel<false><<<blocks, kSelWarps * 32, smem, s>>>(c);
+    }
     return cudaGetLastError();
 }
 

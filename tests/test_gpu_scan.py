@@ -131,3 +131,22 @@ def test_bf16_precision_form_on_scan(engine, oracle, D, c):
     # FP32 accumulation may differ in the last bit on near-ties)
     d0, i0, _ = run(engine, X, Qs, k, precision=engine.PREC_BF16, shortlist=c, scan=engine.SCAN_OFF)
     assert (i == i0).mean() >= 0.999
+
+
+@pytest.mark.parametrize("D,hi", [(64, 256), (256, 256), (128, 1024)])
+def test_integer_data_exact_and_reranked_keys(engine, oracle, D, hi):
+    # 64 x 255^2 keeps every key an exact float integer (the re-rank is skipped);
+    # 256 x 255^2 does not, and values up to 1023 are not BF16-exact: both re-rank
+    X, Qs = ints(30000, 140, D, 7 * D + hi, hi=hi)
+    k = 12
+    d, i, st = run(engine, X, Qs, k, precision=engine.PREC_BF16, shortlist=4, scan=engine.SCAN_ON)
+    assert st["scan"] == 1
+    od, oi = oracle.knn_gemm(X, Qs, k, kp=st["kp"], rerank=True)
+    if hi <= 256:
+        np.testing.assert_array_equal(i, oi)
+        np.testing.assert_array_equal(d, od)
+    else:
+        # BF16 keys pick the shortlist: recall against the exact answer, exact distances returned
+        assert oracle.recall_at_k(i, oracle.knn_f64(X, Qs, k)[1]) >= 0.99
+        got64 = oracle.pair_dist_f64(X, Qs, i)
+        assert (np.abs(d - got64) <= DIST_REL * got64 + 1e-6).all()
