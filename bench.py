@@ -39,6 +39,10 @@ WORKLOADS = {
     "mix4m": dict(desc="Gaussian mixture corpus 4,000,000 x 96 (1,024 centres N(0,1), sigma 0.15, rows "
                        "L2-normalised), 10,000 queries, k=10, seed 2",
                   gen="gauss_mixture", N=4_000_000, D=96, Q=10_000, k=10, seed=2),
+    # serving form: resident corpus, Poisson arrivals of requests of uneven size and k
+    "serve2m": dict(desc="serving: int-descriptor corpus 2,000,000 x 128 resident (FP32 + BF16 + TF32 copies), "
+                         "Poisson arrivals, request sizes log-uniform on [1,512], k in {1,10,100}, seed 1",
+                    gen="int_descriptor", N=2_000_000, D=128, Q=0, k=0, seed=1, serve=True),
     # profiling cut of int1m: full corpus (same candidate density per corpus row), a quarter of the queries
     "int1m_q2500": dict(desc="int-descriptor corpus 1,000,000 x 128, 2,500 queries, k=100, seed 1",
                         gen="int_descriptor", N=1_000_000, D=128, Q=2_500, k=100, seed=1),
@@ -378,6 +382,90 @@ def run_gb300(args, w):
     return 0
 
 
+def run_serve(args, w):
+    """Serving form: a request server over a resident index under Poisson load."""
+    import queue
+    import threading
+    import torch
+    import cuknns
+    import cuknns.synth as S
+
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(w["seed"] + 7)
+    n_req = args.requests
+    sizes = np.minimum(512, np.exp(rng.uniform(0.0, np.log(512.0), n_req)).astype(np.int64) + 0)
+    sizes = np.maximum(sizes, 1)
+    ks = rng.choice([1, 10, 100], n_req)
+    corpus_np, queries_np = S.int_descriptor(w["N"], w["D"], seed=w["seed"], nq=int(sizes.sum()))
+    c = torch.from_numpy(corpus_np).cuda()
+    ix = cuknns.Index(c)
+    prec = cuknns.PREC_BF16 if args.precision == "bf16" else cuknns.PREC_EXACT
+    srv = cuknns.Server(ix, slots=2, max_batch=1024, precision=prec, shortlist=args.shortlist, autotune=True)
+    t0 = time.perf_counter()
+    srv.warmup([32, 64, 128, 256, 512, 1024], [1, 10, 100])
+    warm_s = time.perf_counter() - t0
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n_req))
+    ids = queue.Queue()
+    lat = [0.0] * n_req
+    res = [None] * n_req
+
+    def waiter():
+        while True:
+            item = ids.get()
+            if item is None:
+                return
+            j, rid = item
+            d, i, ms = srv.wait(rid)
+            lat[j] = ms
+            res[j] = i
+
+    pool = [threading.Thread(target=waiter) for _ in range(8)]
+    for t in pool:
+        t.start()
+    with ClockSampler(0) as clk:
+        start = time.perf_counter()
+        for j in range(n_req):
+            dt = arrivals[j] - (time.perf_counter() - start)
+            if dt > 0:
+                time.sleep(dt)
+            ids.put((j, srv.submit(queries_np[offs[j]:offs[j + 1]], int(ks[j]))))
+        for _ in pool:
+            ids.put(None)
+        for t in pool:
+            t.join()
+        wall = time.perf_counter() - start
+    st = srv.stats()
+    # every request's answer is the one the same request gets alone: spot-check a sample
+    checked = 0
+    for j in np.linspace(0, n_req - 1, 16).astype(int):
+        q = torch.from_numpy(queries_np[offs[j]:offs[j + 1]]).cuda()
+        _, i0 = ix.search(q, int(ks[j]), precision=prec, shortlist=args.shortlist)
+        checked += int(np.array_equal(res[j], i0.cpu().numpy()))
+    srv.close()
+    ix.close()
+    lat_a = np.array(lat)
+    total_q = int(sizes.sum())
+    line = {"metric": "queries/s and p50/p99 request latency, serving form (continuous batching)",
+            "value": total_q / wall, "unit": "queries/s", "n_gpus": 1, "steps": n_req, "warmup": 0,
+            "ms_per_step": wall * 1e3 / n_req, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if prec == cuknns.PREC_EXACT else "bf16 keys, f32 re-rank", "data": "synthetic",
+            "config": {"workload": w["desc"], "N": w["N"], "D": w["D"], "requests": n_req,
+                       "offered_rate_rps": args.rate, "mean_request_queries": float(sizes.mean()),
+                       "slots": 2, "max_batch": 1024, "graph_warmup_s": warm_s},
+            "latency_ms": {"p50": float(np.percentile(lat_a, 50)), "p99": float(np.percentile(lat_a, 99)),
+                           "mean": float(lat_a.mean()), "max": float(lat_a.max())},
+            "served": {"launches": st["launches"], "queries_per_launch": st["queries"] / max(1, st["launches"]),
+                       "graphs": st["graphs"], "achieved_rate_rps": n_req / wall,
+                       "answers_equal_alone": f"{checked}/16 sampled requests"},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -393,6 +481,8 @@ def main():
     ap.add_argument("--scan", default="auto", choices=["auto", "on", "off"],
                     help="threshold-scan path for BF16 keys (auto: corpora of 131,072 rows and more)")
     ap.add_argument("--scan-boxes", type=int, default=0, help="threshold scan: K boxes per ring slot (0 = auto)")
+    ap.add_argument("--rate", type=float, default=5000.0, help="serving: offered requests per second")
+    ap.add_argument("--requests", type=int, default=4000, help="serving: requests in the timed run")
     ap.add_argument("--recall-queries", type=int, default=0,
                     help="measure recall@k and distance error against the FP64 oracle on this many queries")
     args = ap.parse_args()
@@ -401,6 +491,8 @@ def main():
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
         return run_reference(args, w)
+    if w.get("serve"):
+        return run_serve(args, w)
     return run_gb300(args, w)
 
 

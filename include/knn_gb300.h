@@ -151,6 +151,59 @@ int knns_timing_collect5(double ms[5], int *count);
 int knns_search_device_noalloc(const float *corpus, int64_t N, int64_t ldc, const float *queries, int64_t Q,
                                int64_t ldq, int D, int k, float *dist, int32_t *idx, void *stream);
 
+/*
+ * Resident index (no counterpart in the reference, whose drivers copy the corpus
+ * to the device on every call, src/cuknnBitonic.cu:493-512).  knns_index_create
+ * prepares a device corpus once -- BF16 copy, row norms, the exactness and
+ * integrality flags and, with KNNS_INDEX_TF32, the TF32 hi/lo copies the exact
+ * form needs for data that are not BF16-exact -- and synchronises `stream`.
+ * The caller keeps the FP32 corpus alive and unchanged while the index is used;
+ * searches on it skip the corpus preparation.  D <= 256.
+ */
+#define KNNS_INDEX_TF32 1
+typedef struct knns_index knns_index;
+int knns_index_create(const float *corpus, int64_t N, int64_t ldc, int D, int flags, knns_index **out,
+                      void *stream);
+int knns_index_search(knns_index *index, const float *queries, int64_t Q, int64_t ldq, int k, float *dist,
+                      int32_t *idx, const knns_options *opt, void *stream);
+void knns_index_destroy(knns_index *index);
+
+/*
+ * Serving form (no counterpart in the reference): a request server over a
+ * resident index.  Requests of uneven size (1..max_batch queries, host memory,
+ * copied at submit) and k (1..128) arrive at any time from any thread; one worker
+ * thread packs the pending requests that share the oldest request's k into
+ * launches of at most max_batch queries, keeps `slots` launches in flight on
+ * their own streams and workspaces (a batch formed while another runs overlaps
+ * it on the device), and runs each launch as a CUDA graph captured once per
+ * (size bucket, k) and slot (buckets: powers of two from 32 to max_batch).  With
+ * autotune = 1 the corpus split count of each graph is chosen by timing
+ * candidates before capture.  A request's results are the ones a search of that
+ * request alone returns (same k, same computation per query).
+ */
+typedef struct knns_server knns_server;
+typedef struct knns_server_config {
+    int slots;     /* launches in flight (default 2) */
+    int max_batch; /* queries per launch, a power of two (default 1024) */
+    int precision; /* KNNS_PREC_* (default exact) */
+    int shortlist; /* KNNS_PREC_BF16: shortlist factor c (0 = 4) */
+    int autotune;  /* 1 (default): time candidate split counts before capturing a graph */
+    int reserved[3];
+} knns_server_config;
+void knns_server_default_config(knns_server_config *cfg);
+int knns_server_create(knns_index *index, const knns_server_config *cfg, knns_server **out);
+/* Returns the request id (> 0), or minus an error code. */
+int64_t knns_server_submit(knns_server *server, const float *queries, int64_t Q, int k);
+/* Blocks until the request is answered; dist / idx receive Q x k values (may be NULL). */
+int knns_server_wait(knns_server *server, int64_t id, float *dist, int32_t *idx, double *latency_ms);
+/* Capture, on every slot, the graphs of each bucket (rounded up to a power of two) x k
+   before traffic (otherwise each is captured at its first use).  Call it while no
+   request is pending. */
+int knns_server_warmup(knns_server *server, const int *buckets, int nb, const int *ks, int nk);
+/* out: requests submitted, launches, queries launched, graphs captured. */
+int knns_server_stats(knns_server *server, int64_t out[4]);
+void knns_server_destroy(knns_server *server);
+
 /* Library version as 10000*major + 100*minor + patch. */
 int knns_version(void);
 

@@ -313,7 +313,7 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
     if (scan_plan(dpb, o.scan_boxes, &P->bps, &P->ring) != 0)
         return set_error(KNNS_ERR_UNSUPPORTED, "threshold scan: no ring geometry for %d BF16 columns with %d boxes per slot",
                          dpb, o.scan_boxes);
-    const int64_t qt = cdiv(Q, kTileQ);
+    const int64_t qt = cdiv(cdiv(Q, kTileQ), 2) * 2;  // query tiles, padded to whole CTA pairs
     const int tn = scan_tile_rows(dpb);
     // levels, finest first: strides 16, 256, ... until the sample fits the selector whole
     int64_t st[kMaxSeedLevels];
@@ -391,7 +391,7 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
 // ---------------------------------------------------------------- search
 int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const float* queries, int64_t Q, int64_t ldq,
                int D, int k, float* dist, int32_t* idx, float* idx_f, const knns_options& o, cudaStream_t s,
-               knns_stats* st)
+               knns_stats* st, const PreparedCorpus* pc, bool capture)
 {
     if (N <= 0 || D <= 0 || k <= 0 || Q < 0) return set_error(KNNS_ERR_INVALID, "invalid sizes N=%lld Q=%lld D=%d k=%d",
                                                                (long long)N, (long long)Q, D, k);
@@ -423,13 +423,25 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         }
     }
     const bool run_old = !(scan && bf16_only);  // the shortlist path is needed (possibly gated)
+    if (pc != nullptr) {
+        if (pc->corpus != corpus || pc->N != N || pc->ldc != ldc || pc->D != D || pc->dpb != c.dpb)
+            return set_error(KNNS_ERR_INVALID, "prepared corpus does not match the search's corpus");
+        if (c.algo == KNNS_ALGO_TC && !bf16_only && !pc->tf32)
+            return set_error(KNNS_ERR_INVALID, "the exact form needs an index prepared with TF32 copies");
+        if (c.algo == KNNS_ALGO_TC && !bf16_only && pc->dp != c.dp)
+            return set_error(KNNS_ERR_INVALID, "prepared corpus has TF32 copies of another width");
+    }
 
     // norms padded with +inf at least one tile (of any kernel) past the corpus
     const int64_t n_pad = cdiv(N, kScanTileN) * kScanTileN + kScanTileN;
     size_t ws = 0;
-    rc = E.cn.ensure(n_pad * sizeof(float));
+    if (!pc) {
+        rc = E.cn.ensure(n_pad * sizeof(float));
+        if (rc) return rc;
+        ws += E.cn.cap;
+    }
+    rc = E.words.ensure(8 * sizeof(uint32_t));
     if (rc) return rc;
-    ws += E.cn.cap;
     rc = E.thr.ensure(Q * sizeof(uint32_t));
     if (rc) return rc;
     ws += E.thr.cap;
@@ -472,7 +484,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         if (rc) return rc;
         ws += E.qn.cap;
     }
-    if (c.algo == KNNS_ALGO_TC) {
+    if (c.algo == KNNS_ALGO_TC && !pc) {
         if (!bf16_only) {
             rc = E.hi.ensure((size_t)N * c.dp * sizeof(float));
             if (!rc) rc = E.lo.ensure((size_t)N * c.dp * sizeof(float));
@@ -484,6 +496,10 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         if (rc) return rc;
         ws += E.hi.cap + E.lo.cap + E.bf.cap + E.loflags.cap;
     }
+    // corpus-side buffers: the index's, or this engine's
+    const void* bf_p = pc ? pc->bf.p : E.bf.p;
+    const float* hi_p = (const float*)(pc ? pc->hi.p : E.hi.p);
+    const float* lo_p = (const float*)(pc ? pc->lo.p : E.lo.p);
     if (scan) {
         rc = E.qbf.ensure((size_t)Q * c.dpb * 2);
         if (!rc) rc = E.cand.ensure(sp.cand_words * sizeof(uint64_t));
@@ -498,7 +514,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     }
     ws += E.part.cap + E.thr2.cap;
 
-    KNN_CUDA(cudaStreamWaitEvent(s, E.last_done, 0));
+    if (!capture) KNN_CUDA(cudaStreamWaitEvent(s, E.last_done, 0));
     cudaEvent_t tv[Engine::kTimingEvents] = {};
     if (o.timing && E.timing_slot(tv) != KNNS_OK) return KNNS_ERR_CUDA;
     auto mark = [&](int i) -> int {
@@ -507,42 +523,51 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     };
     if ((rc = mark(0))) return rc;
     int launches = 0;
-    float* cn = (float*)E.cn.p;
+    float* cn = (float*)(pc ? pc->cn.p : E.cn.p);
     float* qn = (!c.rerank || scan) ? (float*)E.qn.p : nullptr;
-    uint32_t* int_stats = nullptr;  // integrality / magnitude of corpus and queries (scan path)
     uint64_t* part = (uint64_t*)E.part.p;
     uint32_t* thr_g = (uint32_t*)E.thr.p;
-    uint32_t* flags = nullptr;
-    uint32_t* any_lo = nullptr;
-    uint32_t* not_exact = nullptr;
+    // flag words of this search: [0] TF32 low part in the corpus, [1] corpus or queries not
+    // BF16-exact, [2..3] integrality / max |x| of corpus and queries, [4] always zero
+    uint32_t* words = (uint32_t*)E.words.p;
+    uint32_t* any_lo = words;
+    uint32_t* not_exact = words + 1;
+    uint32_t* int_stats = words + 2;
+    const uint32_t* zero_word = words + 4;
+    uint32_t* flags = c.algo == KNNS_ALGO_TC ? (uint32_t*)(pc ? pc->tiles.p : E.loflags.p) : nullptr;
+    if (pc) {
+        KNN_CUDA(cudaMemcpyAsync(words, pc->words.p, 4 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+        KNN_CUDA(cudaMemsetAsync(words + 4, 0, sizeof(uint32_t), s));
+    } else {
+        KNN_CUDA(cudaMemsetAsync(words, 0, 5 * sizeof(uint32_t), s));
+    }
     if (c.algo == KNNS_ALGO_TC) {
-        flags = (uint32_t*)E.loflags.p;
-        any_lo = flags + cdiv(N, 128);
-        not_exact = any_lo + 1;
-        int_stats = scan ? any_lo + 2 : nullptr;
-        KNN_CUDA(cudaMemsetAsync(any_lo, 0, 4 * sizeof(uint32_t), s));
-        // one pass per input: BF16 copy, exactness test, norms.  In the BF16 form the
-        // keys are BF16 whatever the data: the "not exact" word stays 0 (the test
-        // reports into the unused any_lo word instead).
-        uint32_t* exact_word = bf16_only ? any_lo : not_exact;
-        KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, c.dpb, E.bf.p, cn, n_pad, exact_word, s, int_stats));
-        KNN_CUDA(launch_prep_rows(queries, Q, ldq, D, c.dpb, scan ? E.qbf.p : nullptr, qn, Q, exact_word, s,
+        // one pass per input: BF16 copy, exactness test, integrality, norms
+        if (!pc) {
+            KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, c.dpb, E.bf.p, cn, n_pad, not_exact, s, int_stats));
+            ++launches;
+        }
+        KNN_CUDA(launch_prep_rows(queries, Q, ldq, D, c.dpb, scan ? E.qbf.p : nullptr, qn, Q, not_exact, s,
                                   int_stats));
-        launches += 2;
-        if (!bf16_only) {
+        ++launches;
+        if (!bf16_only && !pc) {
             // the TF32 split runs only for data that is not BF16-exact
             KNN_CUDA(launch_split(corpus, N, ldc, D, c.dp, (float*)E.hi.p, (float*)E.lo.p, flags, any_lo, not_exact,
                                   s));
             ++launches;
         }
     } else {
-        KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, 0, nullptr, cn, n_pad, nullptr, s));
-        ++launches;
+        if (!pc) {
+            KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, 0, nullptr, cn, n_pad, nullptr, s));
+            ++launches;
+        }
         if (qn) {
             KNN_CUDA(launch_prep_rows(queries, Q, ldq, D, 0, nullptr, qn, Q, nullptr, s));
             ++launches;
         }
     }
+    // gate of the BF16 kernels: in the BF16 form they always run
+    const uint32_t* bf_gate = bf16_only ? zero_word : not_exact;
     if ((rc = mark(1))) return rc;
 
     // One shortlist pass over a corpus view: rows 0, stride, 2*stride, ... (nview
@@ -554,12 +579,12 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
             memset(&a, 0, sizeof(a));
             int r = 0;
             if (!bf16_only) {
-                r = encode_rows(&a.tm_hi, (const float*)E.hi.p, nview, c.dp, stride * c.dp);
-                if (!r) r = encode_rows(&a.tm_lo, (const float*)E.lo.p, nview, c.dp, stride * c.dp);
+                r = encode_rows(&a.tm_hi, hi_p, nview, c.dp, stride * c.dp);
+                if (!r) r = encode_rows(&a.tm_lo, lo_p, nview, c.dp, stride * c.dp);
             }
-            if (!r) r = encode_rows_bf16(&a.tm_bf, E.bf.p, nview, c.dpb, stride * c.dpb);
+            if (!r) r = encode_rows_bf16(&a.tm_bf, bf_p, nview, c.dpb, stride * c.dpb);
             if (r) return r;
-            a.not_exact = not_exact;
+            a.not_exact = bf_gate;
             a.tile_redo = redo;
             a.dpb = c.dpb;
             a.cn = cn_view;
@@ -669,7 +694,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         a.ring = sp.ring;
         auto scan_pass = [&](int64_t nview, int64_t stride, const float* cn_view, const float* thr, int splits,
                              int64_t split_len, int cap) -> int {
-            int r = encode_rows_bf16(&a.tm_c, E.bf.p, nview, c.dpb, stride * c.dpb, scan_box_rows(c.dpb));
+            int r = encode_rows_bf16(&a.tm_c, bf_p, nview, c.dpb, stride * c.dpb, scan_box_rows(c.dpb));
             if (r) return r;
             a.cn = cn_view;
             a.thr = thr;
@@ -723,7 +748,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         cs.ldq = ldq;
         cs.qn = qn;
         cs.int_stats = int_stats;
-        cs.bf16_inexact = bf16_only ? any_lo : not_exact;
+        cs.bf16_inexact = not_exact;
         cs.out_dist = dist;
         cs.out_idx = idx;
         cs.out_idx_f = idx_f;
@@ -738,11 +763,11 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
             if (rows <= 0) return KNNS_OK;
             TcArgs t;
             memset(&t, 0, sizeof(t));
-            int r = encode_rows_bf16(&t.tm_bf, E.bf.p, N, c.dpb, c.dpb);
+            int r = encode_rows_bf16(&t.tm_bf, bf_p, N, c.dpb, c.dpb);
             if (r) return r;
             uint32_t* thr2 = (uint32_t*)E.thr2.p;
             KNN_CUDA(cudaMemsetAsync(thr2, 0xFF, rows * sizeof(uint32_t), s));
-            t.not_exact = not_exact;  // the BF16 variant runs when the data are BF16 (always in the BF16 form)
+            t.not_exact = bf_gate;  // the BF16 variant runs when the data are BF16 (always in the BF16 form)
             t.dpb = c.dpb;
             t.cn = cn;
             t.queries = queries;
@@ -774,10 +799,53 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         if ((rc = fix_pass(sp.fixA_rows, sp.fixB_rows, sp.fixB_S, sp.fixB_len))) return rc;
         if ((rc = mark(5))) return rc;
     }
-    KNN_CUDA(cudaEventRecord(E.last_done, s));
+    if (!capture) KNN_CUDA(cudaEventRecord(E.last_done, s));
     if (st)
         *st = knns_stats{c.algo, c.splits, c.kp, c.stages, launches, (pilot || scan) ? 1 : 0, (int64_t)ws,
                          scan ? 1 : 0, scan ? sp.S : 0, scan ? sp.cap : 0, scan ? 100 * sp.ring + sp.bps : 0};
+    return KNNS_OK;
+}
+
+void PreparedCorpus::release()
+{
+    cn.release();
+    bf.release();
+    hi.release();
+    lo.release();
+    tiles.release();
+    words.release();
+}
+
+int prepare_corpus(Engine& E, PreparedCorpus* pc, const float* corpus, int64_t N, int64_t ldc, int D, bool tf32,
+                   cudaStream_t s)
+{
+    if (!pc || !corpus || N <= 0 || D <= 0 || ldc < D) return set_error(KNNS_ERR_INVALID, "invalid corpus");
+    if (N > 0x7fffffffLL) return set_error(KNNS_ERR_UNSUPPORTED, "corpus larger than 2^31-1 rows");
+    if (E.cc < 100) return set_error(KNNS_ERR_UNSUPPORTED, "a prepared corpus needs sm_100+");
+    const int dpb = (D + 63) & ~63, dp = (D + 31) & ~31;
+    if (dpb > 256) return set_error(KNNS_ERR_UNSUPPORTED, "a prepared corpus needs D <= 256");
+    tf32 = tf32 && dp <= kMaxDpTC;
+    const int64_t n_pad = cdiv(N, kScanTileN) * kScanTileN + kScanTileN;
+    int rc = pc->cn.ensure(n_pad * sizeof(float));
+    if (!rc) rc = pc->bf.ensure((size_t)N * dpb * 2);
+    if (!rc) rc = pc->words.ensure(8 * sizeof(uint32_t));
+    if (!rc) rc = pc->tiles.ensure(((size_t)cdiv(N, 128) + 1) * sizeof(uint32_t));
+    if (!rc && tf32) rc = pc->hi.ensure((size_t)N * dp * sizeof(float));
+    if (!rc && tf32) rc = pc->lo.ensure((size_t)N * dp * sizeof(float));
+    if (rc) return rc;
+    uint32_t* w = (uint32_t*)pc->words.p;
+    KNN_CUDA(cudaMemsetAsync(w, 0, 8 * sizeof(uint32_t), s));
+    KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, dpb, pc->bf.p, (float*)pc->cn.p, n_pad, w + 1, s, w + 2));
+    if (tf32)
+        KNN_CUDA(launch_split(corpus, N, ldc, D, dp, (float*)pc->hi.p, (float*)pc->lo.p, (uint32_t*)pc->tiles.p, w,
+                              nullptr, s));
+    pc->corpus = corpus;
+    pc->N = N;
+    pc->ldc = ldc;
+    pc->D = D;
+    pc->dpb = dpb;
+    pc->dp = dp;
+    pc->tf32 = tf32;
     return KNNS_OK;
 }
 
@@ -982,6 +1050,57 @@ int knns_timing_collect5(double ms[5], int* count)
     clear_error();
     if (!ms) return set_error(KNNS_ERR_INVALID, "null output");
     return timing_collect(ms, count);
+}
+
+int knns_index_create(const float* corpus, int64_t N, int64_t ldc, int D, int flags, knns_index** out, void* stream)
+{
+    clear_error();
+    if (!out) return set_error(KNNS_ERR_INVALID, "null output");
+    *out = nullptr;
+    Engine* E = nullptr;
+    int rc = get_engine(&E);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(E->mu);
+    std::unique_ptr<knns_index> ix(new knns_index());
+    ix->device = E->device;
+    cudaStream_t s = (cudaStream_t)stream;
+    rc = prepare_corpus(*E, &ix->pc, corpus, N, ldc, D, (flags & KNNS_INDEX_TF32) != 0, s);
+    if (rc) {
+        ix->pc.release();
+        return rc;
+    }
+    // the first search on any stream sees the prepared buffers
+    KNN_CUDA(cudaStreamSynchronize(s));
+    *out = ix.release();
+    return KNNS_OK;
+}
+
+int knns_index_search(knns_index* ix, const float* queries, int64_t Q, int64_t ldq, int k, float* dist, int32_t* idx,
+                      const knns_options* opt, void* stream)
+{
+    clear_error();
+    if (!ix) return set_error(KNNS_ERR_INVALID, "null index");
+    knns_options o;
+    if (opt) o = *opt;
+    else knns_default_options(&o);
+    Engine* E = nullptr;
+    int rc = get_engine(&E);
+    if (rc) return rc;
+    if (E->device != ix->device) return set_error(KNNS_ERR_INVALID, "index built on device %d", ix->device);
+    std::lock_guard<std::mutex> lk(E->mu);
+    knns_stats st;
+    rc = run_search(*E, ix->pc.corpus, ix->pc.N, ix->pc.ldc, queries, Q, ldq, ix->pc.D, k, dist, idx, nullptr, o,
+                    (cudaStream_t)stream, &st, &ix->pc);
+    if (rc == KNNS_OK) remember_stats(st);
+    return rc;
+}
+
+void knns_index_destroy(knns_index* ix)
+{
+    if (!ix) return;
+    cudaDeviceSynchronize();
+    ix->pc.release();
+    delete ix;
 }
 
 int knns_debug_tc_dot_tile(const float* corpus, int64_t N, const float* queries, int64_t Q, int D, float* dump)

@@ -42,6 +42,9 @@ struct Engine {
     // threshold-scan path: BF16 queries, candidate segments and counts, seeded
     // thresholds, sample norms, failed-query list
     DevBuf qbf, cand, cnt, tq, cnv, fail;
+    // per-search flag words: [0] some corpus tile has a TF32 low part, [1] corpus or
+    // queries not BF16-exact, [2] some value not an integer, [3] max |x| (float bits), [4] zero
+    DevBuf words;
     DevBuf in_corpus, in_queries, out_dist, out_idx;
     // stage timing: kTimingEvents events per timed search (start, after prep,
     // after threshold seeding, after the main fused kernel, after the main
@@ -59,18 +62,43 @@ struct Engine {
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
 };
 
+// A corpus prepared once and kept resident (the serving index): BF16 copy,
+// norms, optional TF32 hi/lo copies with their per-tile low-part flags, and
+// the corpus half of the flag words ([0] low part, [1] not BF16-exact,
+// [2] not integer, [3] max |x| bits).  The caller keeps the FP32 corpus alive
+// and unchanged while the index is used.
+struct PreparedCorpus {
+    const float* corpus = nullptr;
+    int64_t N = 0, ldc = 0;
+    int D = 0, dpb = 0, dp = 0;
+    bool tf32 = false;
+    DevBuf cn, bf, hi, lo, tiles, words;
+    void release();
+};
+
 int set_error(int code, const char* fmt, ...);
 void clear_error();
 int get_engine(Engine** out);
 int auto_kp(int k, int rerank);
 int auto_splits(int64_t qtiles, int64_t tiles, int sms, int max_splits);
 int resolve_config(const Engine& E, int64_t N, int64_t Q, int D, int k, const knns_options& o, Config* c);
+// pc (optional): the corpus arrives prepared (its preparation is skipped).
+// capture: the call is being captured into a CUDA graph: no host-side event
+// ordering against earlier calls (the caller serialises its stream).
 int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const float* queries, int64_t Q, int64_t ldq,
                int D, int k, float* dist, int32_t* idx, float* idx_f, const knns_options& o, cudaStream_t s,
-               knns_stats* st);
+               knns_stats* st, const PreparedCorpus* pc = nullptr, bool capture = false);
+int prepare_corpus(Engine& E, PreparedCorpus* pc, const float* corpus, int64_t N, int64_t ldc, int D, bool tf32,
+                   cudaStream_t s);
 int check_device_error(Engine& E, cudaStream_t s);
 int search_host(const float* corpus, int64_t N, const float* queries, int64_t Q, int D, int k, float* dist,
                 int32_t* idx, float* idx_f_host, const knns_options& o, double* seconds, knns_stats* st);
 void remember_stats(const knns_stats& st);
 
 }  // namespace knn
+
+// the resident index behind the opaque knns_index handle
+struct knns_index {
+    int device = 0;
+    knn::PreparedCorpus pc;
+};

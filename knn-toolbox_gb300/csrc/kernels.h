@@ -167,7 +167,7 @@ cudaError_t launch_select(const uint64_t* part, int splits, int64_t Q, int kp, i
 //    trusted (overflow, total < need, total > kCandMax) is appended to
 //    fail_idx (count in *fail_cnt) and gets no result.
 constexpr int kCandMax = 2048;
-constexpr int kScanMaxSegs = 128;  // candidate segments per query (splits x kScanParts)
+constexpr int kScanMaxSegs = 512;  // candidate segments per query (splits x kScanParts)
 struct CandSelect {
     const uint64_t* cand = nullptr;
     const uint32_t* cnt = nullptr;

@@ -36,6 +36,9 @@ OK, ERR_INVALID, ERR_CUDA, ERR_UNSUPPORTED, ERR_DEVICE_TIMEOUT, ERR_NOMEM = rang
 EXPORTED = ["knns_default_options", "knns_search_device", "knns_search_host", "knns_check_device",
             "knns_last_error", "knns_last_stats", "knns_version", "knns_debug_tc_dot_tile",
             "knns_timing_collect", "knns_timing_collect5", "knns_search_device_noalloc",
+            "knns_index_create", "knns_index_search", "knns_index_destroy",
+            "knns_server_default_config", "knns_server_create", "knns_server_submit", "knns_server_wait",
+            "knns_server_stats", "knns_server_destroy", "knns_server_warmup",
             "gpuknnsBitonic", "gpuknnsHeap", "knnsplan", "knnsexecute"]
 
 
@@ -57,6 +60,11 @@ class Stats(ctypes.Structure):
                 ("stages", ctypes.c_int), ("launches", ctypes.c_int), ("pilot", ctypes.c_int),
                 ("workspace_bytes", ctypes.c_int64), ("scan", ctypes.c_int), ("scan_splits", ctypes.c_int),
                 ("scan_cap", ctypes.c_int), ("scan_ring", ctypes.c_int)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("slots", ctypes.c_int), ("max_batch", ctypes.c_int), ("precision", ctypes.c_int),
+                ("shortlist", ctypes.c_int), ("autotune", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
 
 
 KNNPTR2FUNCTION = ctypes.CFUNCTYPE(ctypes.c_double, *([ctypes.POINTER(ctypes.c_float)] * 4),
@@ -97,6 +105,20 @@ def lib():
     L.knns_timing_collect.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
     L.knns_timing_collect5.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
     L.knns_search_device_noalloc.argtypes = [vp, i64, i64, vp, i64, i64, ci, ci, vp, vp, vp]
+    L.knns_index_create.argtypes = [vp, i64, i64, ci, ci, ctypes.POINTER(vp), vp]
+    L.knns_index_search.argtypes = [vp, vp, i64, i64, ci, vp, vp, ctypes.POINTER(Options), vp]
+    L.knns_index_destroy.argtypes = [vp]
+    L.knns_index_destroy.restype = None
+    L.knns_server_default_config.argtypes = [ctypes.POINTER(ServerConfig)]
+    L.knns_server_default_config.restype = None
+    L.knns_server_create.argtypes = [vp, ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)]
+    L.knns_server_submit.argtypes = [vp, vp, i64, ci]
+    L.knns_server_submit.restype = i64
+    L.knns_server_wait.argtypes = [vp, i64, vp, vp, ctypes.POINTER(ctypes.c_double)]
+    L.knns_server_stats.argtypes = [vp, ctypes.POINTER(i64)]
+    L.knns_server_warmup.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ci, ctypes.POINTER(ctypes.c_int), ci]
+    L.knns_server_destroy.argtypes = [vp]
+    L.knns_server_destroy.restype = None
     L.gpuknnsBitonic.argtypes = [fp, fp, fp, fp, ci, ci, ci, ci, ci]
     L.gpuknnsBitonic.restype = ctypes.c_double
     L.gpuknnsHeap.argtypes = [fp, fp, fp, fp, ci, ci, ci, ci, ci]
@@ -280,3 +302,113 @@ def gpuknnHeap(query, pdata, k, numStreams=1):
 def gpuknns(plan: dict, queries, data):
     """toolbox/gpuknns.m: plan is {'function': gpuknnBitonic|gpuknnHeap, 'k': k, 'streams': s}."""
     return plan["function"](queries, data, plan["k"], plan["streams"])
+
+
+# --------------------------------------------------------------------------
+# resident index and the serving form
+# --------------------------------------------------------------------------
+
+INDEX_TF32 = 1
+
+
+class Index:
+    """A device corpus prepared once (BF16 copy, norms, flags, TF32 copies): searches skip its preparation.
+
+    The torch tensor is kept referenced: the engine reads it on every search.
+    """
+
+    def __init__(self, corpus, tf32=True, stream=None):
+        import torch
+        assert corpus.is_cuda and corpus.dtype == torch.float32 and corpus.stride(1) == 1
+        self.corpus = corpus
+        self.N, self.D = corpus.shape
+        s = torch.cuda.current_stream(corpus.device) if stream is None else stream
+        h = ctypes.c_void_p()
+        _check(lib().knns_index_create(corpus.data_ptr(), self.N, corpus.stride(0), self.D,
+                                       INDEX_TF32 if tf32 else 0, ctypes.byref(h), ctypes.c_void_p(s.cuda_stream)))
+        self.handle = h
+
+    def search(self, queries, k, *, dist=None, idx=None, stream=None, check=True, **opts):
+        import torch
+        assert queries.is_cuda and queries.dtype == torch.float32 and queries.stride(1) == 1
+        Q = queries.shape[0]
+        if dist is None:
+            dist = torch.empty((Q, k), dtype=torch.float32, device=queries.device)
+        if idx is None:
+            idx = torch.empty((Q, k), dtype=torch.int32, device=queries.device)
+        s = torch.cuda.current_stream(queries.device) if stream is None else stream
+        o = options(**opts)
+        _check(lib().knns_index_search(self.handle, queries.data_ptr(), Q, queries.stride(0), k, dist.data_ptr(),
+                                       idx.data_ptr(), ctypes.byref(o), ctypes.c_void_p(s.cuda_stream)))
+        if check:
+            _check(lib().knns_check_device(ctypes.c_void_p(s.cuda_stream)))
+        return dist, idx
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().knns_index_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching request server over an Index (see include/knn_gb300.h).
+
+    submit() takes host queries (numpy, Q x D float32) and returns a request id;
+    wait() blocks until that request is answered and returns (dist, idx, latency_ms).
+    """
+
+    def __init__(self, index, slots=2, max_batch=1024, precision=PREC_EXACT, shortlist=0, autotune=True):
+        cfg = ServerConfig()
+        lib().knns_server_default_config(ctypes.byref(cfg))
+        cfg.slots, cfg.max_batch, cfg.precision, cfg.shortlist = slots, max_batch, precision, shortlist
+        cfg.autotune = int(bool(autotune))
+        h = ctypes.c_void_p()
+        _check(lib().knns_server_create(index.handle, ctypes.byref(cfg), ctypes.byref(h)))
+        self.index = index
+        self.handle = h
+        self.D = index.D
+        self._k = {}
+
+    def submit(self, queries, k):
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        assert q.ndim == 2 and q.shape[1] == self.D
+        rid = lib().knns_server_submit(self.handle, q.ctypes.data, q.shape[0], k)
+        if rid <= 0:
+            raise KnnsError(-rid, last_error())
+        self._k[rid] = (q.shape[0], k)
+        return rid
+
+    def wait(self, rid):
+        Q, k = self._k.pop(rid)
+        dist = np.empty((Q, k), np.float32)
+        idx = np.empty((Q, k), np.int32)
+        lat = ctypes.c_double(0.0)
+        _check(lib().knns_server_wait(self.handle, rid, dist.ctypes.data, idx.ctypes.data, ctypes.byref(lat)))
+        return dist, idx, lat.value
+
+    def warmup(self, buckets, ks):
+        b = (ctypes.c_int * len(buckets))(*buckets)
+        kk = (ctypes.c_int * len(ks))(*ks)
+        _check(lib().knns_server_warmup(self.handle, b, len(buckets), kk, len(ks)))
+
+    def stats(self):
+        out = (ctypes.c_int64 * 4)()
+        _check(lib().knns_server_stats(self.handle, out))
+        return {"requests": out[0], "launches": out[1], "queries": out[2], "graphs": out[3]}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().knns_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

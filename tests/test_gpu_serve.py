@@ -1,0 +1,137 @@
+"""Resident index and serving form (continuous batching, graph-captured launches).
+
+Bars: a search through the index returns exactly what the plain search returns;
+a request answered by the server returns exactly what the same request searched
+alone returns (same k: the per-query computation does not depend on the other
+queries of a launch) -- bit-exact on integer data; for the BF16 form, where the
+fix-up of a rare query could rank near-ties in another kernel, at least 99.9 % of
+the indices agree and every distance is exact for its index.
+"""
+import threading
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def ints(n, q, d, seed, hi=256):
+    rng = np.random.default_rng(seed)
+    return (rng.integers(0, hi, (n, d)).astype(np.float32), rng.integers(0, hi, (q, d)).astype(np.float32))
+
+
+def cuda(x):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+@pytest.mark.parametrize("kind", ["int", "uniform"])
+def test_index_search_matches_plain_search(engine, kind):
+    if kind == "int":
+        X, Qs = ints(150_000, 300, 64, 3)
+    else:
+        import cuknns.synth as S
+        X, Qs = S.uniform(140_000, 96, seed=4, nq=200)
+    c, q = cuda(X), cuda(Qs)
+    ix = engine.Index(c)
+    for k in (1, 16, 100):
+        d0, i0 = engine.search(c, q, k)
+        d1, i1 = ix.search(q, k)
+        np.testing.assert_array_equal(i1.cpu().numpy(), i0.cpu().numpy())
+        np.testing.assert_array_equal(d1.cpu().numpy(), d0.cpu().numpy())
+    ix.close()
+
+
+def test_index_bf16_form_matches_plain_search(engine):
+    import cuknns.synth as S
+    X, Qs = S.gauss_mixture(150_000, 96, seed=5, nq=150, centres=256)
+    c, q = cuda(X), cuda(Qs)
+    ix = engine.Index(c, tf32=False)
+    d0, i0 = engine.search(c, q, 10, precision=engine.PREC_BF16)
+    d1, i1 = ix.search(q, 10, precision=engine.PREC_BF16)
+    np.testing.assert_array_equal(i1.cpu().numpy(), i0.cpu().numpy())
+    np.testing.assert_array_equal(d1.cpu().numpy(), d0.cpu().numpy())
+    with pytest.raises(engine.KnnsError):
+        ix.search(q, 10)  # the exact form needs the TF32 copies for data that are not BF16-exact
+    ix.close()
+
+
+def _requests(rng, n, D, hi=256):
+    out = []
+    for _ in range(n):
+        Q = int(np.exp(rng.uniform(0.0, np.log(300.0))))
+        k = int(rng.choice([1, 10, 100]))
+        out.append((rng.integers(0, hi, (Q, D)).astype(np.float32), k))
+    return out
+
+
+@pytest.mark.parametrize("slots,autotune", [(2, False), (1, True)])
+def test_server_results_equal_alone(engine, slots, autotune):
+    X, _ = ints(200_000, 1, 64, 11)
+    c = cuda(X)
+    ix = engine.Index(c)
+    rng = np.random.default_rng(12)
+    reqs = _requests(rng, 60, 64)
+    srv = engine.Server(ix, slots=slots, max_batch=512, autotune=autotune)
+    results = {}
+    lock = threading.Lock()
+
+    def client(part):
+        ids = [(j, srv.submit(reqs[j][0], reqs[j][1])) for j in part]
+        for j, rid in ids:
+            r = srv.wait(rid)
+            with lock:
+                results[j] = r
+
+    threads = [threading.Thread(target=client, args=(list(range(t, len(reqs), 3)),)) for t in range(3)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    st = srv.stats()
+    srv.close()
+    assert st["requests"] == len(reqs) and 1 <= st["launches"] <= len(reqs) and st["graphs"] >= 1
+    for j, (qs, k) in enumerate(reqs):
+        d, i, lat = results[j]
+        d0, i0 = ix.search(cuda(qs), k)
+        np.testing.assert_array_equal(i, i0.cpu().numpy())
+        np.testing.assert_array_equal(d, d0.cpu().numpy())
+        assert lat > 0.0
+    ix.close()
+
+
+def test_server_bf16_form(engine, oracle):
+    import cuknns.synth as S
+    X, Qs = S.gauss_mixture(150_000, 96, seed=7, nq=400, centres=256)
+    c = cuda(X)
+    ix = engine.Index(c, tf32=False)
+    srv = engine.Server(ix, slots=2, max_batch=256, precision=engine.PREC_BF16, shortlist=4, autotune=False)
+    sizes = [1, 7, 64, 128, 200]
+    starts = np.cumsum([0] + sizes)
+    ids = [srv.submit(Qs[starts[j]:starts[j + 1]], 10) for j in range(len(sizes))]
+    got = [srv.wait(r) for r in ids]
+    srv.close()
+    agree = []
+    for j, (d, i, _) in enumerate(got):
+        qs = Qs[starts[j]:starts[j + 1]]
+        d0, i0 = ix.search(cuda(qs), 10, precision=engine.PREC_BF16)
+        agree.append((i == i0.cpu().numpy()).mean())
+        got64 = oracle.pair_dist_f64(X, qs, i)
+        assert (np.abs(d - got64) <= 1e-5 * got64 + 1e-6).all()
+    assert min(agree) >= 0.999
+    ix.close()
+
+
+def test_server_rejects_bad_requests(engine):
+    X, Qs = ints(20_000, 10, 32, 13)
+    ix = engine.Index(cuda(X))
+    srv = engine.Server(ix, max_batch=64, autotune=False)
+    with pytest.raises(engine.KnnsError):
+        srv.submit(np.zeros((65, 32), np.float32), 4)   # more queries than one launch holds
+    with pytest.raises(engine.KnnsError):
+        srv.submit(Qs, 129)                              # k above the largest shortlist
+    # still serving afterwards
+    d, i, lat = srv.wait(srv.submit(Qs, 4))
+    assert i.shape == (10, 4)
+    srv.close()
+    ix.close()
