@@ -481,7 +481,7 @@ def main():
     ap.add_argument("--scan", default="auto", choices=["auto", "on", "off"],
                     help="threshold-scan path for BF16 keys (auto: corpora of 131,072 rows and more)")
     ap.add_argument("--scan-boxes", type=int, default=0, help="threshold scan: K boxes per ring slot (0 = auto)")
-    ap.add_argument("--rate", type=float, default=5000.0, help="serving: offered requests per second")
+    ap.add_argument("--rate", type=float, default=4000.0, help="serving: offered requests per second")
     ap.add_argument("--requests", type=int, default=4000, help="serving: requests in the timed run")
     ap.add_argument("--recall-queries", type=int, default=0,
                     help="measure recall@k and distance error against the FP64 oracle on this many queries")

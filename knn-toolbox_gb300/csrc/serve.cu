@@ -76,12 +76,16 @@ struct Slot {
     float* h_dist = nullptr;
     int32_t* h_idx = nullptr;
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
+    std::map<std::pair<int, int>, int> tuned;  // split count chosen per (bucket, k)
     std::vector<void*> snapshot;  // workspace pointers the graphs were captured with
     std::vector<std::shared_ptr<Request>> batch;
     std::vector<int64_t> offs;
     int k = 0, bucket = 0;
-    bool busy = false;
+    bool busy = false;      // holds a batch (or is being warmed up)
+    bool launched = false;  // its batch is on the GPU: the slot's completion thread waits for it
+    int status = KNNS_OK;   // launch failure to report
     uint64_t seq = 0;
+    std::thread completer;
 };
 
 std::vector<void*> workspace_pointers(const Engine& E)
@@ -113,8 +117,10 @@ struct knns_server {
 
     int setup();
     void run();
+    void run_completer(Slot* sl);
     int launch(Slot& sl, std::vector<std::shared_ptr<Request>>& take, int k, int64_t total);
     int get_graph(Slot& sl, int bucket, int k, cudaGraphExec_t* out);
+    int tune(Slot& sl, int bucket, int k, int* splits);
     void complete(Slot& sl, int status, const char* err);
     knns_options opts(int splits) const;
     Slot* free_slot();
@@ -161,6 +167,10 @@ int knns_server::setup()
         slots.push_back(std::move(sl));
     }
     worker = std::thread([this] { run(); });
+    for (auto& sl : slots) {
+        Slot* p = sl.get();
+        sl->completer = std::thread([this, p] { run_completer(p); });
+    }
     return KNNS_OK;
 }
 
@@ -179,33 +189,34 @@ Slot* knns_server::oldest_busy()
     return best;
 }
 
-// Capture (once per slot) the search of `bucket` packed queries with this k.
-int knns_server::get_graph(Slot& sl, int bucket, int k, cudaGraphExec_t* out)
+// Choose (once per slot and (bucket, k)) the corpus split count: candidates
+// timed over three runs each on the slot's stream; every candidate is also run
+// once, so the workspace reaches the size that configuration needs.
+int knns_server::tune(Slot& sl, int bucket, int k, int* splits)
 {
     auto key = std::make_pair(bucket, k);
-    auto it = sl.graphs.find(key);
-    if (it != sl.graphs.end()) {
-        *out = it->second;
+    auto it = sl.tuned.find(key);
+    if (it != sl.tuned.end()) {
+        *splits = it->second;
         return KNNS_OK;
     }
     const PreparedCorpus& P = *pc;
-    auto search = [&](int splits, bool capture) {
-        knns_options o = opts(splits);
+    auto search = [&](int sp) {
+        knns_options o = opts(sp);
         return run_search(sl.E, P.corpus, P.N, P.ldc, sl.d_q, bucket, P.D, P.D, k, sl.d_dist, sl.d_idx, nullptr, o,
-                          sl.stream, nullptr, &P, capture);
+                          sl.stream, nullptr, &P, false);
     };
     int best_splits = 0;
     if (cfg.autotune) {
-        // candidate corpus split counts, each timed over three runs on the slot's stream
         cudaEvent_t e0, e1;
         if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
             return set_error(KNNS_ERR_CUDA, "autotune events");
         float best = 1e30f;
-        for (int sp : {0, 4, 8, 16, 32}) {
-            int rc = search(sp, false);  // warm (allocates)
+        for (int sp : {0, 4, 8, 16, 32, 76}) {
+            int rc = search(sp);  // warm (allocates)
             if (rc) continue;
             cudaEventRecord(e0, sl.stream);
-            for (int r = 0; r < 3 && !rc; ++r) rc = search(sp, false);
+            for (int r = 0; r < 3 && !rc; ++r) rc = search(sp);
             cudaEventRecord(e1, sl.stream);
             if (rc || cudaEventSynchronize(e1) != cudaSuccess) continue;
             float ms = 0.f;
@@ -218,11 +229,28 @@ int knns_server::get_graph(Slot& sl, int bucket, int k, cudaGraphExec_t* out)
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
     }
-    // warm run with the chosen options: every workspace buffer reaches its size
-    int rc = search(best_splits, false);
+    int rc = search(best_splits);
     if (rc) return rc;
     KNN_CUDA_RET(cudaStreamSynchronize(sl.stream));
     rc = check_device_error(sl.E, sl.stream);
+    if (rc) return rc;
+    sl.tuned[key] = best_splits;
+    *splits = best_splits;
+    return KNNS_OK;
+}
+
+// Capture (once per slot) the search of `bucket` packed queries with this k.
+int knns_server::get_graph(Slot& sl, int bucket, int k, cudaGraphExec_t* out)
+{
+    auto key = std::make_pair(bucket, k);
+    auto it = sl.graphs.find(key);
+    if (it != sl.graphs.end()) {
+        *out = it->second;
+        return KNNS_OK;
+    }
+    const PreparedCorpus& P = *pc;
+    int splits = 0;
+    int rc = tune(sl, bucket, k, &splits);
     if (rc) return rc;
     // a grown workspace buffer moved: graphs captured before hold stale pointers
     auto ptrs = workspace_pointers(sl.E);
@@ -233,7 +261,9 @@ int knns_server::get_graph(Slot& sl, int bucket, int k, cudaGraphExec_t* out)
     }
     cudaGraph_t g = nullptr;
     KNN_CUDA_RET(cudaStreamBeginCapture(sl.stream, cudaStreamCaptureModeThreadLocal));
-    rc = search(best_splits, true);
+    knns_options o = opts(splits);
+    rc = run_search(sl.E, P.corpus, P.N, P.ldc, sl.d_q, bucket, P.D, P.D, k, sl.d_dist, sl.d_idx, nullptr, o,
+                    sl.stream, nullptr, &P, true);
     cudaError_t ce = cudaStreamEndCapture(sl.stream, &g);
     if (rc) {
         if (g) cudaGraphDestroy(g);
@@ -288,7 +318,7 @@ void knns_server::complete(Slot& sl, int status, const char* err)
                 const int64_t o = sl.offs[i];
                 r.dist.assign(sl.h_dist + o * sl.k, sl.h_dist + (o + r.Q) * sl.k);
                 r.idx.assign(sl.h_idx + o * sl.k, sl.h_idx + (o + r.Q) * sl.k);
-            } else {
+            } else if (r.error.empty()) {
                 r.error = err ? err : "";
             }
             r.status = status;
@@ -302,49 +332,79 @@ void knns_server::complete(Slot& sl, int status, const char* err)
     cv.notify_all();
 }
 
+// Dispatcher: forms a batch whenever requests are pending and a slot is free.
 void knns_server::run()
 {
     cudaSetDevice(device);
     for (;;) {
         std::unique_lock<std::mutex> lk(mu);
-        cv.wait(lk, [&] {
-            return stop || (!pending.empty() && free_slot() != nullptr) || oldest_busy() != nullptr;
-        });
-        if (stop && pending.empty() && oldest_busy() == nullptr) return;
-        Slot* fs = free_slot();
-        if (!pending.empty() && fs) {
-            // admit, oldest first, the pending requests with the oldest request's k that fit one launch
-            const int k = pending.front()->k;
-            std::vector<std::shared_ptr<Request>> take;
-            int64_t total = 0;
-            for (auto it = pending.begin(); it != pending.end();) {
-                if ((*it)->k == k && total + (*it)->Q <= cfg.max_batch) {
-                    total += (*it)->Q;
-                    take.push_back(*it);
-                    it = pending.erase(it);
-                } else {
-                    ++it;
-                }
+        cv.wait(lk, [&] { return stop || (!pending.empty() && free_slot() != nullptr); });
+        if (stop) {
+            // requests never launched are answered with an error
+            for (auto& r : pending) {
+                r->status = KNNS_ERR_INVALID;
+                r->error = "the server stopped before the request was launched";
+                r->done = true;
             }
-            fs->busy = true;
-            fs->seq = next_seq++;
-            ++n_batches;
-            n_queries += total;
+            pending.clear();
             lk.unlock();
-            int rc = launch(*fs, take, k, total);
-            if (rc) {
-                fs->batch = take;
-                complete(*fs, rc, knns_last_error());
-            }
-            continue;
+            done_cv.notify_all();
+            return;
         }
-        Slot* bs = oldest_busy();
+        Slot* fs = free_slot();
+        // admit, oldest first, the pending requests with the oldest request's k that fit one launch
+        const int k = pending.front()->k;
+        std::vector<std::shared_ptr<Request>> take;
+        int64_t total = 0;
+        for (auto it = pending.begin(); it != pending.end();) {
+            if ((*it)->k == k && total + (*it)->Q <= cfg.max_batch) {
+                total += (*it)->Q;
+                take.push_back(*it);
+                it = pending.erase(it);
+            } else {
+                ++it;
+            }
+        }
+        fs->busy = true;
+        fs->seq = next_seq++;
+        ++n_batches;
+        n_queries += total;
         lk.unlock();
-        if (!bs) continue;
-        cudaError_t e = cudaEventSynchronize(bs->done_ev);
-        int rc = e == cudaSuccess ? KNNS_OK : set_error(KNNS_ERR_CUDA, "batch failed: %s", cudaGetErrorString(e));
-        if (rc == KNNS_OK) rc = check_device_error(bs->E, bs->stream);
-        complete(*bs, rc, rc ? knns_last_error() : nullptr);
+        const int rc = launch(*fs, take, k, total);
+        if (rc) {
+            for (auto& r : take) r->error = knns_last_error();
+        }
+        lk.lock();
+        fs->batch = take;
+        fs->status = rc;
+        fs->launched = true;
+        lk.unlock();
+        cv.notify_all();
+    }
+}
+
+// Completion: one thread per slot waits for its batch and answers the requests.
+void knns_server::run_completer(Slot* sl)
+{
+    cudaSetDevice(device);
+    for (;;) {
+        std::unique_lock<std::mutex> lk(mu);
+        cv.wait(lk, [&] { return sl->launched || (stop && !sl->busy); });
+        if (!sl->launched) return;
+        int rc = sl->status;
+        lk.unlock();
+        std::string msg = rc ? knns_last_error() : "";
+        if (rc == KNNS_OK) {
+            cudaError_t e = cudaEventSynchronize(sl->done_ev);
+            rc = e == cudaSuccess ? KNNS_OK : set_error(KNNS_ERR_CUDA, "batch failed: %s", cudaGetErrorString(e));
+            if (rc == KNNS_OK) rc = check_device_error(sl->E, sl->stream);
+            if (rc) msg = knns_last_error();
+        }
+        {
+            std::lock_guard<std::mutex> g(mu);
+            sl->launched = false;
+        }
+        complete(*sl, rc, rc ? msg.c_str() : nullptr);
     }
 }
 
@@ -440,27 +500,39 @@ int knns_server_warmup(knns_server* sv, const int* buckets, int nb, const int* k
     std::vector<Slot*> mine;
     {
         std::unique_lock<std::mutex> lk(sv->mu);
-        sv->cv.wait(lk, [&] { return sv->oldest_busy() == nullptr; });
+        sv->cv.wait(lk, [&] {
+            for (auto& sl : sv->slots)
+                if (sl->busy) return false;
+            return true;
+        });
         for (auto& sl : sv->slots) {
             sl->busy = true;
             sl->seq = ~0ull;  // never "oldest": the worker does not wait on a warming slot
             mine.push_back(sl.get());
         }
     }
+    // two passes: tune (and so size the workspace for) every configuration, then capture
+    // them all -- no capture is invalidated by a later buffer growth
     int rc = KNNS_OK;
-    for (Slot* sl : mine)
-        for (int b = 0; b < nb && !rc; ++b)
-            for (int j = 0; j < nk && !rc; ++j) {
-                int bucket = 32;
-                while (bucket < buckets[b]) bucket *= 2;
-                if (bucket > sv->cfg.max_batch || ks[j] < 1 || ks[j] > kMaxKpTC || ks[j] > sv->pc->N) {
-                    rc = set_error(KNNS_ERR_INVALID, "warm-up bucket %d / k %d outside the server's range", buckets[b],
-                                   ks[j]);
-                    break;
+    for (int pass = 0; pass < 2 && !rc; ++pass)
+        for (Slot* sl : mine)
+            for (int b = 0; b < nb && !rc; ++b)
+                for (int j = 0; j < nk && !rc; ++j) {
+                    int bucket = 32;
+                    while (bucket < buckets[b]) bucket *= 2;
+                    if (bucket > sv->cfg.max_batch || ks[j] < 1 || ks[j] > kMaxKpTC || ks[j] > sv->pc->N) {
+                        rc = set_error(KNNS_ERR_INVALID, "warm-up bucket %d / k %d outside the server's range",
+                                       buckets[b], ks[j]);
+                        break;
+                    }
+                    if (pass == 0) {
+                        int sp;
+                        rc = sv->tune(*sl, bucket, ks[j], &sp);
+                    } else {
+                        cudaGraphExec_t ge;
+                        rc = sv->get_graph(*sl, bucket, ks[j], &ge);
+                    }
                 }
-                cudaGraphExec_t ge;
-                rc = sv->get_graph(*sl, bucket, ks[j], &ge);
-            }
     {
         std::lock_guard<std::mutex> lk(sv->mu);
         for (Slot* sl : mine) sl->busy = false;
@@ -489,6 +561,9 @@ void knns_server_destroy(knns_server* sv)
     }
     sv->cv.notify_all();
     if (sv->worker.joinable()) sv->worker.join();
+    // completion threads finish the batches in flight, then leave
+    for (auto& sl : sv->slots)
+        if (sl->completer.joinable()) sl->completer.join();
     for (auto& sl : sv->slots) {
         if (sl->stream) cudaStreamSynchronize(sl->stream);
         for (auto& g : sl->graphs) cudaGraphExecDestroy(g.second);
