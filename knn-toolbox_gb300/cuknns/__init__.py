@@ -276,6 +276,67 @@ def knnsexecute(plan: KnnPlan, data, queries):
 
 
 # --------------------------------------------------------------------------
+# double-precision library (libknngb300_double.so: the reference's libcuknn_double)
+# --------------------------------------------------------------------------
+
+LIB_F64_PATH = os.path.join(PKG, "_build", "libknngb300_double.so")
+EXPORTED_F64 = ["gpuknnsBitonic", "gpuknnsHeap", "knnsplan", "knnsexecute", "knns_search_device_f64",
+                "knns_search_host_f64", "knns_f64_last_error"]
+_lib64 = None
+
+
+def lib_f64():
+    global _lib64
+    if _lib64 is not None:
+        return _lib64
+    if not os.path.exists(LIB_F64_PATH):
+        raise RuntimeError(f"double-precision library not built: {LIB_F64_PATH}")
+    L = ctypes.CDLL(LIB_F64_PATH)
+    vp, i64, ci = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.knns_search_device_f64.argtypes = [vp, i64, i64, vp, i64, i64, ci, ci, vp, vp, vp]
+    L.knns_search_host_f64.argtypes = [vp, i64, vp, i64, ci, ci, vp, vp]
+    L.knns_f64_last_error.restype = ctypes.c_char_p
+    L.gpuknnsBitonic.argtypes = [dp, dp, dp, dp, ci, ci, ci, ci, ci]
+    L.gpuknnsBitonic.restype = ctypes.c_double
+    L.gpuknnsHeap.argtypes = [dp, dp, dp, dp, ci, ci, ci, ci, ci]
+    L.gpuknnsHeap.restype = ctypes.c_double
+    _lib64 = L
+    return L
+
+
+def search_host_f64(corpus, queries, k):
+    """Exact FP64 kNN on host arrays (N x D, Q x D float64).  Returns numpy (dist f64, idx i32)."""
+    corpus = np.ascontiguousarray(corpus, dtype=np.float64)
+    queries = np.ascontiguousarray(queries, dtype=np.float64)
+    N, D = corpus.shape
+    Q = queries.shape[0]
+    dist = np.empty((Q, k), np.float64)
+    idx = np.empty((Q, k), np.int32)
+    rc = lib_f64().knns_search_host_f64(corpus.ctypes.data, N, queries.ctypes.data, Q, D, k, dist.ctypes.data,
+                                        idx.ctypes.data)
+    if rc != OK:
+        raise KnnsError(rc, lib_f64().knns_f64_last_error().decode())
+    return dist, idx
+
+
+def gpuknnsBitonic_f64(query, data, k, numStreams=1):
+    """The double library's gpuknnsBitonic: query Q x D, data N x D (float64).  Returns (values, indices, s)."""
+    query = np.ascontiguousarray(query, dtype=np.float64)
+    data = np.ascontiguousarray(data, dtype=np.float64)
+    Q, D = query.shape
+    N = data.shape[0]
+    vals = np.empty((Q, k), np.float64)
+    idxs = np.empty((Q, k), np.float64)
+    dp = ctypes.POINTER(ctypes.c_double)
+    t = lib_f64().gpuknnsBitonic(query.ctypes.data_as(dp), data.ctypes.data_as(dp), vals.ctypes.data_as(dp),
+                                 idxs.ctypes.data_as(dp), N, Q, D, k, numStreams)
+    if t >= 1e300:
+        raise KnnsError(-1, lib_f64().knns_f64_last_error().decode())
+    return vals, idxs, t
+
+
+# --------------------------------------------------------------------------
 # MATLAB toolbox semantics (toolbox/gpuknnBitonic.m, gpuknnHeap.m, gpuknns.m)
 # --------------------------------------------------------------------------
 

@@ -309,6 +309,56 @@ int oracle_knn_f64(const float *data, int64_t N, const float *queries, int64_t Q
     return err;
 }
 
+/* The same with FP64 inputs: the double-precision library's oracle. */
+static double dist64d(const double *q, const double *c, int D)
+{
+    double acc = 0.0;
+    for (int d = 0; d < D; ++d) {
+        double t = q[d] - c[d];
+        acc += t * t;
+    }
+    return acc;
+}
+
+int oracle_knn_f64d(const double *data, int64_t N, const double *queries, int64_t Q,
+                    int D, int k, double *dist, int32_t *idx, int nthreads)
+{
+    if (!data || !queries || !dist || !idx) return -1;
+    if (N <= 0 || Q < 0 || D <= 0 || k <= 0 || k > N) return -2;
+    if (N > INT32_MAX) return -3;
+    set_threads(nthreads);
+    int err = 0;
+#pragma omp parallel
+    {
+        double *bk = (double *)malloc(sizeof(double) * (size_t)k);
+        int32_t *bi = (int32_t *)malloc(sizeof(int32_t) * (size_t)k);
+        if (!bk || !bi) {
+#pragma omp atomic write
+            err = -4;
+        }
+#pragma omp for schedule(dynamic, 4)
+        for (int64_t q = 0; q < Q; ++q) {
+            if (err) continue;
+            const double *qv = queries + q * (int64_t)D;
+            int m = 0;
+            for (int64_t n = 0; n < N; ++n) {
+                double v = dist64d(qv, data + n * (int64_t)D, D);
+                int32_t id = (int32_t)n;
+                if (m == k && !(v < bk[k - 1])) continue;  /* later index loses ties */
+                int b;
+                if (m < k) { b = m - 1; ++m; } else { b = k - 2; }
+                while (b >= 0 && (v < bk[b] || (v == bk[b] && id < bi[b]))) {
+                    bk[b + 1] = bk[b]; bi[b + 1] = bi[b]; --b;
+                }
+                bk[b + 1] = v; bi[b + 1] = id;
+            }
+            for (int s = 0; s < k; ++s) { dist[q * k + s] = bk[s]; idx[q * k + s] = bi[s]; }
+        }
+        free(bk); free(bi);
+    }
+    return err;
+}
+
 /* FP64 distances of given (query, corpus index) pairs: out[q*m + j] = d(q, idx[q*m+j]). */
 int oracle_pair_dist_f64(const float *data, int64_t N, const float *queries, int64_t Q,
                          int D, const int32_t *idx, int m, double *out)

@@ -61,6 +61,9 @@ def lib():
                                       ctypes.c_int]
         L.oracle_knn_f64.argtypes = [c_fp, ctypes.c_int64, c_fp, ctypes.c_int64, ctypes.c_int,
                                      ctypes.c_int, c_dp, c_ip, ctypes.c_int]
+        L.oracle_knn_f64d.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int64, ctypes.POINTER(ctypes.c_double),
+                                      ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(ctypes.c_int32), ctypes.c_int]
         L.oracle_pair_dist_f64.argtypes = [c_fp, ctypes.c_int64, c_fp, ctypes.c_int64,
                                            ctypes.c_int, c_ip, ctypes.c_int, c_dp]
         L.oracle_merge_replace_max.argtypes = [c_fp, c_fp, ctypes.c_int, ctypes.c_int,
@@ -128,6 +131,20 @@ def knn_f64(data, queries, k, nthreads=0):
     rc = lib().oracle_knn_f64(_f(data), N, _f(queries), Q, D, k, _d(dist), _i(idx), nthreads)
     if rc != 0:
         raise ValueError(f"oracle_knn_f64 failed ({rc})")
+    return dist, idx
+
+
+def knn_f64d(data, queries, k, nthreads=0):
+    """Exact top-k by (FP64 direct-difference distance, index) of FP64 inputs."""
+    data = np.ascontiguousarray(data, dtype=np.float64)
+    queries = np.ascontiguousarray(queries, dtype=np.float64)
+    N, D = data.shape
+    Q = queries.shape[0]
+    dist = np.empty((Q, k), np.float64)
+    idx = np.empty((Q, k), np.int32)
+    rc = lib().oracle_knn_f64d(_d(data), N, _d(queries), Q, D, k, _d(dist), _i(idx), nthreads)
+    if rc != 0:
+        raise ValueError(f"oracle_knn_f64d failed ({rc})")
     return dist, idx
 
 
