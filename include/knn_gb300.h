@@ -169,6 +169,17 @@ int knns_index_search(knns_index *index, const float *queries, int64_t Q, int64_
 void knns_index_destroy(knns_index *index);
 
 /*
+ * Shortlist autotuner of the BF16 precision form: searches the given device
+ * queries (a sample of the workload) with the exact form and with BF16 keys at
+ * shortlist factors c = 2, 4, 8 (while c*k <= 128), and returns in *c_out the
+ * smallest c whose recall@k against the exact form reaches `target` (else the
+ * largest tried), its recall in *recall_out.  Synchronises `stream`; needs an
+ * index with TF32 copies unless the data are BF16-exact.
+ */
+int knns_autotune_shortlist(knns_index *index, const float *queries, int64_t Q, int64_t ldq, int k, double target,
+                            int *c_out, double *recall_out, void *stream);
+
+/*
  * Serving form (no counterpart in the reference): a request server over a
  * resident index.  Requests of uneven size (1..max_batch queries, host memory,
  * copied at submit) and k (1..128) arrive at any time from any thread; one worker

@@ -1095,6 +1095,76 @@ int knns_index_search(knns_index* ix, const float* queries, int64_t Q, int64_t l
     return rc;
 }
 
+int knns_autotune_shortlist(knns_index* ix, const float* queries, int64_t Q, int64_t ldq, int k, double target,
+                            int* c_out, double* recall_out, void* stream)
+{
+    clear_error();
+    if (!ix || !queries || Q <= 0 || k <= 0 || !c_out) return set_error(KNNS_ERR_INVALID, "bad arguments");
+    Engine* E = nullptr;
+    int rc = get_engine(&E);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(E->mu);
+    cudaStream_t s = (cudaStream_t)stream;
+    const PreparedCorpus& P = ix->pc;
+    const size_t n = (size_t)Q * k;
+    float* d_dist = nullptr;
+    int32_t* d_idx = nullptr;
+    KNN_CUDA(cudaMalloc(&d_dist, n * 4));
+    if (cudaMalloc(&d_idx, n * 4 * 4) != cudaSuccess) {
+        cudaFree(d_dist);
+        return set_error(KNNS_ERR_NOMEM, "autotune buffers");
+    }
+    std::vector<int32_t> exact(n), got(n);
+    auto run = [&](int precision, int c, std::vector<int32_t>& out) -> int {
+        knns_options o;
+        knns_default_options(&o);
+        o.precision = precision;
+        o.shortlist = c;
+        int r = run_search(*E, P.corpus, P.N, P.ldc, queries, Q, ldq, P.D, k, d_dist, d_idx, nullptr, o, s, nullptr,
+                           &P);
+        if (r) return r;
+        r = check_device_error(*E, s);
+        if (r) return r;
+        if (cudaMemcpy(out.data(), d_idx, n * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return set_error(KNNS_ERR_CUDA, "autotune copy");
+        return KNNS_OK;
+    };
+    // ground truth: the exact form (needs the index's TF32 copies unless the data are BF16-exact)
+    rc = run(KNNS_PREC_EXACT, 0, exact);
+    int best = 0;
+    double best_recall = 0.0, last_recall = 0.0;
+    int last_c = 0;
+    for (int c : {2, 4, 8}) {
+        if (rc) break;
+        if ((int64_t)c * k > kMaxKpTC && c != 2) break;  // the shortlist holds at most kMaxKpTC entries
+        rc = run(KNNS_PREC_BF16, c, got);
+        if (rc) break;
+        int64_t hit = 0;
+        for (int64_t q = 0; q < Q; ++q) {
+            std::vector<int32_t> a(exact.begin() + q * k, exact.begin() + (q + 1) * k);
+            std::sort(a.begin(), a.end());
+            for (int j = 0; j < k; ++j) hit += std::binary_search(a.begin(), a.end(), got[q * k + j]) ? 1 : 0;
+        }
+        last_recall = (double)hit / (double)n;
+        last_c = c;
+        if (last_recall >= target) {
+            best = c;
+            best_recall = last_recall;
+            break;
+        }
+    }
+    cudaFree(d_dist);
+    cudaFree(d_idx);
+    if (rc) return rc;
+    if (!best) {  // no factor reached the target: the largest one tried
+        best = last_c;
+        best_recall = last_recall;
+    }
+    *c_out = best;
+    if (recall_out) *recall_out = best_recall;
+    return KNNS_OK;
+}
+
 void knns_index_destroy(knns_index* ix)
 {
     if (!ix) return;

@@ -36,7 +36,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_UNSUPPORTED, ERR_DEVICE_TIMEOUT, ERR_NOMEM = rang
 EXPORTED = ["knns_default_options", "knns_search_device", "knns_search_host", "knns_check_device",
             "knns_last_error", "knns_last_stats", "knns_version", "knns_debug_tc_dot_tile",
             "knns_timing_collect", "knns_timing_collect5", "knns_search_device_noalloc",
-            "knns_index_create", "knns_index_search", "knns_index_destroy",
+            "knns_index_create", "knns_index_search", "knns_index_destroy", "knns_autotune_shortlist",
             "knns_server_default_config", "knns_server_create", "knns_server_submit", "knns_server_wait",
             "knns_server_stats", "knns_server_destroy", "knns_server_warmup",
             "gpuknnsBitonic", "gpuknnsHeap", "knnsplan", "knnsexecute"]
@@ -107,6 +107,8 @@ def lib():
     L.knns_search_device_noalloc.argtypes = [vp, i64, i64, vp, i64, i64, ci, ci, vp, vp, vp]
     L.knns_index_create.argtypes = [vp, i64, i64, ci, ci, ctypes.POINTER(vp), vp]
     L.knns_index_search.argtypes = [vp, vp, i64, i64, ci, vp, vp, ctypes.POINTER(Options), vp]
+    L.knns_autotune_shortlist.argtypes = [vp, vp, i64, i64, ci, ctypes.c_double, ctypes.POINTER(ctypes.c_int),
+                                          ctypes.POINTER(ctypes.c_double), vp]
     L.knns_index_destroy.argtypes = [vp]
     L.knns_index_destroy.restype = None
     L.knns_server_default_config.argtypes = [ctypes.POINTER(ServerConfig)]
@@ -404,6 +406,17 @@ class Index:
         if check:
             _check(lib().knns_check_device(ctypes.c_void_p(s.cuda_stream)))
         return dist, idx
+
+    def autotune_shortlist(self, queries, k, target=0.999, stream=None):
+        """Smallest BF16 shortlist factor c in {2, 4, 8} reaching recall@k >= target on these queries."""
+        import torch
+        s = torch.cuda.current_stream(queries.device) if stream is None else stream
+        c = ctypes.c_int(0)
+        r = ctypes.c_double(0.0)
+        _check(lib().knns_autotune_shortlist(self.handle, queries.data_ptr(), queries.shape[0], queries.stride(0), k,
+                                             target, ctypes.byref(c), ctypes.byref(r),
+                                             ctypes.c_void_p(s.cuda_stream)))
+        return c.value, r.value
 
     def close(self):
         if getattr(self, "handle", None):

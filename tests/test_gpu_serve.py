@@ -135,3 +135,20 @@ def test_server_rejects_bad_requests(engine):
     assert i.shape == (10, 4)
     srv.close()
     ix.close()
+
+
+def test_shortlist_autotuner(engine):
+    import cuknns.synth as S
+    X, Qs = S.gauss_mixture(150_000, 96, seed=9, nq=200, centres=256)
+    ix = engine.Index(cuda(X))
+    q = cuda(Qs)
+    c, rec = ix.autotune_shortlist(q, 10, target=0.999)
+    assert c in (2, 4, 8) and 0.0 <= rec <= 1.0
+    if rec >= 0.999 and c > 2:
+        # the next smaller factor misses the target (that is why it was not chosen)
+        _, i_ex = ix.search(q, 10)
+        _, i_lo = ix.search(q, 10, precision=engine.PREC_BF16, shortlist=c // 2)
+        ex, lo = i_ex.cpu().numpy(), i_lo.cpu().numpy()
+        hit = sum(len(set(ex[r]) & set(lo[r])) for r in range(len(ex)))
+        assert hit / ex.size < 0.999
+    ix.close()
