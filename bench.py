@@ -43,6 +43,10 @@ WORKLOADS = {
     "serve2m": dict(desc="serving: int-descriptor corpus 2,000,000 x 128 resident (FP32 + BF16 + TF32 copies), "
                          "Poisson arrivals, request sizes log-uniform on [1,512], k in {1,10,100}, seed 1",
                     gen="int_descriptor", N=2_000_000, D=128, Q=0, k=0, seed=1, serve=True),
+    # precision form with E4M3 keys: anisotropic Gaussian N(0, diag(1/sqrt(1+j)))
+    "aniso8m": dict(desc="anisotropic Gaussian corpus 8,000,000 x 256 (coordinate j ~ N(0, 1/sqrt(1+j))), "
+                         "16,384 queries, k=32, seed 3",
+                    gen="anisotropic", N=8_000_000, D=256, Q=16_384, k=32, seed=3),
     # profiling cut of int1m: full corpus (same candidate density per corpus row), a quarter of the queries
     "int1m_q2500": dict(desc="int-descriptor corpus 1,000,000 x 128, 2,500 queries, k=100, seed 1",
                         gen="int_descriptor", N=1_000_000, D=128, Q=2_500, k=100, seed=1),
@@ -210,24 +214,36 @@ def run_reference(args, w):
     return 0
 
 
-def run_e2e(corpus_np, queries_np, k, Q, world, steps, barrier, dist, dev):
-    """Same metric through the reference-facing C ABI with host buffers (copies timed)."""
+def run_e2e(corpus_np, queries_np, k, Q, world, steps, barrier, dist, dev, prec_opts=None):
+    """Same metric through the reference-facing C ABI with host buffers (copies timed).
+
+    The plain form goes through the drop-in gpuknnsBitonic; the precision forms,
+    which the reference API cannot select, through knns_search_host.
+    """
     import torch
     import cuknns
     hc = torch.from_numpy(corpus_np).pin_memory().numpy()
     hq = torch.from_numpy(queries_np).pin_memory().numpy()
-    cuknns.gpuknnsBitonic(hq, hc, k, 1)  # warm (staging buffers)
+    if prec_opts:
+        def call():
+            return cuknns.search_host(hc, hq, k, **prec_opts)
+        api = "knns_search_host (include/knn_gb300.h)"
+    else:
+        def call():
+            return cuknns.gpuknnsBitonic(hq, hc, k, 1)[:2]
+        api = "gpuknnsBitonic (include/cuknns.h)"
+    call()  # warm (staging buffers)
     barrier()
     t0 = time.perf_counter()
     for _ in range(steps):
-        vals, idxf, secs = cuknns.gpuknnsBitonic(hq, hc, k, 1)
+        vals, idxf = call()
     e2e_s = (time.perf_counter() - t0) / steps
     if dist is not None:
         t = torch.tensor([e2e_s], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     return {"value": Q * world / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": int(hc.nbytes + hq.nbytes),
-            "d2h_bytes_per_step": int(vals.nbytes + idxf.nbytes), "api": "gpuknnsBitonic (include/cuknns.h)",
+            "d2h_bytes_per_step": int(vals.nbytes + idxf.nbytes), "api": api,
             "host_buffers": "pinned inputs, pageable outputs", "steps": steps}
 
 
@@ -253,15 +269,16 @@ def run_gb300(args, w):
     idx_out = torch.empty((Q, k), dtype=torch.int32, device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    prec = cuknns.PREC_BF16 if args.precision == "bf16" else cuknns.PREC_EXACT
+    prec = {"exact": cuknns.PREC_EXACT, "bf16": cuknns.PREC_BF16, "fp8": cuknns.PREC_FP8}[args.precision]
     tuned = None
-    if prec == cuknns.PREC_BF16 and args.shortlist == 0:
+    if prec != cuknns.PREC_EXACT and args.shortlist == 0:
         # shortlist factor c from the autotuner: recall@k against the exact form on a 256-query sample
         t0 = time.perf_counter()
-        ix = cuknns.Index(c)
+        ix = cuknns.Index(c, fp8=prec == cuknns.PREC_FP8)
         sample = q[:256].contiguous()
-        cf, rec = ix.autotune_shortlist(sample, k, target=0.999)
+        cf, rec = ix.autotune_shortlist(sample, k, target=0.999, precision=prec)
         ix.close()
+        torch.cuda.empty_cache()
         args.shortlist = cf
         tuned = {"shortlist_c": cf, "sample_recall": rec, "sample_queries": 256, "target": 0.999,
                  "seconds": time.perf_counter() - t0}
@@ -305,7 +322,7 @@ def run_gb300(args, w):
 
     # ---- accuracy against the FP64 oracle on a query sample
     accuracy = None
-    nrq = args.recall_queries if args.recall_queries else (100 if args.precision == "bf16" else 0)
+    nrq = args.recall_queries if args.recall_queries else (100 if args.precision != "exact" else 0)
     if nrq and rank == 0:
         import oracle
         oracle.build()
@@ -320,30 +337,40 @@ def run_gb300(args, w):
 
     # ---- end to end through the drop-in C ABI from pinned host buffers
     e2e = None
-    e2e_steps = 0 if (args.no_e2e or args.precision != "exact") else max(1, min(args.steps, 20))
+    e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 20))
     if e2e_steps:
-        e2e = run_e2e(corpus_np, queries_np, k, Q, world, e2e_steps, barrier, dist, dev)
+        popts = None if prec == cuknns.PREC_EXACT else {"precision": prec, "shortlist": args.shortlist}
+        e2e = run_e2e(corpus_np, queries_np, k, Q, world, e2e_steps, barrier, dist, dev, popts)
 
     # ---- roofline of the dominant kernel (the main fused distance pass)
     peaks, peak_kind = measured_peaks()
     bf16_exact = bool(((corpus_np.view(np.uint32) & 0xFFFF) == 0).all() and
                       ((queries_np.view(np.uint32) & 0xFFFF) == 0).all())
-    on_scan = bool(st["scan"]) and (args.precision == "bf16" or bf16_exact)
+    on_scan = bool(st["scan"]) and (args.precision != "exact" or bf16_exact)
     kern = "scan_kernel" if on_scan else ("tc_kernel" if st["algo"] == cuknns.ALGO_TC else "simt_kernel")
     # shortlist kernels: the fused stage includes their pilot pass
     fused_avg_ms = (fused_ms if on_scan else seed_ms + fused_ms) / max(1, nt)
     if on_scan:
-        # the main pass alone is timed (seeding passes are their own stage); one BF16 product per pair
+        # the main pass alone is timed (seeding passes are their own stage); one product per pair
         flops = 2.0 * N * Q * D
-        roof = {"bound": "tensor", "achieved": flops / (fused_avg_ms / 1e3) / 1e12, "peak": peaks["bf16_tflops"],
-                "unit": "TFLOP/s", "peak_source": f"{peak_kind} bf16 dense burst",
-                "mma_kind": "bf16 (kind::f16, M128 N256)", "products_per_useful_product": 1.0,
-                "flops_per_launch": flops, "padded_k": int(-(-D // 64) * 64)}
+        if args.precision == "fp8":
+            row_bytes = -(-D // 128) * 128
+            peak, peak_src = 2.0 * peaks["bf16_tflops"], (f"2 x {peak_kind} bf16 dense burst (nominal FP8:BF16 "
+                                                          "dense rate 2:1; no measured FP8 peak)")
+            mma = f"e4m3 (kind::f8f6f4, M128 N{224 if row_bytes <= 256 else 192})"
+            padded_k = row_bytes
+        else:
+            padded_k = -(-D // 64) * 64
+            peak, peak_src = peaks["bf16_tflops"], f"{peak_kind} bf16 dense burst"
+            mma = f"bf16 (kind::f16, M128 N{224 if padded_k <= 128 else 192})"
+        roof = {"bound": "tensor", "achieved": flops / (fused_avg_ms / 1e3) / 1e12, "peak": peak,
+                "unit": "TFLOP/s", "peak_source": peak_src, "mma_kind": mma, "products_per_useful_product": 1.0,
+                "flops_per_launch": flops, "padded_k": int(padded_k)}
     elif st["algo"] == cuknns.ALGO_TC:
         # executed tensor work of the fused stage (main pass + the 1/16-sample pilot pass)
         pilot_f = 1.0 + (1.0 / 16.0 if st["pilot"] else 0.0)
-        if args.precision == "bf16" or bf16_exact:
-            kind, products, peak = ("bf16 shortlist" if args.precision == "bf16" else "bf16 (data BF16-exact)",
+        if args.precision != "exact" or bf16_exact:
+            kind, products, peak = ("bf16 shortlist" if args.precision != "exact" else "bf16 (data BF16-exact)",
                                     1.0, peaks["bf16_tflops"])
             peak_src = f"{peak_kind} bf16 dense burst"
         else:
@@ -375,10 +402,12 @@ def run_gb300(args, w):
     cpu = cpu_baseline(corpus_np, queries_np, k) if world == 1 and not args.no_cpu_baseline else None
     line = {"metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": el_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": {"exact": "f32", "bf16": "bf16 keys, f32 re-rank", "fp8": "e4m3 keys, f32 re-rank"}[args.precision],
+            "data": "synthetic",
             "config": {"workload": w["desc"], "N": N, "Q": Q, "D": D, "k": k,
                        "parallelism": f"replicas x{world} (queries sharded, corpus replicated)",
-                       "l2": "inputs larger than L2 (512 MB corpus + 1 GB TF32 hi/lo copies)" if N * D * 4 > 129e6
+                       "l2": f"inputs larger than L2 ({N * D * 4 / 1e6:.0f} MB FP32 corpus)" if N * D * 4 > 129e6
                        else "working set within L2 (65,536 x 128 corpus)",
                        "algo": {1: "tcgen05", 2: "CUDA-core FP32"}[st["algo"]], "precision": args.precision,
                        "pilot": st["pilot"], "splits": st["scan_splits"] if on_scan else st["splits"],
@@ -488,9 +517,11 @@ def main():
     ap.add_argument("--workload", default="int1m", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
-    ap.add_argument("--precision", default="exact", choices=["exact", "bf16"],
-                    help="exact: FP32-accurate keys (plain form); bf16: BF16 shortlist + exact re-rank")
-    ap.add_argument("--shortlist", type=int, default=0, help="bf16: shortlist factor c (0 = chosen by the autotuner)")
+    ap.add_argument("--precision", default="exact", choices=["exact", "bf16", "fp8"],
+                    help="exact: FP32-accurate keys (plain form); bf16 / fp8: BF16 or E4M3 (per-row scales) "
+                         "shortlist + exact re-rank")
+    ap.add_argument("--shortlist", type=int, default=0,
+                    help="bf16 / fp8: shortlist factor c (0 = chosen by the autotuner)")
     ap.add_argument("--scan", default="auto", choices=["auto", "on", "off"],
                     help="threshold-scan path for BF16 keys (auto: corpora of 131,072 rows and more)")
     ap.add_argument("--scan-boxes", type=int, default=0, help="threshold scan: K boxes per ring slot (0 = auto)")

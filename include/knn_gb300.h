@@ -40,6 +40,10 @@ extern "C" {
 #define KNNS_PREC_EXACT 0 /* FP32-accurate keys (BF16 products when the data are BF16-exact, else 3xTF32) */
 #define KNNS_PREC_BF16 1  /* BF16 keys pick a shortlist of c*k per query, re-ranked by exact distance
                              (tensor cores, D <= 256, c*k <= 128) */
+#define KNNS_PREC_FP8 2   /* FP8 E4M3 keys (per-row absmax scales, FP32 accumulation) pick the shortlist
+                             on the threshold scan, re-ranked by exact distance; same limits as BF16.
+                             Where the scan does not run (N below its threshold, KNNS_SCAN_OFF) and
+                             for the rare queries the scan hands to its fix-up, BF16 keys are used */
 
 /* threshold scan: for large corpora the BF16 tensor-core pass keeps no shortlist
    on chip; per-query thresholds seeded from two corpus samples let it collect
@@ -57,8 +61,8 @@ typedef struct knns_options {
     int timing;      /* 1: record CUDA events around each stage (see knns_timing_collect) */
     int pilot;       /* 1 (default): seed per-query thresholds from a pass over a 1/16 corpus sample
                         (large corpora only); results are identical either way */
-    int precision;   /* KNNS_PREC_EXACT (default) or KNNS_PREC_BF16 */
-    int shortlist;   /* KNNS_PREC_BF16: shortlist factor c, kp = c*k rounded up to 16 (0 = 4) */
+    int precision;   /* KNNS_PREC_EXACT (default), KNNS_PREC_BF16 or KNNS_PREC_FP8 */
+    int shortlist;   /* BF16 / FP8 forms: shortlist factor c, kp = c*k rounded up to 16 (0 = 4) */
     int scan;        /* KNNS_SCAN_* (default AUTO) */
     int scan_boxes;  /* threshold scan: 64-element K boxes per shared-memory ring slot (0 = automatic) */
     int reserved[4];
@@ -161,6 +165,7 @@ int knns_search_device_noalloc(const float *corpus, int64_t N, int64_t ldc, cons
  * searches on it skip the corpus preparation.  D <= 256.
  */
 #define KNNS_INDEX_TF32 1
+#define KNNS_INDEX_FP8 2 /* also prepare E4M3 codes and row scales (the KNNS_PREC_FP8 form) */
 typedef struct knns_index knns_index;
 int knns_index_create(const float *corpus, int64_t N, int64_t ldc, int D, int flags, knns_index **out,
                       void *stream);
@@ -169,15 +174,16 @@ int knns_index_search(knns_index *index, const float *queries, int64_t Q, int64_
 void knns_index_destroy(knns_index *index);
 
 /*
- * Shortlist autotuner of the BF16 precision form: searches the given device
- * queries (a sample of the workload) with the exact form and with BF16 keys at
+ * Shortlist autotuner of the precision forms (precision KNNS_PREC_BF16 or
+ * KNNS_PREC_FP8): searches the given device queries (a sample of the
+ * workload) with the exact form and with the form's keys at
  * shortlist factors c = 2, 4, 8 (while c*k <= 128), and returns in *c_out the
  * smallest c whose recall@k against the exact form reaches `target` (else the
  * largest tried), its recall in *recall_out.  Synchronises `stream`; needs an
  * index with TF32 copies unless the data are BF16-exact.
  */
-int knns_autotune_shortlist(knns_index *index, const float *queries, int64_t Q, int64_t ldq, int k, double target,
-                            int *c_out, double *recall_out, void *stream);
+int knns_autotune_shortlist(knns_index *index, const float *queries, int64_t Q, int64_t ldq, int k, int precision,
+                            double target, int *c_out, double *recall_out, void *stream);
 
 /*
  * Serving form (no counterpart in the reference): a request server over a
@@ -197,7 +203,7 @@ typedef struct knns_server_config {
     int slots;     /* launches in flight (default 2) */
     int max_batch; /* queries per launch, a power of two (default 1024) */
     int precision; /* KNNS_PREC_* (default exact) */
-    int shortlist; /* KNNS_PREC_BF16: shortlist factor c (0 = 4) */
+    int shortlist; /* BF16 / FP8 forms: shortlist factor c (0 = 4) */
     int autotune;  /* 1 (default): time candidate split counts before capturing a graph */
     int reserved[3];
 } knns_server_config;

@@ -202,17 +202,22 @@ int resolve_config(const Engine& E, int64_t N, int64_t Q, int D, int k, const kn
     c->rerank = o.rerank ? 1 : 0;
     c->pilot = o.pilot != 0;
     c->precision = o.precision;
-    if (o.precision == KNNS_PREC_BF16) {
-        // BF16 keys rank a shortlist of c*k; the exact re-rank picks the k
-        if (!o.rerank) return set_error(KNNS_ERR_INVALID, "BF16 precision needs the exact re-rank");
-        if (E.cc < 100) return set_error(KNNS_ERR_UNSUPPORTED, "BF16 precision needs sm_100+");
-        if (o.algo == KNNS_ALGO_SIMT) return set_error(KNNS_ERR_UNSUPPORTED, "BF16 precision runs on tensor cores");
+    if (o.precision == KNNS_PREC_BF16 || o.precision == KNNS_PREC_FP8) {
+        // BF16 (or E4M3) keys rank a shortlist of c*k; the exact re-rank picks the k.
+        // E4M3 keys run on the threshold scan; the fix-up of its rare failed queries
+        // (and corpora too small for the scan) use BF16 keys.
+        const char* name = o.precision == KNNS_PREC_FP8 ? "FP8" : "BF16";
+        if (!o.rerank) return set_error(KNNS_ERR_INVALID, "%s precision needs the exact re-rank", name);
+        if (E.cc < 100) return set_error(KNNS_ERR_UNSUPPORTED, "%s precision needs sm_100+", name);
+        if (o.algo == KNNS_ALGO_SIMT) return set_error(KNNS_ERR_UNSUPPORTED, "%s precision runs on tensor cores", name);
         const int dpb = (D + 63) & ~63;
-        if (dpb / 2 > kMaxDpTC) return set_error(KNNS_ERR_UNSUPPORTED, "BF16 precision needs D <= %d", 2 * kMaxDpTC);
+        if (dpb / 2 > kMaxDpTC) return set_error(KNNS_ERR_UNSUPPORTED, "%s precision needs D <= %d", name, 2 * kMaxDpTC);
+        c->fp8 = o.precision == KNNS_PREC_FP8;
+        c->dpf = c->fp8 ? ((D + 127) & ~127) / 2 : 0;
         const int cf = o.shortlist > 0 ? o.shortlist : 4;
         c->kp = o.kp > 0 ? o.kp : std::max(32, round16(k * cf));
         if (c->kp % 16 != 0 || c->kp < k || c->kp > kMaxKpTC)
-            return set_error(KNNS_ERR_UNSUPPORTED, "BF16 shortlist of %d entries (k=%d) outside [k, %d]", c->kp, k,
+            return set_error(KNNS_ERR_UNSUPPORTED, "%s shortlist of %d entries (k=%d) outside [k, %d]", name, c->kp, k,
                              kMaxKpTC);
         c->algo = KNNS_ALGO_TC;
         c->dp = kChunkK;  // TF32 operands unused
@@ -308,9 +313,10 @@ static int seg_cap(double per_seg, double sigmas)
 
 static int seed_rank(double m) { return (int)std::ceil(2.0 * m + 4.0 * std::sqrt(m)) + 1; }
 
-static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, const knns_options& o, ScanPlan* P)
+static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, const knns_options& o, ScanPlan* P,
+                     bool fp8)
 {
-    if (scan_plan(dpb, o.scan_boxes, &P->bps, &P->ring) != 0)
+    if (scan_plan(dpb, o.scan_boxes, &P->bps, &P->ring, fp8) != 0)
         return set_error(KNNS_ERR_UNSUPPORTED, "threshold scan: no ring geometry for %d BF16 columns with %d boxes per slot",
                          dpb, o.scan_boxes);
     const int64_t qt = cdiv(cdiv(Q, kTileQ), 2) * 2;  // query tiles, padded to whole CTA pairs
@@ -407,7 +413,8 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         if (st) *st = knns_stats{c.algo, c.splits, c.kp, c.stages, 0, 0, 0, 0, 0, 0, 0};
         return KNNS_OK;
     }
-    const bool bf16_only = c.precision == KNNS_PREC_BF16;
+    // the precision forms: BF16 / E4M3 keys only, always re-ranked
+    const bool bf16_only = c.precision == KNNS_PREC_BF16 || c.precision == KNNS_PREC_FP8;
 
     // The threshold scan serves BF16 keys on large corpora: always in the BF16
     // precision form, and in the exact form when the data turn out BF16-exact
@@ -417,15 +424,20 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     if (c.algo == KNNS_ALGO_TC && o.scan != KNNS_SCAN_OFF && E.cc >= 100 && c.dpb <= 256 && c.rerank) {
         const int64_t min_n = o.scan == KNNS_SCAN_ON ? 16384 : 131072;
         if (N >= min_n) {
-            rc = plan_scan(E, N, Q, c.dpb, c.kp, o, &sp);
+            rc = plan_scan(E, N, Q, c.fp8 ? c.dpf : c.dpb, c.kp, o, &sp, c.fp8);
             if (rc) return rc;
             scan = true;
         }
     }
+    // E4M3 keys exist only on the scan: without it the form falls back to BF16 keys
+    const bool f8 = scan && c.fp8;
     const bool run_old = !(scan && bf16_only);  // the shortlist path is needed (possibly gated)
     if (pc != nullptr) {
-        if (pc->corpus != corpus || pc->N != N || pc->ldc != ldc || pc->D != D || pc->dpb != c.dpb)
+        // (the CUDA-core kernel uses the index's norms only)
+        if (pc->corpus != corpus || pc->N != N || pc->ldc != ldc || pc->D != D ||
+            (c.algo == KNNS_ALGO_TC && pc->dpb != c.dpb))
             return set_error(KNNS_ERR_INVALID, "prepared corpus does not match the search's corpus");
+        if (f8 && !pc->fp8) return set_error(KNNS_ERR_INVALID, "the FP8 form needs an index prepared with E4M3 copies");
         if (c.algo == KNNS_ALGO_TC && !bf16_only && !pc->tf32)
             return set_error(KNNS_ERR_INVALID, "the exact form needs an index prepared with TF32 copies");
         if (c.algo == KNNS_ALGO_TC && !bf16_only && pc->dp != c.dp)
@@ -495,13 +507,29 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         rc = E.loflags.ensure(((size_t)cdiv(N, 128) + 4) * sizeof(uint32_t));
         if (rc) return rc;
         ws += E.hi.cap + E.lo.cap + E.bf.cap + E.loflags.cap;
+        if (f8) {
+            rc = E.f8.ensure((size_t)N * c.dpf * 2);
+            if (!rc) rc = E.cs.ensure(n_pad * sizeof(float));
+            if (rc) return rc;
+            ws += E.f8.cap + E.cs.cap;
+        }
+    }
+    if (f8) {
+        rc = E.qs.ensure(Q * sizeof(float));
+        if (!rc) rc = E.csv.ensure(sp.norm_words * sizeof(float));
+        if (rc) return rc;
+        ws += E.qs.cap + E.csv.cap;
     }
     // corpus-side buffers: the index's, or this engine's
     const void* bf_p = pc ? pc->bf.p : E.bf.p;
     const float* hi_p = (const float*)(pc ? pc->hi.p : E.hi.p);
     const float* lo_p = (const float*)(pc ? pc->lo.p : E.lo.p);
+    const void* f8_p = pc ? pc->f8.p : E.f8.p;
+    const float* cs_p = (const float*)(pc ? pc->cs.p : E.cs.p);
+    // the scan's operand row width in 16-bit units
+    const int sdp = f8 ? c.dpf : c.dpb;
     if (scan) {
-        rc = E.qbf.ensure((size_t)Q * c.dpb * 2);
+        rc = E.qbf.ensure((size_t)Q * sdp * 2);
         if (!rc) rc = E.cand.ensure(sp.cand_words * sizeof(uint64_t));
         if (!rc) rc = E.cnt.ensure(sp.cnt_words * sizeof(uint32_t));
         if (!rc) rc = E.tq.ensure((size_t)2 * Q * sizeof(float));
@@ -544,11 +572,16 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     if (c.algo == KNNS_ALGO_TC) {
         // one pass per input: BF16 copy, exactness test, integrality, norms
         if (!pc) {
-            KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, c.dpb, E.bf.p, cn, n_pad, not_exact, s, int_stats));
+            KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, c.dpb, E.bf.p, cn, n_pad, not_exact, s, int_stats,
+                                      f8 ? E.f8.p : nullptr, 2 * c.dpf, f8 ? (float*)E.cs.p : nullptr));
             ++launches;
         }
-        KNN_CUDA(launch_prep_rows(queries, Q, ldq, D, c.dpb, scan ? E.qbf.p : nullptr, qn, Q, not_exact, s,
-                                  int_stats));
+        if (f8)
+            KNN_CUDA(launch_prep_rows(queries, Q, ldq, D, c.dpb, nullptr, qn, Q, not_exact, s, int_stats, E.qbf.p,
+                                      2 * c.dpf, (float*)E.qs.p));
+        else
+            KNN_CUDA(launch_prep_rows(queries, Q, ldq, D, c.dpb, scan ? E.qbf.p : nullptr, qn, Q, not_exact, s,
+                                      int_stats));
         ++launches;
         if (!bf16_only && !pc) {
             // the TF32 split runs only for data that is not BF16-exact
@@ -688,15 +721,19 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         a.cnt = (uint32_t*)E.cnt.p;
         a.err = (int*)E.err.p;
         a.Q = Q;
-        a.dpb = c.dpb;
-        a.ksteps = (D + 15) / 16;
+        a.dpb = sdp;
+        a.ksteps = f8 ? (D + 31) / 32 : (D + 15) / 16;
         a.bps = sp.bps;
         a.ring = sp.ring;
-        auto scan_pass = [&](int64_t nview, int64_t stride, const float* cn_view, const float* thr, int splits,
-                             int64_t split_len, int cap) -> int {
-            int r = encode_rows_bf16(&a.tm_c, bf_p, nview, c.dpb, stride * c.dpb, scan_box_rows(c.dpb));
+        a.fp8 = f8 ? 1 : 0;
+        a.qs = f8 ? (const float*)E.qs.p : nullptr;
+        auto scan_pass = [&](int64_t nview, int64_t stride, const float* cn_view, const float* cs_view,
+                             const float* thr, int splits, int64_t split_len, int cap) -> int {
+            // the map moves bytes: E4M3 rows are described as rows of 16-bit units
+            int r = encode_rows_bf16(&a.tm_c, f8 ? f8_p : bf_p, nview, sdp, stride * sdp, scan_box_rows(sdp));
             if (r) return r;
             a.cn = cn_view;
+            a.cs = cs_view;
             a.thr = thr;
             a.N = nview;
             a.split_len = split_len;
@@ -714,11 +751,17 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         // seeding, coarse to fine: level l keeps the keys below the previous level's
         // threshold (the coarsest keeps every key) and yields the key of rank j_l
         float* cnv = (float*)E.cnv.p;
+        float* csv = f8 ? (float*)E.csv.p : nullptr;
         const float* T = nullptr;
         for (int l = 0; l < sp.levels; ++l) {
             const ScanLevel& v = sp.lv[l];
             KNN_CUDA(launch_gather_norms(cn, v.n, v.stride, cnv, v.n_pad, s));
-            if ((rc = scan_pass(v.n, v.stride, cnv, T, v.S, v.len, v.cap))) return rc;
+            if (f8) {
+                // scales of the sample rows, 0 for padding (whose +inf norms keep their keys at +inf)
+                KNN_CUDA(launch_gather_norms(cs_p, v.n, v.stride, csv, v.n_pad, s, 0.f));
+                ++launches;
+            }
+            if ((rc = scan_pass(v.n, v.stride, cnv, csv, T, v.S, v.len, v.cap))) return rc;
             cs.nseg = kScanParts * v.S;
             cs.cap = v.cap;
             cs.thr_out = Tbuf[l & 1];
@@ -728,10 +771,11 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
             launches += 3;
             T = Tbuf[l & 1];
             cnv += v.n_pad;
+            if (csv) csv += v.n_pad;
         }
         if ((rc = mark(2))) return rc;
         // main pass
-        if ((rc = scan_pass(N, 1, cn, T, sp.S, sp.len, sp.cap))) return rc;
+        if ((rc = scan_pass(N, 1, cn, cs_p, T, sp.S, sp.len, sp.cap))) return rc;
         if ((rc = mark(3))) return rc;
         KNN_CUDA(cudaMemsetAsync(fail_cnt, 0, sizeof(uint32_t), s));
         cs.nseg = kScanParts * sp.S;
@@ -747,7 +791,8 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         cs.queries = queries;
         cs.ldq = ldq;
         cs.qn = qn;
-        cs.int_stats = int_stats;
+        // E4M3 keys are never exact: always re-ranked
+        cs.int_stats = f8 ? nullptr : int_stats;
         cs.bf16_inexact = not_exact;
         cs.out_dist = dist;
         cs.out_idx = idx;
@@ -814,10 +859,12 @@ void PreparedCorpus::release()
     lo.release();
     tiles.release();
     words.release();
+    f8.release();
+    cs.release();
 }
 
 int prepare_corpus(Engine& E, PreparedCorpus* pc, const float* corpus, int64_t N, int64_t ldc, int D, bool tf32,
-                   cudaStream_t s)
+                   cudaStream_t s, bool fp8)
 {
     if (!pc || !corpus || N <= 0 || D <= 0 || ldc < D) return set_error(KNNS_ERR_INVALID, "invalid corpus");
     if (N > 0x7fffffffLL) return set_error(KNNS_ERR_UNSUPPORTED, "corpus larger than 2^31-1 rows");
@@ -832,10 +879,14 @@ int prepare_corpus(Engine& E, PreparedCorpus* pc, const float* corpus, int64_t N
     if (!rc) rc = pc->tiles.ensure(((size_t)cdiv(N, 128) + 1) * sizeof(uint32_t));
     if (!rc && tf32) rc = pc->hi.ensure((size_t)N * dp * sizeof(float));
     if (!rc && tf32) rc = pc->lo.ensure((size_t)N * dp * sizeof(float));
+    const int dpf = ((D + 127) & ~127) / 2;
+    if (!rc && fp8) rc = pc->f8.ensure((size_t)N * dpf * 2);
+    if (!rc && fp8) rc = pc->cs.ensure(n_pad * sizeof(float));
     if (rc) return rc;
     uint32_t* w = (uint32_t*)pc->words.p;
     KNN_CUDA(cudaMemsetAsync(w, 0, 8 * sizeof(uint32_t), s));
-    KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, dpb, pc->bf.p, (float*)pc->cn.p, n_pad, w + 1, s, w + 2));
+    KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, dpb, pc->bf.p, (float*)pc->cn.p, n_pad, w + 1, s, w + 2,
+                              fp8 ? pc->f8.p : nullptr, 2 * dpf, fp8 ? (float*)pc->cs.p : nullptr));
     if (tf32)
         KNN_CUDA(launch_split(corpus, N, ldc, D, dp, (float*)pc->hi.p, (float*)pc->lo.p, (uint32_t*)pc->tiles.p, w,
                               nullptr, s));
@@ -844,6 +895,8 @@ int prepare_corpus(Engine& E, PreparedCorpus* pc, const float* corpus, int64_t N
     pc->ldc = ldc;
     pc->D = D;
     pc->dpb = dpb;
+    pc->dpf = dpf;
+    pc->fp8 = fp8;
     pc->dp = dp;
     pc->tf32 = tf32;
     return KNNS_OK;
@@ -1064,7 +1117,8 @@ int knns_index_create(const float* corpus, int64_t N, int64_t ldc, int D, int fl
     std::unique_ptr<knns_index> ix(new knns_index());
     ix->device = E->device;
     cudaStream_t s = (cudaStream_t)stream;
-    rc = prepare_corpus(*E, &ix->pc, corpus, N, ldc, D, (flags & KNNS_INDEX_TF32) != 0, s);
+    rc = prepare_corpus(*E, &ix->pc, corpus, N, ldc, D, (flags & KNNS_INDEX_TF32) != 0, s,
+                        (flags & KNNS_INDEX_FP8) != 0);
     if (rc) {
         ix->pc.release();
         return rc;
@@ -1095,11 +1149,13 @@ int knns_index_search(knns_index* ix, const float* queries, int64_t Q, int64_t l
     return rc;
 }
 
-int knns_autotune_shortlist(knns_index* ix, const float* queries, int64_t Q, int64_t ldq, int k, double target,
-                            int* c_out, double* recall_out, void* stream)
+int knns_autotune_shortlist(knns_index* ix, const float* queries, int64_t Q, int64_t ldq, int k, int precision,
+                            double target, int* c_out, double* recall_out, void* stream)
 {
     clear_error();
     if (!ix || !queries || Q <= 0 || k <= 0 || !c_out) return set_error(KNNS_ERR_INVALID, "bad arguments");
+    if (precision != KNNS_PREC_BF16 && precision != KNNS_PREC_FP8)
+        return set_error(KNNS_ERR_INVALID, "the shortlist factor belongs to the BF16 and FP8 forms");
     Engine* E = nullptr;
     int rc = get_engine(&E);
     if (rc) return rc;
@@ -1137,7 +1193,7 @@ int knns_autotune_shortlist(knns_index* ix, const float* queries, int64_t Q, int
     for (int c : {2, 4, 8}) {
         if (rc) break;
         if ((int64_t)c * k > kMaxKpTC && c != 2) break;  // the shortlist holds at most kMaxKpTC entries
-        rc = run(KNNS_PREC_BF16, c, got);
+        rc = run(precision, c, got);
         if (rc) break;
         int64_t hit = 0;
         for (int64_t q = 0; q < Q; ++q) {

@@ -30,6 +30,9 @@ struct Config {
     int dp = 0;
     int dpb = 0;
     int stages = 0;
+    // E4M3 keys (KNNS_PREC_FP8): the scan's row width in 16-bit units, (D rounded up to 128) / 2
+    bool fp8 = false;
+    int dpf = 0;
 };
 
 struct Engine {
@@ -42,6 +45,8 @@ struct Engine {
     // threshold-scan path: BF16 queries, candidate segments and counts, seeded
     // thresholds, sample norms, failed-query list
     DevBuf qbf, cand, cnt, tq, cnv, fail;
+    // E4M3 keys: corpus codes and row scales, query scales, sample scales
+    DevBuf f8, cs, qs, csv;
     // per-search flag words: [0] some corpus tile has a TF32 low part, [1] corpus or
     // queries not BF16-exact, [2] some value not an integer, [3] max |x| (float bits), [4] zero
     DevBuf words;
@@ -63,16 +68,16 @@ struct Engine {
 };
 
 // A corpus prepared once and kept resident (the serving index): BF16 copy,
-// norms, optional TF32 hi/lo copies with their per-tile low-part flags, and
-// the corpus half of the flag words ([0] low part, [1] not BF16-exact,
+// norms, optional TF32 hi/lo copies with their per-tile low-part flags,
+// optional E4M3 codes with per-row scales, and the corpus half of the flag words ([0] low part, [1] not BF16-exact,
 // [2] not integer, [3] max |x| bits).  The caller keeps the FP32 corpus alive
 // and unchanged while the index is used.
 struct PreparedCorpus {
     const float* corpus = nullptr;
     int64_t N = 0, ldc = 0;
-    int D = 0, dpb = 0, dp = 0;
-    bool tf32 = false;
-    DevBuf cn, bf, hi, lo, tiles, words;
+    int D = 0, dpb = 0, dp = 0, dpf = 0;
+    bool tf32 = false, fp8 = false;
+    DevBuf cn, bf, hi, lo, tiles, words, f8, cs;
     void release();
 };
 
@@ -89,7 +94,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
                int D, int k, float* dist, int32_t* idx, float* idx_f, const knns_options& o, cudaStream_t s,
                knns_stats* st, const PreparedCorpus* pc = nullptr, bool capture = false);
 int prepare_corpus(Engine& E, PreparedCorpus* pc, const float* corpus, int64_t N, int64_t ldc, int D, bool tf32,
-                   cudaStream_t s);
+                   cudaStream_t s, bool fp8 = false);
 int check_device_error(Engine& E, cudaStream_t s);
 int search_host(const float* corpus, int64_t N, const float* queries, int64_t Q, int D, int k, float* dist,
                 int32_t* idx, float* idx_f_host, const knns_options& o, double* seconds, knns_stats* st);

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <limits>
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -44,8 +45,11 @@ cudaError_t launch_bf16(const float* x, int64_t n, int64_t ld, int D, int dpb, v
 constexpr int kPrepMaxD = 383;
 // int_stats (optional, 2 words, zeroed by the caller): [0] |= 1 when some value is not an
 // integer, [1] = max |x| as float bits.
+// f8 / scales (optional): E4M3 copy [n][f8_bytes] (f8_bytes a multiple of 128, zero padded) with
+// per-row absmax scales (row = scale * codes; scales[n..n_pad) = 0); needs D <= kPrepMaxD.
 cudaError_t launch_prep_rows(const float* x, int64_t n, int64_t ld, int D, int dpb, void* out, float* norms,
-                             int64_t n_pad, uint32_t* not_exact, cudaStream_t s, uint32_t* int_stats = nullptr);
+                             int64_t n_pad, uint32_t* not_exact, cudaStream_t s, uint32_t* int_stats = nullptr,
+                             void* f8 = nullptr, int f8_bytes = 0, float* scales = nullptr);
 
 // CUDA-core FP32 fused distance + shortlist.  qpb in {32, 128}.
 size_t simt_smem_bytes(int qpb, int kp);
@@ -101,10 +105,15 @@ constexpr int kScanTileN = 256;
 constexpr int kScanParts = 4;
 constexpr int kScanMaxRing = 8;
 constexpr size_t kScanSmemLimit = 232448;
+// Row width of the scan's operands in 16-bit units (dpb below): D rounded up to
+// 64 for BF16 keys; for E4M3 keys the row's bytes (D rounded up to 128) / 2,
+// so both key types share one tile geometry per 128-byte K box.
 struct ScanArgs {
-    CUtensorMap tm_c;          // corpus bf16 [N][dpb] (view), box {64, scan_box_rows(dpb)}, 128B swizzle
-    const void* qbf;           // queries bf16 [Q][dpb]
+    CUtensorMap tm_c;          // corpus [N][dpb] 16-bit units (view), box {64, scan_box_rows(dpb)}, 128B swizzle
+    const void* qbf;           // queries [Q][dpb] 16-bit units (BF16, or E4M3 bytes)
     const float* cn;           // [>= N + scan_tile_rows(dpb)] corpus norms of the view, +inf padding
+    const float* cs;           // fp8: corpus row scales of the view (same padding, 0 there)
+    const float* qs;           // fp8: query row scales [Q]
     const float* thr;          // [Q] thresholds (null: +inf, every key collected)
     const uint32_t* skip_if;   // optional: the kernel returns at once when *skip_if != 0
     uint64_t* cand;            // [splits*kScanParts][Q][cap]
@@ -114,18 +123,19 @@ struct ScanArgs {
     int64_t N;
     int64_t split_len;         // multiple of scan_tile_rows(dpb)
     int cap;
-    int dpb;                   // D rounded up to 64, <= 256
-    int ksteps;                // MMA K steps of 16 holding data: ceil(D / 16)
+    int dpb;                   // row width in 16-bit units, multiple of 64, <= 256
+    int ksteps;                // MMA K steps holding data (32 bytes each): ceil(D / 16) BF16, ceil(D / 32) E4M3
     int bps;                   // K-boxes per ring slot (divides dpb/64)
     int ring;                  // ring slots
+    int fp8;                   // keys from E4M3 operands with per-row scales
 };
 // corpus rows per tile (MMA N): 224 for dpb <= 128, 192 for dpb <= 256
 int scan_tile_rows(int dpb);
 // rows of the corpus tensor map's box: the share of a tile one CTA of a cluster loads
 int scan_box_rows(int dpb);
-size_t scan_smem_bytes(int dpb, int bps, int ring);
+size_t scan_smem_bytes(int dpb, int bps, int ring, bool fp8 = false);
 // Ring geometry for dpb (want_bps = 0: automatic).  Returns 0 on success.
-int scan_plan(int dpb, int want_bps, int* bps, int* ring);
+int scan_plan(int dpb, int want_bps, int* bps, int* ring, bool fp8 = false);
 cudaError_t launch_scan(const ScanArgs& a, int splits, cudaStream_t s);
 
 // Merge of the per-split shortlists, optional exact re-rank, final top-k.
@@ -202,7 +212,8 @@ struct CandSelect {
 cudaError_t launch_select_cand(const CandSelect& c, cudaStream_t s);
 
 // out[i] = src[i * stride] for i < n, +inf for n <= i < n_pad (norms of a strided corpus sample).
+// out[i] = src[i * stride] for i < n, pad for n <= i < n_pad (+inf: norms of padding rows)
 cudaError_t launch_gather_norms(const float* src, int64_t n, int64_t stride, float* out, int64_t n_pad,
-                                cudaStream_t s);
+                                cudaStream_t s, float pad = std::numeric_limits<float>::infinity());
 
 }  // namespace knn

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 #include <cuda_runtime.h>
 #include "common.cuh"
 #include "kernels.h"
@@ -105,17 +106,19 @@ __global__ void split_tiles_kernel(const float* __restrict__ x, int64_t n, int64
 }
 
 __global__ void gather_norms_kernel(const float* __restrict__ src, int64_t n, int64_t stride, float* __restrict__ out,
-                                    int64_t n_pad)
+                                    int64_t n_pad, float pad)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_pad) return;
-    out[i] = i < n ? src[i * stride] : __int_as_float(0x7f800000);
+    out[i] = i < n ? src[i * stride] : pad;
 }
 
 // Fused preparation of a row-major matrix in one coalesced read: rows staged in
 // shared memory ([rows][pitch], pitch odd: conflict-free per-row walks), then
 //  * BF16 copy into out[n][dpb] (zero padded) and the "not exactly
 //    representable" flag (*not_exact |= 1), when out / not_exact are given;
+//  * E4M3 copy into f8[n][f8_bytes] (zero padded) with per-row absmax scales
+//    (scale = max|x| / 448, codes = satfinite(x * 448 / max|x|)), when given;
 //  * row norms into norms[0..n_pad) (+inf for n <= i < n_pad), when given:
 //    the float rounding of the double sum of x_d^2 in d order.  A row of
 //    integers whose float sum stays below 2^24 is summed in float: every
@@ -125,7 +128,9 @@ __global__ void __launch_bounds__(256) prep_rows_kernel(const float* __restrict_
                                                         int dpb, __nv_bfloat16* __restrict__ out,
                                                         float* __restrict__ norms, int64_t n_pad,
                                                         uint32_t* __restrict__ not_exact,
-                                                        uint32_t* __restrict__ int_stats)
+                                                        uint32_t* __restrict__ int_stats,
+                                                        uint8_t* __restrict__ f8, int f8_bytes,
+                                                        float* __restrict__ scales)
 {
     extern __shared__ float tile[];
     const int pitch = D | 1;
@@ -168,6 +173,27 @@ __global__ void __launch_bounds__(256) prep_rows_kernel(const float* __restrict_
         bad = __syncthreads_or(bad);
         if (threadIdx.x == 0 && bad && not_exact) atomicOr(not_exact, 1u);
     }
+    if (f8 != nullptr) {
+        for (int r = warp; r < rows; r += 8) {
+            const float* row = tile + r * pitch;
+            float mx = 0.f;
+            for (int c = lane; c < D; c += 32) mx = fmaxf(mx, fabsf(row[c]));
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            const float inv = mx > 0.f ? 448.f / mx : 0.f;
+            uint32_t* dst = reinterpret_cast<uint32_t*>(f8 + (r0 + r) * (int64_t)f8_bytes);
+            for (int c = 4 * lane; c < f8_bytes; c += 128) {
+                float v[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) v[j] = c + j < D ? row[c + j] * inv : 0.f;
+                const uint32_t lo = __nv_cvt_float2_to_fp8x2(make_float2(v[0], v[1]), __NV_SATFINITE, __NV_E4M3);
+                const uint32_t hi = __nv_cvt_float2_to_fp8x2(make_float2(v[2], v[3]), __NV_SATFINITE, __NV_E4M3);
+                dst[c >> 2] = lo | (hi << 16);
+            }
+            if (lane == 0) scales[r0 + r] = mx / 448.f;
+        }
+        for (int r = rows + (int)threadIdx.x; r < kRows && r0 + r < n_pad; r += blockDim.x) scales[r0 + r] = 0.f;
+    }
     if (norms != nullptr && threadIdx.x < kRows) {
         const int64_t i = r0 + threadIdx.x;
         if (i < n) {
@@ -195,11 +221,15 @@ __global__ void __launch_bounds__(256) prep_rows_kernel(const float* __restrict_
 }
 
 cudaError_t launch_prep_rows(const float* x, int64_t n, int64_t ld, int D, int dpb, void* out, float* norms,
-                             int64_t n_pad, uint32_t* not_exact, cudaStream_t s, uint32_t* int_stats)
+                             int64_t n_pad, uint32_t* not_exact, cudaStream_t s, uint32_t* int_stats, void* f8,
+                             int f8_bytes, float* scales)
 {
-    const int64_t rows = std::max(n, norms ? n_pad : n);
+    const int64_t rows = std::max(n, (norms || scales) ? n_pad : n);
     if (rows <= 0) return cudaSuccess;
     const int pitch = D | 1;
+    if (f8 != nullptr && (D > kPrepMaxD || scales == nullptr || f8_bytes % 128 != 0 || f8_bytes < D))
+        return cudaErrorInvalidValue;
+    uint8_t* f8b = static_cast<uint8_t*>(f8);
     if (D > kPrepMaxD) {
         // wide rows: separate passes
         cudaError_t e = cudaSuccess;
@@ -214,23 +244,25 @@ cudaError_t launch_prep_rows(const float* x, int64_t n, int64_t ld, int D, int d
                                              (int)smem);
         if (e != cudaSuccess) return e;
         prep_rows_kernel<128><<<(unsigned)((rows + 127) / 128), 256, smem, s>>>(
-            x, n, ld, D, dpb, static_cast<__nv_bfloat16*>(out), norms, n_pad, not_exact, int_stats);
+            x, n, ld, D, dpb, static_cast<__nv_bfloat16*>(out), norms, n_pad, not_exact, int_stats, f8b, f8_bytes,
+            scales);
     } else {
         const size_t smem = (size_t)64 * pitch * 4;
         cudaError_t e = cudaFuncSetAttribute(prep_rows_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
         prep_rows_kernel<64><<<(unsigned)((rows + 63) / 64), 256, smem, s>>>(
-            x, n, ld, D, dpb, static_cast<__nv_bfloat16*>(out), norms, n_pad, not_exact, int_stats);
+            x, n, ld, D, dpb, static_cast<__nv_bfloat16*>(out), norms, n_pad, not_exact, int_stats, f8b, f8_bytes,
+            scales);
     }
     return cudaGetLastError();
 }
 
 cudaError_t launch_gather_norms(const float* src, int64_t n, int64_t stride, float* out, int64_t n_pad,
-                                cudaStream_t s)
+                                cudaStream_t s, float pad)
 {
     if (n_pad <= 0) return cudaSuccess;
-    gather_norms_kernel<<<(unsigned)((n_pad + 255) / 256), 256, 0, s>>>(src, n, stride, out, n_pad);
+    gather_norms_kernel<<<(unsigned)((n_pad + 255) / 256), 256, 0, s>>>(src, n, stride, out, n_pad, pad);
     return cudaGetLastError();
 }
 

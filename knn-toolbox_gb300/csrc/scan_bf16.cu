@@ -11,6 +11,11 @@
 // from the segments by select_cand_kernel.  Keys are the reference's ranking
 // key ||c||^2 - 2 q.c (demo/knn.m:5), q.c from BF16 operands with FP32
 // accumulation (exact products), the norm added with one FP32 fma.
+// The E4M3 variant (kF8) takes both operands as FP8 E4M3 codes with per-row
+// absmax scales (x = s_x * codes): kind::f8f6f4 MMAs accumulate the code
+// products in FP32 and the epilogue forms ||c||^2 + (-2 s_q) * (s_c * acc),
+// with the corpus scales streamed beside the norms.  A 128-byte K box holds
+// 64 BF16 or 128 E4M3 values; everything else is shared.
 //
 // Tile: 128 queries (MMA M, TMEM lanes) x TN corpus rows (MMA N), TN = 224
 // for up to 128 BF16 columns, 192 for up to 256.  Tensor memory holds two
@@ -60,7 +65,11 @@ constexpr uint32_t kTmemCols = 512;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 
 __host__ __device__ constexpr uint32_t box_bytes(int tn) { return (uint32_t)tn * 128u; }  // 64 bf16 x tn rows
-__host__ __device__ constexpr uint32_t norm_bytes(int tn) { return (uint32_t)kNormSlots * tn * 4u; }
+// norm ring: kNormSlots tiles of norms, then (E4M3 keys) as many tiles of corpus scales
+__host__ __device__ constexpr uint32_t norm_bytes(int tn, bool f8 = false)
+{
+    return (uint32_t)kNormSlots * tn * 4u * (f8 ? 2u : 1u);
+}
 
 struct ScanSmem {
     unsigned char* ring;
@@ -94,16 +103,28 @@ __device__ __forceinline__ float min8(const float* k)
 }
 
 // Keys ||c||^2 - 2 q.c of a W-column chunk and the mask of its 8-column groups
-// that hold a key below the lane's threshold.
-template <int W>
-__device__ __forceinline__ uint32_t chunk_keys(const float (&v)[W], const float* nrm, float T, float (&key)[W])
+// that hold a key below the lane's threshold.  BF16: q.c = acc, m = -2;
+// E4M3: q.c = s_q s_c acc with m = -2 s_q and the corpus scales s_c at scl.
+template <int W, bool kF8>
+__device__ __forceinline__ uint32_t chunk_keys(const float (&v)[W], const float* nrm, const float* scl, float m,
+                                               float T, float (&key)[W])
 {
     const float4* n4 = reinterpret_cast<const float4*>(nrm);
+    const float4* s4 = reinterpret_cast<const float4*>(scl);
 #pragma unroll
     for (int u = 0; u < W / 4; ++u) {
         const float4 c = n4[u];
-        ptx::fma2(key[4 * u], key[4 * u + 1], v[4 * u], v[4 * u + 1], -2.0f, c.x, c.y);
-        ptx::fma2(key[4 * u + 2], key[4 * u + 3], v[4 * u + 2], v[4 * u + 3], -2.0f, c.z, c.w);
+        if (kF8) {
+            const float4 sc = s4[u];
+            float t0, t1, t2, t3;
+            ptx::mul2(t0, t1, v[4 * u], v[4 * u + 1], sc.x, sc.y);
+            ptx::mul2(t2, t3, v[4 * u + 2], v[4 * u + 3], sc.z, sc.w);
+            ptx::fma2(key[4 * u], key[4 * u + 1], t0, t1, m, c.x, c.y);
+            ptx::fma2(key[4 * u + 2], key[4 * u + 3], t2, t3, m, c.z, c.w);
+        } else {
+            ptx::fma2(key[4 * u], key[4 * u + 1], v[4 * u], v[4 * u + 1], m, c.x, c.y);
+            ptx::fma2(key[4 * u + 2], key[4 * u + 3], v[4 * u + 2], v[4 * u + 3], m, c.z, c.w);
+        }
     }
     uint32_t gm = 0;
 #pragma unroll
@@ -133,13 +154,13 @@ __device__ __forceinline__ void chunk_append(const float (&key)[W], uint32_t gm,
     }
 }
 
-template <int TN>
+template <int TN, bool kF8>
 __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads, 1)
     scan_kernel(const __grid_constant__ ScanArgs a)
 {
     constexpr int TW = TN / kScanParts - 32;  // tail columns per epilogue part (24 or 16)
     constexpr uint32_t kBoxB = box_bytes(TN);
-    constexpr uint32_t kIdesc = ptx::idesc_bf16(kTileQ, TN);
+    constexpr uint32_t kIdesc = kF8 ? ptx::idesc_e4m3(kTileQ, TN) : ptx::idesc_bf16(kTileQ, TN);
     constexpr uint32_t kACol = 2u * TN;  // A operand columns [kACol, kACol + dpb/2)
     constexpr int kPieceRows = TN / kCluster;  // rows of every box this CTA loads for the cluster
     static_assert(kPieceRows % 8 == 0, "pieces of whole 8-row swizzle atoms");
@@ -162,7 +183,8 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads,
     ScanSmem s;
     s.ring = sm;
     s.norms = reinterpret_cast<float*>(s.ring + (size_t)R * slot_bytes);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(s.norms) + norm_bytes(TN));
+    float* scales = s.norms + kNormSlots * TN;  // E4M3 keys: corpus scales, same slots as the norms
+    uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(s.norms) + norm_bytes(TN, kF8));
     s.full = bars;
     s.empty = bars + kScanMaxRing;
     s.accf = bars + 2 * kScanMaxRing;
@@ -238,8 +260,9 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads,
                     ok = false;
                     break;
                 }
-                ptx::mbar_arrive_expect_tx(&s.nfull[ns], TN * 4u);
+                ptx::mbar_arrive_expect_tx(&s.nfull[ns], TN * 4u * (kF8 ? 2u : 1u));
                 ptx::bulk_load(s.norms + ns * TN, a.cn + n0, TN * 4u, &s.nfull[ns]);
+                if (kF8) ptx::bulk_load(scales + ns * TN, a.cs + n0, TN * 4u, &s.nfull[ns]);
             }
             // let copies already issued land before the CTA winds down
             if (!ok) {
@@ -268,12 +291,16 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads,
                     const uint32_t b_base = ptx::smem_u32(s.ring + (size_t)st * slot_bytes);
                     for (int bx = 0; bx < bps; ++bx) {
                         const int box = c * bps + bx;
-                        // K steps of 16 past the last data column hold zeros on both sides: skipped
+                        // K steps (32 bytes) past the last data column hold zeros on both sides: skipped
                         const int kn = min(4, a.ksteps - 4 * box);
                         for (int kk = 0; kk < kn; ++kk) {
                             const uint64_t db = ptx::desc_sw128_kmajor(b_base + bx * kBoxB + kk * 32);
-                            ptx::mma_bf16_ts(d_tmem, a_tmem + (uint32_t)(box * 32 + kk * 8), db, kIdesc,
-                                             (box | kk) != 0);
+                            if (kF8)
+                                ptx::mma_f8_ts(d_tmem, a_tmem + (uint32_t)(box * 32 + kk * 8), db, kIdesc,
+                                               (box | kk) != 0);
+                            else
+                                ptx::mma_bf16_ts(d_tmem, a_tmem + (uint32_t)(box * 32 + kk * 8), db, kIdesc,
+                                                 (box | kk) != 0);
                         }
                     }
                     // the slot is free once every CTA of the cluster has consumed it
@@ -296,7 +323,8 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads,
         const bool valid = q < a.Q;
         const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
         if (part == 0) {
-            // A operand: this lane's query (BF16 pairs, lower K index in the low half) into TMEM
+            // A operand: this lane's query into TMEM (BF16 pairs or E4M3 quads per 32-bit column,
+            // lower K index in the low bits)
             const uint32_t* qrow = reinterpret_cast<const uint32_t*>(a.qbf) + (valid ? q : 0) * (a.dpb / 2);
             for (int bx = 0; bx < nbox; ++bx) {
                 float w[32];
@@ -312,6 +340,7 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads,
         }
         // padding lanes of the last query tile collect nothing
         const float T = valid ? (a.thr ? __ldg(a.thr + q) : __int_as_float(0x7f800000)) : -__int_as_float(0x7f800000);
+        const float m = kF8 ? -2.0f * (valid ? __ldg(a.qs + q) : 0.f) : -2.0f;
         const size_t seg = (size_t)blockIdx.y * kScanParts + part;
         uint64_t* out = a.cand + (seg * (size_t)a.Q + (size_t)(valid ? q : 0)) * (size_t)a.cap;
         uint32_t cnt = 0;
@@ -328,6 +357,7 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads,
             // this part's columns, every TMEM load at a multiple of its own width:
             // [32p, 32p+32) then the tail [128+16p, 128+16p+16) and, for TN = 224, [192+8p, 192+8p+8)
             const float* nrm = s.norms + ns * TN;
+            const float* scl = scales + ns * TN;
             const uint32_t tb = tmem + (uint32_t)b * TN + lane_base;
             const uint32_t nb = (uint32_t)(n_begin + (int64_t)t * TN);
             const int c32 = 32 * part, c16 = 128 + 16 * part, c8 = 192 + 8 * part;
@@ -339,7 +369,7 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads,
             ptx::tmem_ld16(tb + (uint32_t)c16, v16);
             if (TW == 24) ptx::tmem_ld8(tb + (uint32_t)c8, v8);
             float key[32];
-            const uint32_t ga = chunk_keys<32>(va, nrm + c32, T, key);
+            const uint32_t ga = chunk_keys<32, kF8>(va, nrm + c32, scl + c32, m, T, key);
             ptx::tmem_wait_ld();
             ptx::tie_regs(v16);
             if (TW == 24) ptx::tie_regs(v8);
@@ -349,8 +379,8 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads,
             if (lane == 0) ptx::mbar_arrive(&s.acce[b]);
             if (__any_sync(0xffffffffu, ga != 0u)) chunk_append<32>(key, ga, T, nb + (uint32_t)c32, out, cap, cnt);
             float k16[16], k8[8];
-            const uint32_t g16 = chunk_keys<16>(v16, nrm + c16, T, k16);
-            const uint32_t g8 = TW == 24 ? chunk_keys<8>(v8, nrm + c8, T, k8) : 0u;
+            const uint32_t g16 = chunk_keys<16, kF8>(v16, nrm + c16, scl + c16, m, T, k16);
+            const uint32_t g8 = TW == 24 ? chunk_keys<8, kF8>(v8, nrm + c8, scl + c8, m, T, k8) : 0u;
             if (__any_sync(0xffffffffu, (g16 | g8) != 0u)) {
                 chunk_append<16>(k16, g16, T, nb + (uint32_t)c16, out, cap, cnt);
                 if (TW == 24) chunk_append<8>(k8, g8, T, nb + (uint32_t)c8, out, cap, cnt);
@@ -378,18 +408,18 @@ int scan_tile_rows(int dpb) { return dpb <= 128 ? 224 : 192; }
 
 int scan_box_rows(int dpb) { return scan_tile_rows(dpb) / kCluster; }
 
-size_t scan_smem_bytes(int dpb, int bps, int ring)
+size_t scan_smem_bytes(int dpb, int bps, int ring, bool fp8)
 {
     const int tn = scan_tile_rows(dpb);
-    return (size_t)ring * bps * box_bytes(tn) + norm_bytes(tn) + kCtrlBytes;
+    return (size_t)ring * bps * box_bytes(tn) + norm_bytes(tn, fp8) + kCtrlBytes;
 }
 
-int scan_plan(int dpb, int want_bps, int* bps, int* ring)
+int scan_plan(int dpb, int want_bps, int* bps, int* ring, bool fp8)
 {
     const int nbox = dpb / 64;
     if (dpb % 64 != 0 || nbox < 1 || nbox > 4) return -1;
     const int tn = scan_tile_rows(dpb);
-    const size_t fixed = norm_bytes(tn) + kCtrlBytes;
+    const size_t fixed = norm_bytes(tn, fp8) + kCtrlBytes;
     auto slots = [&](int b) {
         return (int)std::min<size_t>(kScanMaxRing, (kScanSmemLimit - fixed) / ((size_t)b * box_bytes(tn)));
     };
@@ -411,30 +441,32 @@ int scan_plan(int dpb, int want_bps, int* bps, int* ring)
     return 0;
 }
 
+template <int TN, bool kF8>
+static cudaError_t launch_scan_t(const ScanArgs& a, dim3 grid, size_t smem, cudaStream_t st)
+{
+    cudaError_t e = cudaFuncSetAttribute(scan_kernel<TN, kF8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    scan_kernel<TN, kF8><<<grid, kScanThreads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_scan(const ScanArgs& a, int splits, cudaStream_t st)
 {
     const int nbox = a.dpb / 64;
     const int tn = scan_tile_rows(a.dpb);
+    const bool f8 = a.fp8 != 0;
     if (a.dpb % 64 != 0 || nbox < 1 || nbox > 4 || a.bps < 1 || nbox % a.bps != 0 || a.ring < 2 ||
-        a.ring > kScanMaxRing || a.split_len % tn != 0 || a.cap < 1 || splits < 1 || a.qbf == nullptr)
+        a.ring > kScanMaxRing || a.split_len % tn != 0 || a.cap < 1 || splits < 1 || a.qbf == nullptr ||
+        a.ksteps < 1 || a.ksteps > 4 * nbox || (f8 && (a.cs == nullptr || a.qs == nullptr)))
         return cudaErrorInvalidValue;
-    const size_t smem = scan_smem_bytes(a.dpb, a.bps, a.ring);
+    const size_t smem = scan_smem_bytes(a.dpb, a.bps, a.ring, f8);
     if (smem > kScanSmemLimit) return cudaErrorInvalidValue;
     if (a.Q <= 0) return cudaSuccess;
     // whole clusters: a padding query tile (all rows past Q) still loads its share of the corpus
     const int64_t qt = (a.Q + kTileQ - 1) / kTileQ;
     dim3 grid((unsigned)((qt + kCluster - 1) / kCluster * kCluster), (unsigned)splits);
-    cudaError_t e;
-    if (tn == 224) {
-        e = cudaFuncSetAttribute(scan_kernel<224>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        scan_kernel<224><<<grid, kScanThreads, smem, st>>>(a);
-    } else {
-        e = cudaFuncSetAttribute(scan_kernel<192>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        scan_kernel<192><<<grid, kScanThreads, smem, st>>>(a);
-    }
-    return cudaGetLastError();
+    if (tn == 224) return f8 ? launch_scan_t<224, true>(a, grid, smem, st) : launch_scan_t<224, false>(a, grid, smem, st);
+    return f8 ? launch_scan_t<192, true>(a, grid, smem, st) : launch_scan_t<192, false>(a, grid, smem, st);
 }
 
 }  // namespace knn

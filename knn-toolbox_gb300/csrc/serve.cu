@@ -435,7 +435,7 @@ int knns_server_create(knns_index* ix, const knns_server_config* cfg, knns_serve
     if (c.slots < 1 || c.slots > 8) return set_error(KNNS_ERR_INVALID, "slots must be 1..8");
     if (c.max_batch < 32 || c.max_batch > 65536 || (c.max_batch & (c.max_batch - 1)))
         return set_error(KNNS_ERR_INVALID, "max_batch must be a power of two in [32, 65536]");
-    if (c.precision != KNNS_PREC_EXACT && c.precision != KNNS_PREC_BF16)
+    if (c.precision != KNNS_PREC_EXACT && c.precision != KNNS_PREC_BF16 && c.precision != KNNS_PREC_FP8)
         return set_error(KNNS_ERR_INVALID, "unknown precision %d", c.precision);
     int rc = sv->setup();
     if (rc) {

@@ -153,6 +153,20 @@ __device__ __forceinline__ void mma_bf16_ts(uint32_t d_tmem, uint32_t a_tmem, ui
         : "memory");
 }
 
+// D[tmem] (+)= A[tmem] * B[smem desc]^T, kind::f8f6f4 (8-bit operands of the types named in idesc,
+// FP32 accumulate), cta_group::1: A rows in TMEM lanes, four K elements per 32-bit column
+// (lowest K in the low byte), 32 K elements per instruction
+__device__ __forceinline__ void mma_f8_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc, uint32_t idesc,
+                                          uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [%1], %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "r"(a_tmem), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
 // D[tmem] (+)= A[smem desc] * B[smem desc]^T, kind::f16 (BF16 operands, FP32 accumulate), cta_group::1
 __device__ __forceinline__ void mma_bf16_ss(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
                                             uint32_t accumulate)
@@ -301,6 +315,16 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
            | ((uint32_t)(M >> 4) << 24);   // M / 16
 }
 
+// Instruction descriptor: kind::f8f6f4 with E4M3 A/B (format code 0), D f32, K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_e4m3(int M, int N)
+{
+    return (1u << 4)                       // D format f32
+           | (0u << 7)                     // A format e4m3
+           | (0u << 10)                    // B format e4m3
+           | ((uint32_t)(N >> 3) << 17)    // N / 8
+           | ((uint32_t)(M >> 4) << 24);   // M / 16
+}
+
 // Instruction descriptor: kind::tf32, D f32, A/B tf32 K-major, M x N.
 __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N)
 {
@@ -320,6 +344,16 @@ __device__ __forceinline__ void fma2(float& o0, float& o1, float a0, float a1, f
     asm("mov.b64 %0, {%1, %2};" : "=l"(mm) : "f"(m), "f"(m));
     asm("mov.b64 %0, {%1, %2};" : "=l"(c) : "f"(c0), "f"(c1));
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(mm), "l"(c));
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(o0), "=f"(o1) : "l"(r));
+}
+
+// (o0, o1) = (a0 * b0, a1 * b1), one packed instruction
+__device__ __forceinline__ void mul2(float& o0, float& o1, float a0, float a1, float b0, float b1)
+{
+    uint64_t a, b, r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(a) : "f"(a0), "f"(a1));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(b) : "f"(b0), "f"(b1));
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
     asm("mov.b64 {%0, %1}, %2;" : "=f"(o0), "=f"(o1) : "l"(r));
 }
 

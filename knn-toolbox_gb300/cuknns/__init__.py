@@ -28,7 +28,7 @@ PKG = os.path.dirname(HERE)
 LIB_PATH = os.path.join(PKG, "_build", "libknngb300.so")
 
 ALGO_AUTO, ALGO_TC, ALGO_SIMT = 0, 1, 2
-PREC_EXACT, PREC_BF16 = 0, 1
+PREC_EXACT, PREC_BF16, PREC_FP8 = 0, 1, 2
 SCAN_AUTO, SCAN_ON, SCAN_OFF = 0, 1, 2
 OK, ERR_INVALID, ERR_CUDA, ERR_UNSUPPORTED, ERR_DEVICE_TIMEOUT, ERR_NOMEM = range(6)
 
@@ -107,7 +107,7 @@ def lib():
     L.knns_search_device_noalloc.argtypes = [vp, i64, i64, vp, i64, i64, ci, ci, vp, vp, vp]
     L.knns_index_create.argtypes = [vp, i64, i64, ci, ci, ctypes.POINTER(vp), vp]
     L.knns_index_search.argtypes = [vp, vp, i64, i64, ci, vp, vp, ctypes.POINTER(Options), vp]
-    L.knns_autotune_shortlist.argtypes = [vp, vp, i64, i64, ci, ctypes.c_double, ctypes.POINTER(ctypes.c_int),
+    L.knns_autotune_shortlist.argtypes = [vp, vp, i64, i64, ci, ci, ctypes.c_double, ctypes.POINTER(ctypes.c_int),
                                           ctypes.POINTER(ctypes.c_double), vp]
     L.knns_index_destroy.argtypes = [vp]
     L.knns_index_destroy.restype = None
@@ -208,15 +208,18 @@ def search(corpus, queries, k, *, dist=None, idx=None, algo=ALGO_AUTO, splits=0,
     return dist, idx
 
 
-def search_host(corpus, queries, k, *, algo=ALGO_AUTO, splits=0, rerank=True, kp=0):
-    """kNN on host arrays (N x D, Q x D float32).  Returns numpy (dist, idx)."""
+def search_host(corpus, queries, k, *, algo=ALGO_AUTO, splits=0, rerank=True, kp=0, **opts):
+    """kNN on host arrays (N x D, Q x D float32).  Returns numpy (dist, idx).
+
+    Further keyword options (precision, shortlist, scan, ...) as for search().
+    """
     corpus = np.ascontiguousarray(corpus, dtype=np.float32)
     queries = np.ascontiguousarray(queries, dtype=np.float32)
     N, D = corpus.shape
     Q = queries.shape[0]
     dist = np.empty((Q, k), np.float32)
     idx = np.empty((Q, k), np.int32)
-    o = options(algo, splits, rerank, kp)
+    o = options(algo, splits, rerank, kp, **opts)
     _check(lib().knns_search_host(corpus.ctypes.data, N, queries.ctypes.data, Q, D, k, dist.ctypes.data,
                                   idx.ctypes.data, ctypes.byref(o)))
     return dist, idx
@@ -372,15 +375,16 @@ def gpuknns(plan: dict, queries, data):
 # --------------------------------------------------------------------------
 
 INDEX_TF32 = 1
+INDEX_FP8 = 2
 
 
 class Index:
-    """A device corpus prepared once (BF16 copy, norms, flags, TF32 copies): searches skip its preparation.
+    """A device corpus prepared once (BF16 copy, norms, flags, TF32 copies, E4M3 codes): searches skip its preparation.
 
     The torch tensor is kept referenced: the engine reads it on every search.
     """
 
-    def __init__(self, corpus, tf32=True, stream=None):
+    def __init__(self, corpus, tf32=True, fp8=False, stream=None):
         import torch
         assert corpus.is_cuda and corpus.dtype == torch.float32 and corpus.stride(1) == 1
         self.corpus = corpus
@@ -388,7 +392,8 @@ class Index:
         s = torch.cuda.current_stream(corpus.device) if stream is None else stream
         h = ctypes.c_void_p()
         _check(lib().knns_index_create(corpus.data_ptr(), self.N, corpus.stride(0), self.D,
-                                       INDEX_TF32 if tf32 else 0, ctypes.byref(h), ctypes.c_void_p(s.cuda_stream)))
+                                       (INDEX_TF32 if tf32 else 0) | (INDEX_FP8 if fp8 else 0), ctypes.byref(h),
+                                       ctypes.c_void_p(s.cuda_stream)))
         self.handle = h
 
     def search(self, queries, k, *, dist=None, idx=None, stream=None, check=True, **opts):
@@ -407,14 +412,14 @@ class Index:
             _check(lib().knns_check_device(ctypes.c_void_p(s.cuda_stream)))
         return dist, idx
 
-    def autotune_shortlist(self, queries, k, target=0.999, stream=None):
-        """Smallest BF16 shortlist factor c in {2, 4, 8} reaching recall@k >= target on these queries."""
+    def autotune_shortlist(self, queries, k, target=0.999, precision=PREC_BF16, stream=None):
+        """Smallest shortlist factor c in {2, 4, 8} of the BF16 / FP8 form reaching recall@k >= target."""
         import torch
         s = torch.cuda.current_stream(queries.device) if stream is None else stream
         c = ctypes.c_int(0)
         r = ctypes.c_double(0.0)
         _check(lib().knns_autotune_shortlist(self.handle, queries.data_ptr(), queries.shape[0], queries.stride(0), k,
-                                             target, ctypes.byref(c), ctypes.byref(r),
+                                             precision, target, ctypes.byref(c), ctypes.byref(r),
                                              ctypes.c_void_p(s.cuda_stream)))
         return c.value, r.value
 

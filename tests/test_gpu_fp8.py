@@ -1,0 +1,123 @@
+"""FP8 E4M3 precision form: E4M3 codes with per-row absmax scales on the tensor
+cores (FP32 accumulation) rank a shortlist of c*k per query on the threshold
+scan, re-ranked by exact distance.
+
+Bars:
+ * data whose E4M3 codes and scales are exact (integers in [-7, 7], every row
+   holding a +-7, so scale = 7/448 = 2^-6 and codes = 64 x) make every key an
+   exact integer: the form returns exactly what the exact form returns, which
+   pins the 8-bit operand layout in tensor memory and the scale arithmetic;
+ * anisotropic Gaussian data (the 8M x 256 workload's generator, smaller):
+   recall@k >= 0.999 against the FP64 oracle at c = 2, distances within 1e-5
+   relative of FP64 for the returned indices, rows sorted;
+ * the fix-up (BF16 keys) and the small-corpus fallback (BF16 keys) stay exact
+   where their keys are exact; the resident index and the server give what a
+   plain search gives.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+DIST_REL = 1e-5
+
+
+def cuda(x):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def run(engine, X, Qs, k, **kw):
+    d, i = engine.search(cuda(X), cuda(Qs), k, **kw)
+    return d.cpu().numpy(), i.cpu().numpy(), engine.last_stats()
+
+
+def exact_codes(n, d, rng):
+    x = rng.integers(-7, 8, (n, d)).astype(np.float32)
+    x[np.arange(n), rng.integers(0, d, n)] = rng.choice([-7.0, 7.0], n).astype(np.float32)
+    return x
+
+
+@pytest.mark.parametrize("N,D,Q,k,c", [(150_000, 256, 257, 32, 2), (140_000, 64, 130, 10, 4),
+                                       (131_072, 200, 64, 16, 2), (40_000, 128, 300, 1, 8)])
+def test_exact_codes_match_exact_form(engine, oracle, N, D, Q, k, c):
+    rng = np.random.default_rng(N + D)
+    X, Qs = exact_codes(N, D, rng), exact_codes(Q, D, rng)
+    d, i, st = run(engine, X, Qs, k, precision=engine.PREC_FP8, shortlist=c, scan=engine.SCAN_ON)
+    assert st["scan"] == 1
+    d0, i0, _ = run(engine, X, Qs, k)
+    np.testing.assert_array_equal(i, i0)
+    np.testing.assert_array_equal(d, d0)
+    sub = np.arange(0, Q, 5)
+    od, oi = oracle.knn_gemm(X, Qs[sub], k, kp=st["kp"], rerank=True)
+    np.testing.assert_array_equal(i[sub], oi)
+    np.testing.assert_array_equal(d[sub], od)
+
+
+@pytest.mark.parametrize("N,D,k", [(300_000, 256, 32), (200_000, 100, 10)])
+def test_anisotropic_recall(engine, oracle, N, D, k):
+    import cuknns.synth as S
+    X, Qs = S.anisotropic(N, D, seed=21, nq=160)
+    d, i, st = run(engine, X, Qs, k, precision=engine.PREC_FP8, shortlist=2)
+    assert st["scan"] == 1 and st["kp"] >= 2 * k
+    ex = oracle.knn_f64(X, Qs, k)
+    rec = oracle.recall_at_k(i, ex[1])
+    assert rec >= 0.999, rec
+    got64 = oracle.pair_dist_f64(X, Qs, i)
+    assert (np.abs(d - got64) <= DIST_REL * got64 + 1e-6).all()
+    assert (np.diff(d, axis=1) >= 0).all()
+
+
+def test_duplicate_rows_go_to_the_fixup(engine, oracle):
+    # every query equals 2,000 corpus rows: the segments overflow and the fix-up
+    # (BF16 keys, exact for these integers) answers; ties go to the lower index
+    rng = np.random.default_rng(5)
+    base = rng.integers(0, 64, (10, 64)).astype(np.float32)
+    X = np.repeat(base, 2000, axis=0)
+    rng.shuffle(X)
+    Qs = base[rng.integers(0, 10, 40)]
+    k = 16
+    d, i, st = run(engine, X, Qs, k, precision=engine.PREC_FP8, shortlist=2, scan=engine.SCAN_ON)
+    assert st["scan"] == 1
+    od, oi = oracle.knn_gemm(X, Qs, k, kp=st["kp"], rerank=True)
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_array_equal(d, od)
+
+
+def test_small_corpus_uses_bf16_keys(engine):
+    import cuknns.synth as S
+    X, Qs = S.anisotropic(20_000, 128, seed=4, nq=100)
+    d, i, st = run(engine, X, Qs, 10, precision=engine.PREC_FP8, shortlist=4)
+    assert st["scan"] == 0
+    d0, i0, _ = run(engine, X, Qs, 10, precision=engine.PREC_BF16, shortlist=4)
+    np.testing.assert_array_equal(i, i0)
+    np.testing.assert_array_equal(d, d0)
+
+
+def test_index_server_and_autotuner(engine):
+    import cuknns.synth as S
+    X, Qs = S.anisotropic(200_000, 256, seed=8, nq=200)
+    c, q = cuda(X), cuda(Qs)
+    d0, i0 = engine.search(c, q, 32, precision=engine.PREC_FP8, shortlist=2)
+    ix = engine.Index(c, tf32=True, fp8=True)  # TF32 copies: the autotuner's ground truth is the exact form
+    d1, i1 = ix.search(q, 32, precision=engine.PREC_FP8, shortlist=2)
+    np.testing.assert_array_equal(i1.cpu().numpy(), i0.cpu().numpy())
+    np.testing.assert_array_equal(d1.cpu().numpy(), d0.cpu().numpy())
+    # the exact form at D = 256 runs on the CUDA-core kernel, with the index's norms
+    de, ie = engine.search(c, q, 32)
+    dx, ixx = ix.search(q, 32)
+    np.testing.assert_array_equal(ixx.cpu().numpy(), ie.cpu().numpy())
+    np.testing.assert_array_equal(dx.cpu().numpy(), de.cpu().numpy())
+    cf, rec = ix.autotune_shortlist(q[:64], 32, target=0.999, precision=engine.PREC_FP8)
+    assert cf in (2, 4) and rec <= 1.0
+    srv = engine.Server(ix, slots=2, max_batch=256, precision=engine.PREC_FP8, shortlist=2, autotune=False)
+    ids = [srv.submit(Qs[j:j + 50], 32) for j in range(0, 200, 50)]
+    got = [srv.wait(r) for r in ids]
+    srv.close()
+    i_alone = np.concatenate([g[1] for g in got])
+    assert (i_alone == i0.cpu().numpy()).mean() >= 0.999
+    ix.close()
+    ix2 = engine.Index(c, tf32=False)
+    with pytest.raises(engine.KnnsError):
+        ix2.search(q, 32, precision=engine.PREC_FP8)  # no E4M3 copies in this index
+    ix2.close()
