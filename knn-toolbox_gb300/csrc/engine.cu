@@ -1229,6 +1229,24 @@ void knns_index_destroy(knns_index* ix)
     delete ix;
 }
 
+int knns_debug_prep(const float* x, int64_t n, int64_t ld, int D, float* norms, void* bf16, void* f8, float* scales,
+                    uint32_t* words)
+{
+    clear_error();
+    if (!x || !norms || !bf16 || !f8 || !scales || !words || n <= 0 || D <= 0 || D > kPrepMaxD || ld < D)
+        return set_error(KNNS_ERR_INVALID, "bad args");
+    Engine* E = nullptr;
+    int rc = get_engine(&E);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(E->mu);
+    cudaStream_t s = E->host_stream();
+    KNN_CUDA(cudaMemsetAsync(words, 0, 3 * sizeof(uint32_t), s));
+    KNN_CUDA(launch_prep_rows(x, n, ld, D, (D + 63) & ~63, bf16, norms, n, words, s, words + 1, f8, (D + 127) & ~127,
+                              scales));
+    KNN_CUDA(cudaStreamSynchronize(s));
+    return KNNS_OK;
+}
+
 int knns_debug_tc_dot_tile(const float* corpus, int64_t N, const float* queries, int64_t Q, int D, float* dump)
 {
     clear_error();

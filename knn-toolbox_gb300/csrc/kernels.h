@@ -42,7 +42,7 @@ cudaError_t launch_bf16(const float* x, int64_t n, int64_t ld, int D, int dpb, v
 // with the exactness flag, optional norms[0..n_pad) (+inf padding), same
 // conventions as launch_norms / launch_bf16.  Rows wider than kPrepMaxD fall
 // back to those two kernels.
-constexpr int kPrepMaxD = 383;
+constexpr int kPrepMaxD = 384;
 // int_stats (optional, 2 words, zeroed by the caller): [0] |= 1 when some value is not an
 // integer, [1] = max |x| as float bits.
 // f8 / scales (optional): E4M3 copy [n][f8_bytes] (f8_bytes a multiple of 128, zero padded) with

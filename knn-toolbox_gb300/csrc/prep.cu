@@ -113,110 +113,200 @@ __global__ void gather_norms_kernel(const float* __restrict__ src, int64_t n, in
     out[i] = i < n ? src[i * stride] : pad;
 }
 
-// Fused preparation of a row-major matrix in one coalesced read: rows staged in
-// shared memory ([rows][pitch], pitch odd: conflict-free per-row walks), then
+// Fused preparation of a row-major matrix in one coalesced read, one warp per
+// row: lane l holds columns 128 j + 4 l .. 128 j + 4 l + 3 of every 128-column
+// chunk j < kChunks (float4 loads when rows are 16-byte aligned), kU rows per
+// warp in flight.  Per row, as requested:
 //  * BF16 copy into out[n][dpb] (zero padded) and the "not exactly
-//    representable" flag (*not_exact |= 1), when out / not_exact are given;
+//    representable" flag (*not_exact |= 1);
+//  * integrality and magnitude: int_stats[0] |= 1 when some value is not an
+//    integer, int_stats[1] = max |x| as float bits;
 //  * E4M3 copy into f8[n][f8_bytes] (zero padded) with per-row absmax scales
-//    (scale = max|x| / 448, codes = satfinite(x * 448 / max|x|)), when given;
-//  * row norms into norms[0..n_pad) (+inf for n <= i < n_pad), when given:
-//    the float rounding of the double sum of x_d^2 in d order.  A row of
-//    integers whose float sum stays below 2^24 is summed in float: every
-//    partial sum is then an exact integer, so the result is the same value.
-template <int kRows>
-__global__ void __launch_bounds__(256) prep_rows_kernel(const float* __restrict__ x, int64_t n, int64_t ld, int D,
-                                                        int dpb, __nv_bfloat16* __restrict__ out,
-                                                        float* __restrict__ norms, int64_t n_pad,
-                                                        uint32_t* __restrict__ not_exact,
-                                                        uint32_t* __restrict__ int_stats,
-                                                        uint8_t* __restrict__ f8, int f8_bytes,
-                                                        float* __restrict__ scales)
+//    (scale = max|x| / 448, codes = satfinite(x * 448 / max|x|));
+//  * row norms into norms[0..n_pad) (+inf for n <= i < n_pad): the float
+//    rounding of the double sum of x_d^2 taken in d order (the convention of
+//    norms_kernel and the CPU oracle), certified from a float-float sum -- see
+//    certified_norm -- with the serial double loop for the rare rows the
+//    certificate does not settle.
+struct PrepArgs {
+    const float* x;
+    int64_t n, ld, n_pad;
+    int D, dpb, f8_bytes, vec;
+    __nv_bfloat16* out;
+    float* norms;
+    uint32_t* not_exact;
+    uint32_t* int_stats;
+    uint8_t* f8;
+    float* scales;
+};
+
+// s + t = a + b exactly (Knuth's TwoSum; no contraction: explicit roundings)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& t)
 {
-    extern __shared__ float tile[];
-    const int pitch = D | 1;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t r0 = (int64_t)blockIdx.x * kRows;
-    const int rows = (int)max((int64_t)0, min((int64_t)kRows, n - r0));
-    for (int r = warp; r < rows; r += 8) {
-        const float* src = x + (r0 + r) * ld;
-        for (int c = lane; c < D; c += 32) tile[r * pitch + c] = __ldg(src + c);
-    }
-    __syncthreads();
-    if (int_stats != nullptr) {
-        // integrality and magnitude of the data: int_stats[0] |= 1 when some value is not an
-        // integer, int_stats[1] = max(|x|) as float bits (non-negative floats order as integers)
-        int frac = 0;
-        float mx = 0.f;
-        for (int r = warp; r < rows; r += 8)
-            for (int c = lane; c < D; c += 32) {
-                const float v = tile[r * pitch + c];
-                frac |= !(v == rintf(v));
-                mx = fmaxf(mx, fabsf(v));
-            }
-        frac = __syncthreads_or(frac);
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    t = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Norm of a row from the lanes' float-float partial sums (hi, lo) and e, a sum
+// of the magnitudes of every term folded into lo.  The TwoSums are exact, so
+// S_ff = hi + lo differs from the exact sum S only by the roundings of the lo
+// additions and by residuals of squares below the float range (< 2^-149 each).
+// A lane's chain of 2m lo roundings (m <= 12 elements) errs by at most
+// 2m 2^-24 times its own share of e, and each of the 5 butterfly levels by
+// 2 2^-24 e, so the total stays below 34 2^-24 e (+ D 2^-148) <= 2^-18 e + D 2^-148
+// (e itself is within 2^-14 of the true magnitude sum).  The d-order double sum differs from S by at most
+// D 2^-52 S.  When [S_ff - B, S_ff + B] (B the sum of both bounds) lies
+// strictly inside the rounding interval of f = fl(S_ff), the double sum rounds
+// to f as well; otherwise the caller recomputes the row in double.
+__device__ __forceinline__ bool certified_norm(float hi, float lo, float e, int D, float& f)
+{
+    f = __fadd_rn(hi, lo);
+    if (!(f >= 0x1p-100f && f <= 0x1p126f)) return false;  // also rejects nan
+    const float r = __fadd_rn(__fsub_rn(hi, f), lo);        // hi - f exact (Sterbenz)
+    const float B = e * 0x1p-18f + (float)D * 0x1p-52f * 1.01f * (hi + fabsf(lo) + e) + 0x1p-139f;
+    const float h = 0.5f * (f - nextafterf(f, 0.f));         // half spacing below f (<= the one above)
+    return fabsf(r) * 1.0001f + B < h;
+}
+
+template <int kChunks, int kU>
+__global__ void __launch_bounds__(256) prep_rows_kernel(const PrepArgs p)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int D = p.D;
+    int frac = 0, bad = 0;
+    float mx_all = 0.f;
+    for (int64_t base = gw * kU; base < p.n; base += nw * kU) {
+        float v[kU][kChunks][4];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if (lane == 0) atomicMax(int_stats + 1, __float_as_uint(mx));
-        if (threadIdx.x == 0 && frac) atomicOr(int_stats, 1u);
-    }
-    if (out != nullptr || not_exact != nullptr) {
-        int bad = 0;
-        for (int r = warp; r < rows; r += 8) {
-            for (int c = 2 * lane; c < dpb; c += 64) {
-                const float v0 = c < D ? tile[r * pitch + c] : 0.f;
-                const float v1 = c + 1 < D ? tile[r * pitch + c + 1] : 0.f;
-                const __nv_bfloat162 b = __floats2bfloat162_rn(v0, v1);
-                if (out) *reinterpret_cast<__nv_bfloat162*>(out + (r0 + r) * dpb + c) = b;
-                bad |= !(__low2float(b) == v0) | !(__high2float(b) == v1);
-            }
-        }
-        bad = __syncthreads_or(bad);
-        if (threadIdx.x == 0 && bad && not_exact) atomicOr(not_exact, 1u);
-    }
-    if (f8 != nullptr) {
-        for (int r = warp; r < rows; r += 8) {
-            const float* row = tile + r * pitch;
-            float mx = 0.f;
-            for (int c = lane; c < D; c += 32) mx = fmaxf(mx, fabsf(row[c]));
+        for (int u = 0; u < kU; ++u) {
+            const int64_t r = base + u;
+            const float* row = p.x + (r < p.n ? r : 0) * p.ld;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-            const float inv = mx > 0.f ? 448.f / mx : 0.f;
-            uint32_t* dst = reinterpret_cast<uint32_t*>(f8 + (r0 + r) * (int64_t)f8_bytes);
-            for (int c = 4 * lane; c < f8_bytes; c += 128) {
-                float v[4];
+            for (int j = 0; j < kChunks; ++j) {
+                const int c = 128 * j + 4 * lane;
+                if (p.vec) {
+                    float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (r < p.n && c < D) t = __ldg(reinterpret_cast<const float4*>(row + c));
+                    v[u][j][0] = t.x;
+                    v[u][j][1] = t.y;
+                    v[u][j][2] = t.z;
+                    v[u][j][3] = t.w;
+                } else {
 #pragma unroll
-                for (int j = 0; j < 4; ++j) v[j] = c + j < D ? row[c + j] * inv : 0.f;
-                const uint32_t lo = __nv_cvt_float2_to_fp8x2(make_float2(v[0], v[1]), __NV_SATFINITE, __NV_E4M3);
-                const uint32_t hi = __nv_cvt_float2_to_fp8x2(make_float2(v[2], v[3]), __NV_SATFINITE, __NV_E4M3);
-                dst[c >> 2] = lo | (hi << 16);
-            }
-            if (lane == 0) scales[r0 + r] = mx / 448.f;
-        }
-        for (int r = rows + (int)threadIdx.x; r < kRows && r0 + r < n_pad; r += blockDim.x) scales[r0 + r] = 0.f;
-    }
-    if (norms != nullptr && threadIdx.x < kRows) {
-        const int64_t i = r0 + threadIdx.x;
-        if (i < n) {
-            const float* row = tile + threadIdx.x * pitch;
-            float s32 = 0.f;
-            bool ints = true;
-            for (int d = 0; d < D; ++d) {
-                const float v = row[d];
-                ints &= v == rintf(v);
-                s32 = __fmaf_rn(v, v, s32);
-            }
-            if (!(ints && s32 < 16777216.f)) {
-                double acc = 0.0;
-                for (int d = 0; d < D; ++d) {
-                    const double v = (double)row[d];
-                    acc = __fma_rn(v, v, acc);
+                    for (int i = 0; i < 4; ++i) v[u][j][i] = (r < p.n && c + i < D) ? __ldg(row + c + i) : 0.f;
                 }
-                s32 = __double2float_rn(acc);
             }
-            norms[i] = s32;
-        } else if (i < n_pad) {
-            norms[i] = __int_as_float(0x7f800000);
         }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const int64_t r = base + u;
+            if (r >= p.n) break;  // warp-uniform
+            float mx = 0.f;
+            float hi = 0.f, lo = 0.f, e = 0.f;
+#pragma unroll
+            for (int j = 0; j < kChunks; ++j)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const float x = v[u][j][i];  // zero past D
+                    frac |= !(x == rintf(x));
+                    mx = fmaxf(mx, fabsf(x));
+                    const float q = __fmul_rn(x, x);
+                    const float qe = __fmaf_rn(x, x, -q);
+                    float s, t;
+                    two_sum(hi, q, s, t);
+                    hi = s;
+                    lo = __fadd_rn(lo, __fadd_rn(t, qe));
+                    e = __fadd_rn(e, __fadd_rn(fabsf(t), fabsf(qe)));
+                }
+            if (p.out != nullptr || p.not_exact != nullptr) {
+#pragma unroll
+                for (int j = 0; j < kChunks; ++j) {
+                    const int c = 128 * j + 4 * lane;
+                    const __nv_bfloat162 b0 = __floats2bfloat162_rn(v[u][j][0], v[u][j][1]);
+                    const __nv_bfloat162 b1 = __floats2bfloat162_rn(v[u][j][2], v[u][j][3]);
+                    bad |= !(__low2float(b0) == v[u][j][0]) | !(__high2float(b0) == v[u][j][1]) |
+                           !(__low2float(b1) == v[u][j][2]) | !(__high2float(b1) == v[u][j][3]);
+                    if (p.out != nullptr && c < p.dpb) {
+                        uint2 w;
+                        w.x = *reinterpret_cast<const uint32_t*>(&b0);
+                        w.y = *reinterpret_cast<const uint32_t*>(&b1);
+                        *reinterpret_cast<uint2*>(p.out + r * p.dpb + c) = w;
+                    }
+                }
+            }
+            if (p.f8 != nullptr || p.int_stats != nullptr) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+                mx_all = fmaxf(mx_all, mx);
+            }
+            if (p.f8 != nullptr) {
+                const float inv = mx > 0.f ? 448.f / mx : 0.f;
+                uint32_t* dst = reinterpret_cast<uint32_t*>(p.f8 + r * (int64_t)p.f8_bytes);
+#pragma unroll
+                for (int j = 0; j < kChunks; ++j) {
+                    const int c = 128 * j + 4 * lane;
+                    if (c < p.f8_bytes) {
+                        const uint32_t a = __nv_cvt_float2_to_fp8x2(make_float2(v[u][j][0] * inv, v[u][j][1] * inv),
+                                                                    __NV_SATFINITE, __NV_E4M3);
+                        const uint32_t b = __nv_cvt_float2_to_fp8x2(make_float2(v[u][j][2] * inv, v[u][j][3] * inv),
+                                                                    __NV_SATFINITE, __NV_E4M3);
+                        dst[c >> 2] = a | (b << 16);
+                    }
+                }
+                if (lane == 0) p.scales[r] = mx / 448.f;
+            }
+            if (p.norms != nullptr) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+                    const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+                    const float oe = __shfl_xor_sync(0xffffffffu, e, o);
+                    float s, t;
+                    two_sum(hi, oh, s, t);
+                    hi = s;
+                    lo = __fadd_rn(__fadd_rn(lo, ol), t);
+                    e = __fadd_rn(__fadd_rn(e, oe), fabsf(t));
+                }
+                // every lane holds the same values (the butterfly adds in commutative pairs)
+                float f;
+                bool ok = certified_norm(hi, lo, e, D, f);
+                if (!ok && hi == 0.f && e == 0.f) {
+                    // all squares zero: an all-zero row has norm 0; tiny values go the slow way
+                    float m2 = mx;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+                    ok = m2 == 0.f;
+                    f = 0.f;
+                }
+                if (lane == 0) {
+                    if (!ok) {
+                        const float* row = p.x + r * p.ld;
+                        double acc = 0.0;
+                        for (int d = 0; d < D; ++d) {
+                            const double a = (double)__ldg(row + d);
+                            acc = __fma_rn(a, a, acc);
+                        }
+                        f = __double2float_rn(acc);
+                    }
+                    p.norms[r] = f;
+                }
+            }
+        }
+    }
+    // padding rows past n
+    for (int64_t i = p.n + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.n_pad;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        if (p.norms) p.norms[i] = __int_as_float(0x7f800000);
+        if (p.scales) p.scales[i] = 0.f;
+    }
+    // flags: one atomic per warp
+    if (p.not_exact != nullptr && __any_sync(0xffffffffu, bad) && lane == 0) atomicOr(p.not_exact, 1u);
+    if (p.int_stats != nullptr) {
+        if (__any_sync(0xffffffffu, frac) && lane == 0) atomicOr(p.int_stats, 1u);
+        if (lane == 0 && mx_all > 0.f) atomicMax(p.int_stats + 1, __float_as_uint(mx_all));
     }
 }
 
@@ -226,10 +316,12 @@ cudaError_t launch_prep_rows(const float* x, int64_t n, int64_t ld, int D, int d
 {
     const int64_t rows = std::max(n, (norms || scales) ? n_pad : n);
     if (rows <= 0) return cudaSuccess;
-    const int pitch = D | 1;
     if (f8 != nullptr && (D > kPrepMaxD || scales == nullptr || f8_bytes % 128 != 0 || f8_bytes < D))
         return cudaErrorInvalidValue;
-    uint8_t* f8b = static_cast<uint8_t*>(f8);
+    // the kernel covers ceil(D / 128) chunks of 128 columns (or bytes)
+    const int span = (D + 127) / 128 * 128;
+    if (out != nullptr && (dpb % 64 != 0 || dpb < D || (D <= kPrepMaxD && dpb > span))) return cudaErrorInvalidValue;
+    if (f8 != nullptr && f8_bytes > span) return cudaErrorInvalidValue;
     if (D > kPrepMaxD) {
         // wide rows: separate passes
         cudaError_t e = cudaSuccess;
@@ -238,23 +330,31 @@ cudaError_t launch_prep_rows(const float* x, int64_t n, int64_t ld, int D, int d
         if (e == cudaSuccess && int_stats) e = cudaMemsetAsync(int_stats, 0xFF, sizeof(uint32_t), s);  // unknown
         return e;
     }
-    if (D <= 128) {
-        const size_t smem = (size_t)128 * pitch * 4;
-        cudaError_t e = cudaFuncSetAttribute(prep_rows_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-        if (e != cudaSuccess) return e;
-        prep_rows_kernel<128><<<(unsigned)((rows + 127) / 128), 256, smem, s>>>(
-            x, n, ld, D, dpb, static_cast<__nv_bfloat16*>(out), norms, n_pad, not_exact, int_stats, f8b, f8_bytes,
-            scales);
-    } else {
-        const size_t smem = (size_t)64 * pitch * 4;
-        cudaError_t e = cudaFuncSetAttribute(prep_rows_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-        if (e != cudaSuccess) return e;
-        prep_rows_kernel<64><<<(unsigned)((rows + 63) / 64), 256, smem, s>>>(
-            x, n, ld, D, dpb, static_cast<__nv_bfloat16*>(out), norms, n_pad, not_exact, int_stats, f8b, f8_bytes,
-            scales);
-    }
+    PrepArgs a;
+    a.x = x;
+    a.n = n;
+    a.ld = ld;
+    a.n_pad = std::max(n, n_pad);
+    a.D = D;
+    a.dpb = dpb;
+    a.f8_bytes = f8_bytes;
+    a.vec = (ld % 4 == 0 && D % 4 == 0 && (reinterpret_cast<uintptr_t>(x) & 15u) == 0) ? 1 : 0;
+    a.out = static_cast<__nv_bfloat16*>(out);
+    a.norms = norms;
+    a.not_exact = not_exact;
+    a.int_stats = int_stats;
+    a.f8 = static_cast<uint8_t*>(f8);
+    a.scales = scales;
+    auto blocks = [&](int ku) {
+        const int64_t b = (rows + 8 * ku - 1) / (8 * ku);
+        return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, 16384));
+    };
+    if (D <= 128)
+        prep_rows_kernel<1, 4><<<blocks(4), 256, 0, s>>>(a);
+    else if (D <= 256)
+        prep_rows_kernel<2, 2><<<blocks(2), 256, 0, s>>>(a);
+    else
+        prep_rows_kernel<3, 1><<<blocks(1), 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -35,6 +35,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_UNSUPPORTED, ERR_DEVICE_TIMEOUT, ERR_NOMEM = rang
 # Every symbol include/knn_gb300.h and include/cuknns.h declare.
 EXPORTED = ["knns_default_options", "knns_search_device", "knns_search_host", "knns_check_device",
             "knns_last_error", "knns_last_stats", "knns_version", "knns_debug_tc_dot_tile",
+            "knns_debug_prep",
             "knns_timing_collect", "knns_timing_collect5", "knns_search_device_noalloc",
             "knns_index_create", "knns_index_search", "knns_index_destroy", "knns_autotune_shortlist",
             "knns_server_default_config", "knns_server_create", "knns_server_submit", "knns_server_wait",
@@ -102,6 +103,7 @@ def lib():
     L.knns_last_error.restype = ctypes.c_char_p
     L.knns_last_stats.argtypes = [ctypes.POINTER(Stats)]
     L.knns_debug_tc_dot_tile.argtypes = [vp, i64, vp, i64, ci, vp]
+    L.knns_debug_prep.argtypes = [vp, i64, i64, ci, vp, vp, vp, vp, vp]
     L.knns_timing_collect.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
     L.knns_timing_collect5.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
     L.knns_search_device_noalloc.argtypes = [vp, i64, i64, vp, i64, i64, ci, ci, vp, vp, vp]
@@ -223,6 +225,21 @@ def search_host(corpus, queries, k, *, algo=ALGO_AUTO, splits=0, rerank=True, kp
     _check(lib().knns_search_host(corpus.ctypes.data, N, queries.ctypes.data, Q, D, k, dist.ctypes.data,
                                   idx.ctypes.data, ctypes.byref(o)))
     return dist, idx
+
+
+def debug_prep(x):
+    """Preparation pass over a device matrix: (norms, bf16 copy, E4M3 codes, scales, words), all torch tensors."""
+    import torch
+    n, D = x.shape
+    dev = x.device
+    norms = torch.empty(n, dtype=torch.float32, device=dev)
+    bf = torch.empty((n, (D + 63) // 64 * 64), dtype=torch.bfloat16, device=dev)
+    f8 = torch.empty((n, (D + 127) // 128 * 128), dtype=torch.uint8, device=dev)
+    scales = torch.empty(n, dtype=torch.float32, device=dev)
+    words = torch.zeros(3, dtype=torch.int32, device=dev)
+    _check(lib().knns_debug_prep(x.data_ptr(), n, x.stride(0), D, norms.data_ptr(), bf.data_ptr(), f8.data_ptr(),
+                                 scales.data_ptr(), words.data_ptr()))
+    return norms, bf, f8, scales, words
 
 
 def debug_tc_dot_tile(corpus, queries):
