@@ -157,16 +157,20 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& t)
 // 2 2^-24 e, so the total stays below 34 2^-24 e (+ D 2^-148) <= 2^-18 e + D 2^-148
 // (e itself is within 2^-14 of the true magnitude sum).  The d-order double sum differs from S by at most
 // D 2^-52 S.  When [S_ff - B, S_ff + B] (B the sum of both bounds) lies
-// strictly inside the rounding interval of f = fl(S_ff), the double sum rounds
-// to f as well; otherwise the caller recomputes the row in double.
+// strictly inside the rounding interval of f = fl(S_ff) -- half the spacing
+// below f on one side, half the spacing above on the other (they differ at
+// powers of two) -- the double sum rounds to f as well; otherwise the caller
+// recomputes the row in double.
 __device__ __forceinline__ bool certified_norm(float hi, float lo, float e, int D, float& f)
 {
     f = __fadd_rn(hi, lo);
     if (!(f >= 0x1p-100f && f <= 0x1p126f)) return false;  // also rejects nan
-    const float r = __fadd_rn(__fsub_rn(hi, f), lo);        // hi - f exact (Sterbenz)
+    const float r = __fadd_rn(__fsub_rn(hi, f), lo);        // S_ff - f: hi - f exact (Sterbenz)
     const float B = e * 0x1p-18f + (float)D * 0x1p-52f * 1.01f * (hi + fabsf(lo) + e) + 0x1p-139f;
-    const float h = 0.5f * (f - nextafterf(f, 0.f));         // half spacing below f (<= the one above)
-    return fabsf(r) * 1.0001f + B < h;
+    const float rr = fabsf(r) * 0.0001f;                      // rounding of r itself
+    const float h_dn = 0.5f * (f - nextafterf(f, 0.f));
+    const float h_up = 0.5f * (nextafterf(f, 0x1p127f) - f);
+    return r + rr + B < h_up && r - rr - B > -h_dn;
 }
 
 template <int kChunks, int kU>

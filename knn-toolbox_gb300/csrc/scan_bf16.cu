@@ -25,12 +25,17 @@
 // Clusters of two CTAs (neighbouring query tiles, same corpus split) share
 // every corpus tile: each CTA loads half of each box's rows with a multicast
 // TMA into both, and each MMA commit releases the slot in both.
-// Warp roles (576 threads):
+// Warp roles (608 threads):
 //   warp 0      producer: per tile its half of the corpus K-boxes (2-D TMA
 //               multicast, 64 bf16 x TN/2 rows, 128-byte swizzle) and the
 //               corpus norms (1-D bulk copy);
-//   warp 1      TMEM owner (512 columns) and single-thread MMA issuer
-//               (tcgen05.mma kind::f16, A from TMEM, B from shared memory);
+//   warp 1      TMEM owner (512 columns) and MMA issuer of the even tiles
+//               (tcgen05.mma kind::f16 / kind::f8f6f4, A from TMEM, B from
+//               shared memory) into accumulator 0;
+//   warp 18     MMA issuer of the odd tiles into accumulator 1.  The tensor
+//               pipe queues little work ahead of the instruction being issued,
+//               so with one issuer every barrier wait and commit of that thread
+//               idled it; two issuers overlap one's waits with the other's MMAs;
 //   warps 2..17 epilogue: thread = query (TMEM lane); warps 2..5 first write
 //               the queries into TMEM; warps 2+4p..5+4p (p = 0..3) read a
 //               quarter of each tile's columns as a 32-column chunk and a
@@ -53,7 +58,8 @@ namespace knn {
 
 namespace {
 constexpr int kEpiWarps = 4 * kScanParts;  // 4 TMEM lane quarters x kScanParts column ranges
-constexpr int kScanThreads = 32 * (2 + kEpiWarps);
+constexpr int kIssuers = 2;                 // MMA issuing threads (warps 1 and 2 + kEpiWarps)
+constexpr int kScanThreads = 32 * (1 + kIssuers + kEpiWarps);
 constexpr int kNormSlots = 8;
 // CTAs per cluster: the cluster's CTAs work on neighbouring query tiles of the
 // same corpus split; each TMA-loads 1/kCluster of every corpus box's rows and
@@ -217,7 +223,7 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads,
             ptx::mbar_init(&s.nempty[b], kEpiWarps);
         }
         ptx::mbar_init(s.aready, 4);
-        ptx::mbar_init(s.drain, 1);
+        ptx::mbar_init(s.drain, kIssuers);
         *s.abort = 0;
         ptx::fence_mbar_init();
         ptx::tma_prefetch_desc(&a.tm_c);
@@ -270,19 +276,22 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads,
                 for (int j = first; j < it; ++j) ptx::mbar_wait(&s.full[j % R], (uint32_t)(j / R) & 1u, kTimeoutNs);
             }
         }
-    } else if (warp == 1) {
-        // ------------------------------------------------------------ MMA issuer
+    } else if (warp == 1 || warp == 2 + kEpiWarps) {
+        // ------------------------------------------------------------ MMA issuers
+        // issuer i takes the tiles t = i (mod 2), i.e. accumulator i; each commit
+        // tracks only its own thread's MMAs
         if (lane == 0) {
+            const int iss = warp == 1 ? 0 : 1;
             bool ok = scan_wait(a, s, s.aready, 0, kDevTimeoutAload);
             ptx::tc_fence_after();
             const uint32_t a_tmem = tmem + kACol;
-            int it = 0;
-            for (int t = 0; t < ntiles && ok; ++t) {
+            for (int t = iss; t < ntiles && ok; t += kIssuers) {
                 const int b = t & 1;
                 const uint32_t use = (uint32_t)(t >> 1);
                 if (!scan_wait(a, s, &s.acce[b], (use & 1u) ^ 1u, kDevTimeoutMma)) { ok = false; break; }
                 ptx::tc_fence_after();
                 const uint32_t d_tmem = tmem + (uint32_t)b * TN;
+                int it = t * slots_per_tile;
                 for (int c = 0; c < slots_per_tile; ++c, ++it) {
                     const int st = it % R;
                     const uint32_t ph = (uint32_t)(it / R) & 1u;
