@@ -47,6 +47,9 @@ WORKLOADS = {
     "aniso8m": dict(desc="anisotropic Gaussian corpus 8,000,000 x 256 (coordinate j ~ N(0, 1/sqrt(1+j))), "
                          "16,384 queries, k=32, seed 3",
                     gen="anisotropic", N=8_000_000, D=256, Q=16_384, k=32, seed=3),
+    # profiling-sized cut of aniso8m for ncu captures of the E4M3 scan (corpus still larger than L2)
+    "aniso1m": dict(desc="anisotropic Gaussian corpus 1,000,000 x 256, 4,096 queries, k=32, seed 3",
+                    gen="anisotropic", N=1_000_000, D=256, Q=4_096, k=32, seed=3),
     # profiling cut of int1m: full corpus (same candidate density per corpus row), a quarter of the queries
     "int1m_q2500": dict(desc="int-descriptor corpus 1,000,000 x 128, 2,500 queries, k=100, seed 1",
                         gen="int_descriptor", N=1_000_000, D=128, Q=2_500, k=100, seed=1),

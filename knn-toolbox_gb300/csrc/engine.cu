@@ -278,17 +278,22 @@ int resolve_config(const Engine& E, int64_t N, int64_t Q, int D, int k, const kn
 // Seeding: the main scan needs, per query, a threshold T with at least kp keys
 // below it (then every top-kp candidate is collected) and few more.  Nested
 // corpus samples give it, coarse to fine: level l keeps every stride_l-th row
-// (stride 16 for the finest level, 16x more per coarser level, the coarsest
-// small enough to keep every key).  Each level collects the keys below the
-// previous level's threshold and picks the key of rank j_l as its own.  With
+// (stride kSeedStride for the finest level, 16x more per coarser level, the
+// coarsest small enough to keep every key).  Each level collects the keys below
+// the previous level's threshold and picks the key of rank j_l as its own.  With
 // m = j_next / 16 (the expected rank, in this level's sample, of the key of
-// rank j_next in the next one; m = kp / 16 for the finest level)
+// rank j_next in the next one; m = kp / kSeedStride for the finest level)
 // j = 2m + 4 sqrt(m) + 1 leaves a chance of roughly 1e-5 that fewer than j_next
 // keys fall below the threshold at the next level.  Queries for which that
 // happens in the main pass (and any whose segments overflow) are found by the
 // selection and searched again without a threshold, so results never depend
 // on the seeds.
 constexpr int kMaxSeedLevels = 6;
+// Finest sampling stride: a coarser sample makes seeding cheaper and the main
+// pass collect more candidates (about 2 kp + 4 sqrt(kp * stride) per query);
+// 32 gave the lowest seeding + scan + selection time on the 1M x 128 and the
+// 4M x 96 workloads (16 and 64 were each slower on one of them).
+constexpr int64_t kSeedStride = 32;
 
 struct ScanLevel {
     int64_t n = 0, stride = 1, len = 0, n_pad = 0;
@@ -321,10 +326,11 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
                          dpb, o.scan_boxes);
     const int64_t qt = cdiv(cdiv(Q, kTileQ), 2) * 2;  // query tiles, padded to whole CTA pairs
     const int tn = scan_tile_rows(dpb);
-    // levels, finest first: strides 16, 256, ... until the sample fits the selector whole
+    // levels, finest first: strides kSeedStride, 16 kSeedStride, ... until the sample fits
+    // the selector whole
     int64_t st[kMaxSeedLevels];
     int L = 0;
-    for (int64_t stride = 16;; stride *= 16) {
+    for (int64_t stride = kSeedStride;; stride *= 16) {
         if (L == kMaxSeedLevels) return set_error(KNNS_ERR_UNSUPPORTED, "threshold scan: corpus too large to seed");
         st[L++] = stride;
         if (cdiv(N, stride) <= kCandMax / 2) break;
@@ -338,7 +344,7 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
         v.n_pad = cdiv(v.n, kScanTileN) * kScanTileN + kScanTileN;  // >= one tile past the view
     }
     // ranks, finest to coarsest
-    double m = (double)kp / 16.0;
+    double m = (double)kp / (double)kSeedStride;
     for (int l = L - 1; l >= 0; --l) {
         ScanLevel& v = P->lv[l];
         v.j = std::min<int>((int)v.n, seed_rank(m));

@@ -74,13 +74,6 @@ __device__ __forceinline__ void tma_prefetch_desc(const CUtensorMap* m)
     asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)m) : "memory");
 }
 
-// L2 prefetch of a tensor-map box (no shared memory, no completion)
-__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* m, int x, int y)
-{
-    asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"((uint64_t)m), "r"(x), "r"(y)
-                 : "memory");
-}
-
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* m, uint64_t* bar, int x, int y)
 {
     asm volatile(

@@ -85,13 +85,14 @@ def test_duplicate_rows_overflow_and_fixup(engine, oracle, Q):
 
 
 def test_unrepresentative_sample_fixup(engine, oracle):
-    # Only every 16th row (the seeding sample) lies near the queries, so the
-    # seeded threshold admits fewer than kp rows and the fix-up must take over.
+    # Only every 32nd row (exactly the finest seeding sample) lies near the
+    # queries, so the seeded threshold admits fewer than kp rows and the fix-up
+    # must take over.
     rng = np.random.default_rng(78)
-    N, D, Q, k = 16 * 8192, 64, 150, 10
+    N, D, Q, k = 32 * 4096, 64, 150, 10
     Qs = rng.integers(0, 32, (Q, D)).astype(np.float32)
     X = rng.integers(200, 256, (N, D)).astype(np.float32)
-    near = np.arange(0, N, 16)
+    near = np.arange(0, N, 32)
     X[near] = Qs[rng.integers(0, Q, near.size)] + rng.integers(0, 2, (near.size, D)).astype(np.float32)
     d, i, st = run(engine, X, Qs, k)
     assert st["scan"] == 1
