@@ -65,7 +65,11 @@ typedef struct knns_options {
     int shortlist;   /* BF16 / FP8 forms: shortlist factor c, kp = c*k rounded up to 16 (0 = 4) */
     int scan;        /* KNNS_SCAN_* (default AUTO) */
     int scan_boxes;  /* threshold scan: 64-element K boxes per shared-memory ring slot (0 = automatic) */
-    int reserved[4];
+    int block_rows;  /* host-buffer searches (knns_search_host, gpuknnsBitonic / gpuknnsHeap): corpus rows
+                        per device block; 0 = automatic: the whole corpus when it fits in free device memory,
+                        else blocks sized to it.  Each block is searched and merged into the running top-k
+                        by (distance, index): results are identical to one search over the whole corpus */
+    int reserved[3];
 } knns_options;
 
 typedef struct knns_stats {

@@ -920,6 +920,77 @@ int check_device_error(Engine& E, cudaStream_t s)
     return KNNS_OK;
 }
 
+// Corpus rows per device block of a host-buffer search: the requested count, or
+// (requested 0) the whole corpus when its copies fit in about 60 % of the free
+// device memory (the engine's own cached corpus buffers counted as free), else as
+// many rows as do, rounded down to 4096.  0 when not even k rows fit.
+static int64_t host_block_rows(Engine& E, int64_t N, int64_t Q, int D, int k, int requested)
+{
+    if (requested > 0) return std::max<int64_t>(std::min<int64_t>(requested, N), std::min<int64_t>(k, N));
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return N;
+    const double avail = 0.6 * (double)(fr + E.in_corpus.cap + E.bf.cap + E.hi.cap + E.lo.cap + E.cn.cap);
+    // FP32 input, BF16 copy, TF32 hi/lo, norms and flags per row; query-side workspace
+    const double per_row = (double)D * (4 + 2 + 8) + 32;
+    const double fixed = (double)Q * ((double)D * 8 + 8192) + 256.0 * (1 << 20);
+    const double rows = (avail - fixed) / per_row;
+    if (rows >= (double)N) return N;
+    const int64_t r = (int64_t)rows / 4096 * 4096;
+    return r >= k ? r : 0;
+}
+
+// Host-buffer search over a corpus streamed in blocks of br rows: each block is
+// copied, searched for its top-min(k, rows) and merged into the running top-k
+// (src/cuknnBitonic.cu:550-589).  Per-pair arithmetic does not depend on the
+// blocking, so the result is the one search over the whole corpus gives.
+static int search_host_blocked(Engine& E, cudaStream_t s, const float* corpus, int64_t N, const float* queries,
+                               int64_t Q, int D, int k, float* dist, int32_t* idx, float* idx_f_host,
+                               const knns_options& o, int64_t br, double* seconds, knns_stats* st)
+{
+    if (N > 0x7fffffffLL) return set_error(KNNS_ERR_UNSUPPORTED, "corpus larger than 2^31-1 rows");
+    const size_t qb = (size_t)Q * D * sizeof(float), ob = (size_t)Q * k;
+    int rc = E.in_corpus.ensure((size_t)br * D * sizeof(float));
+    if (!rc) rc = E.in_queries.ensure(std::max(qb, (size_t)4));
+    if (!rc) rc = E.out_dist.ensure(std::max(ob * 4, (size_t)4));
+    if (!rc) rc = E.out_idx.ensure(std::max(ob * 4, (size_t)4));
+    if (!rc) rc = E.mrg.ensure(std::max(ob * 20, (size_t)20));
+    if (rc) return rc;
+    // two running lists (distances, indices) and the float indices of the drop-in output
+    float* rd[2] = {(float*)E.mrg.p, (float*)E.mrg.p + ob};
+    int32_t* ri[2] = {(int32_t*)E.mrg.p + 2 * ob, (int32_t*)E.mrg.p + 3 * ob};
+    float* fidx = (float*)E.mrg.p + 4 * ob;
+    cudaEvent_t t0 = E.t0(), t1 = E.t1();
+    KNN_CUDA(cudaEventRecord(t0, s));
+    if (qb) KNN_CUDA(cudaMemcpyAsync(E.in_queries.p, queries, qb, cudaMemcpyHostToDevice, s));
+    int have = 0, cur = 0;
+    for (int64_t b0 = 0; b0 < N; b0 += br) {
+        const int64_t nb = std::min<int64_t>(br, N - b0);
+        const int kb = (int)std::min<int64_t>(k, nb);
+        KNN_CUDA(cudaMemcpyAsync(E.in_corpus.p, corpus + b0 * D, (size_t)nb * D * sizeof(float),
+                                 cudaMemcpyHostToDevice, s));
+        rc = run_search(E, (const float*)E.in_corpus.p, nb, D, (const float*)E.in_queries.p, Q, D, D, kb,
+                        (float*)E.out_dist.p, (int32_t*)E.out_idx.p, nullptr, o, s, st);
+        if (rc) return rc;
+        const bool last = b0 + nb >= N;
+        KNN_CUDA(launch_merge_topk(rd[cur], ri[cur], have, (const float*)E.out_dist.p, (const int32_t*)E.out_idx.p,
+                                   kb, (int32_t)b0, Q, k, rd[cur ^ 1], ri[cur ^ 1],
+                                   (last && idx_f_host) ? fidx : nullptr, s));
+        have = (int)std::min<int64_t>(k, have + kb);
+        cur ^= 1;
+    }
+    // the final lists: rd[cur], ri[cur]; float indices (drop-in) in fidx
+    if (dist && ob) KNN_CUDA(cudaMemcpyAsync(dist, rd[cur], ob * 4, cudaMemcpyDeviceToHost, s));
+    if (idx && ob) KNN_CUDA(cudaMemcpyAsync(idx, ri[cur], ob * 4, cudaMemcpyDeviceToHost, s));
+    if (idx_f_host && ob) KNN_CUDA(cudaMemcpyAsync(idx_f_host, fidx, ob * 4, cudaMemcpyDeviceToHost, s));
+    KNN_CUDA(cudaEventRecord(t1, s));
+    rc = check_device_error(E, s);
+    if (rc) return rc;
+    float ms = 0.f;
+    KNN_CUDA(cudaEventElapsedTime(&ms, t0, t1));
+    if (seconds) *seconds = ms / 1000.0;
+    return KNNS_OK;
+}
+
 int search_host(const float* corpus, int64_t N, const float* queries, int64_t Q, int D, int k, float* dist,
                 int32_t* idx, float* idx_f_host, const knns_options& o, double* seconds, knns_stats* st)
 {
@@ -931,6 +1002,11 @@ int search_host(const float* corpus, int64_t N, const float* queries, int64_t Q,
     std::lock_guard<std::mutex> lk(E->mu);
     cudaStream_t s = E->host_stream();
     if (!s) return set_error(KNNS_ERR_CUDA, "stream creation failed");
+    if (k > N) return set_error(KNNS_ERR_INVALID, "k=%d exceeds the corpus size N=%lld", k, (long long)N);
+    if (o.block_rows < 0) return set_error(KNNS_ERR_INVALID, "negative block_rows");
+    const int64_t br = host_block_rows(*E, N, Q, D, k, o.block_rows);
+    if (br <= 0) return set_error(KNNS_ERR_NOMEM, "no corpus block of at least %d rows fits in device memory", k);
+    if (br < N) return search_host_blocked(*E, s, corpus, N, queries, Q, D, k, dist, idx, idx_f_host, o, br, seconds, st);
     const size_t cb = (size_t)N * D * sizeof(float), qb = (size_t)Q * D * sizeof(float);
     const size_t ob = (size_t)Q * k;
     if ((rc = E->in_corpus.ensure(cb))) return rc;

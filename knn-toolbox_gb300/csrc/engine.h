@@ -51,6 +51,8 @@ struct Engine {
     // queries not BF16-exact, [2] some value not an integer, [3] max |x| (float bits), [4] zero
     DevBuf words;
     DevBuf in_corpus, in_queries, out_dist, out_idx;
+    // corpus blocks of host-buffer searches: two running top-k lists (distances, indices)
+    DevBuf mrg;
     // stage timing: kTimingEvents events per timed search (start, after prep,
     // after threshold seeding, after the main fused kernel, after the main
     // selection, end)

@@ -211,6 +211,12 @@ struct CandSelect {
 };
 cudaError_t launch_select_cand(const CandSelect& c, cudaStream_t s);
 
+// Running top-k (have entries, row pitch k) merged with a block's top-kb (pitch kb,
+// indices + offset) into out (pitch k, min(k, have + kb) entries); out_idx_f optional.
+cudaError_t launch_merge_topk(const float* run_d, const int32_t* run_i, int have, const float* blk_d,
+                              const int32_t* blk_i, int kb, int32_t offset, int64_t Q, int k, float* out_d,
+                              int32_t* out_i, float* out_idx_f, cudaStream_t s);
+
 // out[i] = src[i * stride] for i < n, +inf for n <= i < n_pad (norms of a strided corpus sample).
 // out[i] = src[i * stride] for i < n, pad for n <= i < n_pad (+inf: norms of padding rows)
 cudaError_t launch_gather_norms(const float* src, int64_t n, int64_t stride, float* out, int64_t n_pad,

@@ -402,6 +402,59 @@ cudaError_t launch_select(const uint64_t* part, int splits, int64_t Q, int kp, i
     return cudaGetLastError();
 }
 
+// Merge of a corpus block's top-kb into the running top-k of every query (the
+// reference's cross-block merge of its host-streamed corpus blocks,
+// src/cuknnBitonic.cu:550-589, done on the device): both lists are sorted by
+// (distance, index); block indices are shifted by the block's first row; the
+// first min(k, have + kb) entries of the union in (distance, index) order go to
+// the output list (and, as floats, to out_idx_f when given).  One thread per query.
+__global__ void merge_topk_kernel(const float* __restrict__ run_d, const int32_t* __restrict__ run_i, int have,
+                                  const float* __restrict__ blk_d, const int32_t* __restrict__ blk_i, int kb,
+                                  int32_t offset, int64_t Q, int k, float* __restrict__ out_d,
+                                  int32_t* __restrict__ out_i, float* __restrict__ out_idx_f)
+{
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= Q) return;
+    const float* rd = run_d + q * k;
+    const int32_t* ri = run_i + q * k;
+    const float* bd = blk_d + q * kb;
+    const int32_t* bi = blk_i + q * kb;
+    const int n = min(k, have + kb);
+    int a = 0, b = 0;
+    for (int j = 0; j < n; ++j) {
+        bool take_a;
+        if (a >= have) {
+            take_a = false;
+        } else if (b >= kb) {
+            take_a = true;
+        } else {
+            const float da = rd[a], db = bd[b];
+            const int32_t ia = ri[a], ib = bi[b] + offset;
+            take_a = da < db || (da == db && ia < ib);
+        }
+        const float d = take_a ? rd[a] : bd[b];
+        const int32_t i = take_a ? ri[a] : bi[b] + offset;
+        a += take_a ? 1 : 0;
+        b += take_a ? 0 : 1;
+        out_d[q * k + j] = d;
+        out_i[q * k + j] = i;
+        if (out_idx_f) out_idx_f[q * k + j] = (float)i;
+    }
+}
+
+cudaError_t launch_merge_topk(const float* run_d, const int32_t* run_i, int have, const float* blk_d,
+                              const int32_t* blk_i, int kb, int32_t offset, int64_t Q, int k, float* out_d,
+                              int32_t* out_i, float* out_idx_f, cudaStream_t s)
+{
+    if (Q <= 0) return cudaSuccess;
+    if (k < 1 || kb < 0 || kb > k || have < 0 || have > k || (have > 0 && (!run_d || !run_i)) || !out_d || !out_i ||
+        (kb > 0 && (!blk_d || !blk_i)))
+        return cudaErrorInvalidValue;
+    merge_topk_kernel<<<(unsigned)((Q + 127) / 128), 128, 0, s>>>(run_d, run_i, have, blk_d, blk_i, kb, offset, Q, k,
+                                                                  out_d, out_i, out_idx_f);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_select_cand(const CandSelect& c, cudaStream_t s)
 {
     if (c.Q <= 0) return cudaSuccess;

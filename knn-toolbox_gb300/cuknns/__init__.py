@@ -53,7 +53,7 @@ class Options(ctypes.Structure):
     _fields_ = [("algo", ctypes.c_int), ("splits", ctypes.c_int), ("rerank", ctypes.c_int),
                 ("kp", ctypes.c_int), ("timing", ctypes.c_int), ("pilot", ctypes.c_int),
                 ("precision", ctypes.c_int), ("shortlist", ctypes.c_int), ("scan", ctypes.c_int),
-                ("scan_boxes", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
+                ("scan_boxes", ctypes.c_int), ("block_rows", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
 
 
 class Stats(ctypes.Structure):
@@ -145,7 +145,7 @@ def _check(rc):
 
 
 def options(algo=ALGO_AUTO, splits=0, rerank=True, kp=0, timing=False, pilot=True, precision=PREC_EXACT,
-            shortlist=0, scan=SCAN_AUTO, scan_boxes=0) -> Options:
+            shortlist=0, scan=SCAN_AUTO, scan_boxes=0, block_rows=0) -> Options:
     o = Options()
     lib().knns_default_options(ctypes.byref(o))
     o.algo, o.splits, o.rerank, o.kp = int(algo), int(splits), int(bool(rerank)), int(kp)
@@ -153,6 +153,7 @@ def options(algo=ALGO_AUTO, splits=0, rerank=True, kp=0, timing=False, pilot=Tru
     o.pilot = int(bool(pilot))
     o.precision, o.shortlist = int(precision), int(shortlist)
     o.scan, o.scan_boxes = int(scan), int(scan_boxes)
+    o.block_rows = int(block_rows)
     return o
 
 
