@@ -148,25 +148,27 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& t)
     t = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
-// Norm of a row from the lanes' float-float partial sums (hi, lo) and e, a sum
-// of the magnitudes of every term folded into lo.  The TwoSums are exact, so
-// S_ff = hi + lo differs from the exact sum S only by the roundings of the lo
-// additions and by residuals of squares below the float range (< 2^-149 each).
-// A lane's chain of 2m lo roundings (m <= 12 elements) errs by at most
-// 2m 2^-24 times its own share of e, and each of the 5 butterfly levels by
-// 2 2^-24 e, so the total stays below 34 2^-24 e (+ D 2^-148) <= 2^-18 e + D 2^-148
-// (e itself is within 2^-14 of the true magnitude sum).  The d-order double sum differs from S by at most
-// D 2^-52 S.  When [S_ff - B, S_ff + B] (B the sum of both bounds) lies
-// strictly inside the rounding interval of f = fl(S_ff) -- half the spacing
-// below f on one side, half the spacing above on the other (they differ at
-// powers of two) -- the double sum rounds to f as well; otherwise the caller
-// recomputes the row in double.
-__device__ __forceinline__ bool certified_norm(float hi, float lo, float e, int D, float& f)
+// Norm of a row from the lanes' float-float partial sums (hi, lo).  The TwoSums
+// are exact, so S_ff = hi + lo differs from the exact sum S only by the roundings
+// of the lo additions and by residuals of squares below the float range
+// (< 2^-149 each).  Every term folded into lo is at most 2^-24 of a partial sum:
+// a lane's TwoSum residuals total at most m 2^-24 of its share of S (m <= 12
+// elements), its square residuals 2^-24 of it, and the 31 butterfly TwoSums 2^-24 S
+// each, so the terms total E <= 44 2^-24 S.  A lane's 2m lo roundings err by at
+// most 2^-24 of its share of E each and the 5 butterfly levels by 2 2^-24 E, so
+// |S_ff - S| <= 34 2^-24 E + D 2^-149 < 2^-36 S + D 2^-149.  The double d-order sum
+// differs from S by at most D 2^-52 S.  When [S_ff - B, S_ff + B] (B the sum of
+// both bounds, S bounded by 1.01 (hi + |lo|)) lies strictly inside the rounding
+// interval of f = fl(S_ff) -- half the spacing below f on one side, half the
+// spacing above on the other (they differ at powers of two) -- the double sum
+// rounds to f as well; otherwise the caller recomputes the row in double.
+__device__ __forceinline__ bool certified_norm(float hi, float lo, int D, float& f)
 {
     f = __fadd_rn(hi, lo);
     if (!(f >= 0x1p-100f && f <= 0x1p126f)) return false;  // also rejects nan
     const float r = __fadd_rn(__fsub_rn(hi, f), lo);        // S_ff - f: hi - f exact (Sterbenz)
-    const float B = e * 0x1p-18f + (float)D * 0x1p-52f * 1.01f * (hi + fabsf(lo) + e) + 0x1p-139f;
+    const float S = 1.01f * (hi + fabsf(lo));
+    const float B = (0x1p-36f + (float)D * 0x1p-52f) * S + 0x1p-139f;
     const float rr = fabsf(r) * 0.0001f;                      // rounding of r itself
     const float h_dn = 0.5f * (f - nextafterf(f, 0.f));
     const float h_up = 0.5f * (nextafterf(f, 0x1p127f) - f);
@@ -209,22 +211,16 @@ __global__ void __launch_bounds__(256) prep_rows_kernel(const PrepArgs p)
             const int64_t r = base + u;
             if (r >= p.n) break;  // warp-uniform
             float mx = 0.f;
-            float hi = 0.f, lo = 0.f, e = 0.f;
+            int rfrac = 0;
 #pragma unroll
             for (int j = 0; j < kChunks; ++j)
 #pragma unroll
                 for (int i = 0; i < 4; ++i) {
                     const float x = v[u][j][i];  // zero past D
-                    frac |= !(x == rintf(x));
+                    rfrac |= !(x == rintf(x));
                     mx = fmaxf(mx, fabsf(x));
-                    const float q = __fmul_rn(x, x);
-                    const float qe = __fmaf_rn(x, x, -q);
-                    float s, t;
-                    two_sum(hi, q, s, t);
-                    hi = s;
-                    lo = __fadd_rn(lo, __fadd_rn(t, qe));
-                    e = __fadd_rn(e, __fadd_rn(fabsf(t), fabsf(qe)));
                 }
+            frac |= rfrac;
             if (p.out != nullptr || p.not_exact != nullptr) {
 #pragma unroll
                 for (int j = 0; j < kChunks; ++j) {
@@ -241,11 +237,10 @@ __global__ void __launch_bounds__(256) prep_rows_kernel(const PrepArgs p)
                     }
                 }
             }
-            if (p.f8 != nullptr || p.int_stats != nullptr) {
+            // the row's max |x| (E4M3 scale, int_stats, the integer test of the norm)
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-                mx_all = fmaxf(mx_all, mx);
-            }
+            for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            mx_all = fmaxf(mx_all, mx);
             if (p.f8 != nullptr) {
                 const float inv = mx > 0.f ? 448.f / mx : 0.f;
                 uint32_t* dst = reinterpret_cast<uint32_t*>(p.f8 + r * (int64_t)p.f8_bytes);
@@ -263,27 +258,49 @@ __global__ void __launch_bounds__(256) prep_rows_kernel(const PrepArgs p)
                 if (lane == 0) p.scales[r] = mx / 448.f;
             }
             if (p.norms != nullptr) {
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
-                    const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
-                    const float oe = __shfl_xor_sync(0xffffffffu, e, o);
-                    float s, t;
-                    two_sum(hi, oh, s, t);
-                    hi = s;
-                    lo = __fadd_rn(__fadd_rn(lo, ol), t);
-                    e = __fadd_rn(__fadd_rn(e, oe), fabsf(t));
-                }
-                // every lane holds the same values (the butterfly adds in commutative pairs)
                 float f;
-                bool ok = certified_norm(hi, lo, e, D, f);
-                if (!ok && hi == 0.f && e == 0.f) {
-                    // all squares zero: an all-zero row has norm 0; tiny values go the slow way
-                    float m2 = mx;
+                bool ok;
+                if (!__any_sync(0xffffffffu, rfrac) && (float)D * mx * mx < 16777216.f) {
+                    // integers whose squares sum below 2^24: every partial sum is an exact
+                    // integer, so any order gives the double sum's value
+                    float s32 = 0.f;
 #pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, o));
-                    ok = m2 == 0.f;
-                    f = 0.f;
+                    for (int j = 0; j < kChunks; ++j)
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) s32 = __fmaf_rn(v[u][j][i], v[u][j][i], s32);
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) s32 = __fadd_rn(s32, __shfl_xor_sync(0xffffffffu, s32, o));
+                    f = s32;
+                    ok = true;
+                } else {
+                    float hi = 0.f, lo = 0.f;
+#pragma unroll
+                    for (int j = 0; j < kChunks; ++j)
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            const float x = v[u][j][i];
+                            const float q = __fmul_rn(x, x);
+                            const float qe = __fmaf_rn(x, x, -q);
+                            float sum, t;
+                            two_sum(hi, q, sum, t);
+                            hi = sum;
+                            lo = __fadd_rn(lo, __fadd_rn(t, qe));
+                        }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+                        const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+                        float sum, t;
+                        two_sum(hi, oh, sum, t);
+                        hi = sum;
+                        lo = __fadd_rn(__fadd_rn(lo, ol), t);
+                    }
+                    // every lane holds the same values (the butterfly adds in commutative pairs)
+                    ok = certified_norm(hi, lo, D, f);
+                    if (!ok && mx == 0.f) {  // an all-zero row
+                        ok = true;
+                        f = 0.f;
+                    }
                 }
                 if (lane == 0) {
                     if (!ok) {
