@@ -39,7 +39,8 @@ def exact_codes(n, d, rng):
 
 
 @pytest.mark.parametrize("N,D,Q,k,c", [(150_000, 256, 257, 32, 2), (140_000, 64, 130, 10, 4),
-                                       (131_072, 200, 64, 16, 2), (40_000, 128, 300, 1, 8)])
+                                       (131_072, 200, 64, 16, 2), (40_000, 128, 300, 1, 8),
+                                       (131_077, 8, 1, 1, 2), (17_001, 37, 33, 64, 2)])
 def test_exact_codes_match_exact_form(engine, oracle, N, D, Q, k, c):
     rng = np.random.default_rng(N + D)
     X, Qs = exact_codes(N, D, rng), exact_codes(Q, D, rng)
