@@ -7,11 +7,13 @@ clip(round(|N(0,40)|),0,255) with 8% of each row's coordinates zeroed,
 search of the whole query batch against the whole corpus.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload int1m|uniform64k]
+                    [--workload int1m|uniform64k|mix4m|aniso8m|serve2m|...]
+                    [--precision exact|bf16|fp8] [--shortlist C]
 
 Prints one JSON line (rank 0).  `value` is queries/s with the corpus and the
 queries resident in HBM; `e2e` is the same metric through the drop-in C ABI
-(gpuknnsBitonic) from pinned host buffers, host<->device copies included.
+(gpuknnsBitonic; knns_search_host for the precision forms) from pinned host
+buffers, host<->device copies included.
 `--impl reference` times the reference's CPU path (demo/knn.m, restated in C
 in oracle/knn_oracle.c) on the host cores on a bounded query sample.
 """
@@ -67,6 +69,17 @@ def gen_data(w, rank=0):
     if rank:
         _, queries = fn(w["Q"], w["D"], seed=w["seed"] + 1000 * rank, nq=w["Q"])
     return corpus, queries
+
+
+def reduce_max(x, dist, device):
+    """Max of a float over the ranks (dist = torch.distributed or None; device = where the
+    backend's tensors live: the rank's GPU for NCCL, the CPU for gloo)."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def measured_peaks():
@@ -241,10 +254,7 @@ def run_e2e(corpus_np, queries_np, k, Q, world, steps, barrier, dist, dev, prec_
     for _ in range(steps):
         vals, idxf = call()
     e2e_s = (time.perf_counter() - t0) / steps
-    if dist is not None:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = reduce_max(e2e_s, dist, dev)
     return {"value": Q * world / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": int(hc.nbytes + hq.nbytes),
             "d2h_bytes_per_step": int(vals.nbytes + idxf.nbytes), "api": api,
             "host_buffers": "pinned inputs, pageable outputs", "steps": steps}
@@ -317,10 +327,7 @@ def run_gb300(args, w):
     rc = cuknns.lib().knns_check_device(None)
     if rc != 0:
         raise RuntimeError(cuknns.last_error())
-    if dist is not None:
-        t = torch.tensor([el_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        el_ms = float(t.item())
+    el_ms = reduce_max(el_ms, dist, dev)
     value = Q * args.steps * world / (el_ms / 1e3)
 
     # ---- accuracy against the FP64 oracle on a query sample
