@@ -311,6 +311,27 @@ struct ScanPlan {
     size_t cand_words = 0, cnt_words = 0, part_words = 0, norm_words = 0;
 };
 
+// Split count of a seeding pass: few tiles per CTA, so each CTA's fixed cost (setup, the
+// queries into tensor memory, the first corpus copies, the drain; about 8 tiles' worth)
+// counts beside the waves x tiles of auto_splits.  (The main pass keeps auto_splits: there
+// the model moved it to more splits, a slower scan and a slower selection.)
+static int seed_splits(int64_t qtiles, int64_t tiles, int sms, int max_splits)
+{
+    constexpr double kFixedTiles = 8.0;
+    int best = 1;
+    double best_cost = 1e300;
+    const int lim = (int)std::min<int64_t>(tiles, max_splits);
+    for (int S = 1; S <= lim; ++S) {
+        const double waves = (double)cdiv(qtiles * S, sms);
+        const double cost = waves * ((double)cdiv(tiles, S) + kFixedTiles);
+        if (cost < best_cost - 1e-9) {
+            best_cost = cost;
+            best = S;
+        }
+    }
+    return best;
+}
+
 static int seg_cap(double per_seg, double sigmas)
 {
     return round16((int)std::ceil(sigmas * per_seg + 8.0 * std::sqrt(per_seg) + 16.0));
@@ -365,7 +386,7 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
             v.S = (int)cdiv(v.n, v.len);
             v.cap = (int)(v.len / kScanParts);
         } else {
-            v.S = auto_splits(qt, tiles, E.sms, kScanMaxSegs / kScanParts);
+            v.S = seed_splits(qt, tiles, E.sms, kScanMaxSegs / kScanParts);
             v.len = cdiv(tiles, v.S) * tn;
             v.S = (int)cdiv(v.n, v.len);
             const double hits = (double)P->lv[l - 1].j * (double)v.n / (double)P->lv[l - 1].n;
