@@ -208,6 +208,7 @@ struct CandSelect {
     // re-rank is then skipped (distance = key + qn[q], the same value it would compute)
     const uint32_t* int_stats = nullptr;  // [0] not-integer flag, [1] max|x| bits (corpus and queries)
     const uint32_t* bf16_inexact = nullptr;
+    int buf_words = 0;  // set by launch_select_cand: per-warp candidate buffer of this launch
 };
 cudaError_t launch_select_cand(const CandSelect& c, cudaStream_t s);
 

@@ -12,6 +12,7 @@
 //               re-sorted by (distance, index) and the first k are returned;
 //   rerank = 0: the first k by GEMM-form key are returned with
 //               distance = key + ||q||^2 (the reference's output contract).
+#include <algorithm>
 #include <cstdint>
 #include <cuda_runtime.h>
 #include "common.cuh"
@@ -142,9 +143,9 @@ __host__ __device__ inline int cand_stage_rows(int D) { return D <= 128 ? 32 : 1
 // candidate words a warp can hold: threshold mode (seeding passes) and result mode
 constexpr int kCandThrMax = 1024;
 
-__host__ __device__ inline size_t cand_warp_bytes(int D, bool thr_mode, bool rerank)
+__host__ __device__ inline size_t cand_warp_bytes(int D, bool thr_mode, bool rerank, int buf_words)
 {
-    const size_t sel = (size_t)(thr_mode ? kCandThrMax : kCandMax) * 8;
+    const size_t sel = (size_t)buf_words * 8;
     const size_t rr = rerank && !thr_mode ? (size_t)kMaxKpTC * 8 + (size_t)cand_stage_rows(D) * (D + 1) * 4 : 0;
     const size_t w = sel > rr ? sel : rr;
     return (w + 15) & ~(size_t)15;
@@ -245,8 +246,8 @@ __global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandS
     extern __shared__ __align__(16) unsigned char smem[];
     if (c.skip_if != nullptr && *c.skip_if != 0u) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const size_t wb = cand_warp_bytes(c.D, kThr, c.rerank != 0);
-    const int buf_max = kThr ? kCandThrMax : kCandMax;
+    const size_t wb = cand_warp_bytes(c.D, kThr, c.rerank != 0, c.buf_words);
+    const int buf_max = c.buf_words;
     uint64_t* buf = reinterpret_cast<uint64_t*>(smem + (size_t)warp * wb);
     float* qv = reinterpret_cast<float*>(smem + (size_t)kSelWarps * wb) + (size_t)warp * ((c.D + 3) & ~3);
     const int64_t q = (int64_t)blockIdx.x * kSelWarps + warp;
@@ -455,16 +456,20 @@ cudaError_t launch_merge_topk(const float* run_d, const int32_t* run_i, int have
     return cudaGetLastError();
 }
 
-cudaError_t launch_select_cand(const CandSelect& c, cudaStream_t s)
+cudaError_t launch_select_cand(const CandSelect& c_in, cudaStream_t s)
 {
-    if (c.Q <= 0) return cudaSuccess;
+    if (c_in.Q <= 0) return cudaSuccess;
+    CandSelect c = c_in;
     const bool thr = c.thr_out != nullptr;
+    // threshold mode: a query stores at most nseg * cap words, often far fewer than the
+    // buffer's limit at the coarse seeding levels; a smaller buffer lets more warps run
+    c.buf_words = thr ? (int)std::min<int64_t>(kCandThrMax, ((int64_t)c.nseg * c.cap + 31) / 32 * 32) : kCandMax;
     if (c.nseg < 1 || c.nseg > kScanMaxSegs || c.cap < 1 ||
         (!thr && (c.kp < 1 || c.kp > kMaxKpTC || c.k > c.kp || c.fail_idx == nullptr || c.fail_cnt == nullptr ||
                   (!c.rerank && c.qn == nullptr))) ||
         (thr && (c.thr_rank < 1 || c.thr_rank > kCandThrMax)))
         return cudaErrorInvalidValue;
-    const size_t smem = (size_t)kSelWarps * cand_warp_bytes(c.D, thr, c.rerank != 0) +
+    const size_t smem = (size_t)kSelWarps * cand_warp_bytes(c.D, thr, c.rerank != 0, c.buf_words) +
                         (size_t)kSelWarps * ((c.D + 3) & ~3) * 4;
     const unsigned blocks = (unsigned)((c.Q + kSelWarps - 1) / kSelWarps);
     cudaError_t e;
