@@ -158,20 +158,23 @@ __device__ __forceinline__ uint64_t raw_to_ordered(uint64_t w)
 }
 
 // number of words w[0..n) (shared memory) not above x, summed over the warp
-__device__ __forceinline__ uint32_t count_not_above_u64(const uint64_t* w, int n, uint64_t x)
+// Radix-4 step of the rank search: the counts of values not above y0 < y1 < y2 in one
+// pass (n <= 65,535, so two counts share a 32-bit reduction), and the 2-bit digit d of the
+// rank-th smallest value: the number of thresholds with fewer than `rank` values not
+// above them.  Half the dependent rounds of a bitwise search.
+template <typename V, typename F>
+__device__ __forceinline__ uint32_t radix4_digit(const uint64_t* w, int n, V y0, V y1, V y2, uint32_t rank, F val)
 {
     const int lane = threadIdx.x & 31;
-    uint32_t c = 0;
-    for (int e = lane; e < n; e += 32) c += w[e] <= x ? 1u : 0u;
-    return __reduce_add_sync(0xffffffffu, c);
-}
-
-__device__ __forceinline__ uint32_t count_key_not_above(const uint64_t* w, int n, uint32_t x)
-{
-    const int lane = threadIdx.x & 31;
-    uint32_t c = 0;
-    for (int e = lane; e < n; e += 32) c += (uint32_t)(w[e] >> 32) <= x ? 1u : 0u;
-    return __reduce_add_sync(0xffffffffu, c);
+    uint32_t a = 0, b = 0;
+    for (int e = lane; e < n; e += 32) {
+        const V v = val(w[e]);
+        a += (v <= y0 ? 1u : 0u) + (v <= y1 ? 0x10000u : 0u);
+        b += v <= y2 ? 1u : 0u;
+    }
+    a = __reduce_add_sync(0xffffffffu, a);
+    b = __reduce_add_sync(0xffffffffu, b);
+    return ((a & 0xffffu) < rank ? 1u : 0u) + ((a >> 16) < rank ? 1u : 0u) + (b < rank ? 1u : 0u);
 }
 
 // Exact distances of cur[0..kp) (direct difference, oracle order: eight partial
@@ -311,11 +314,15 @@ __global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandS
     const int n = (int)total;
 
     if (kThr) {
-        // smallest key x with at least thr_rank keys not above it (bitwise binary search)
+        // smallest key x with at least thr_rank keys not above it (radix-4 search, two bits
+        // per round: x's digit at bits [b0, b0 + 2) is the number of the thresholds
+        // x | d 2^b0 | (2^b0 - 1), d = 0, 1, 2, with fewer than thr_rank keys not above them)
         uint32_t x = 0;
-        for (int bit = 31; bit >= 0; --bit) {
-            const uint32_t y = x | ((1u << bit) - 1u);  // x with the lower bits set
-            if (count_key_not_above(buf, n, y) < (uint32_t)c.thr_rank) x |= 1u << bit;
+        for (int b0 = 30; b0 >= 0; b0 -= 2) {
+            const uint32_t low = (1u << b0) - 1u;
+            const uint32_t d = radix4_digit(buf, n, x | low, x | (1u << b0) | low, x | (2u << b0) | low,
+                                            (uint32_t)c.thr_rank, [](uint64_t v) { return (uint32_t)(v >> 32); });
+            x |= d << b0;
         }
         if (lane == 0) {
             const float key = ord2f(x);
@@ -330,9 +337,12 @@ __global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandS
     uint64_t W = kSentinel;
     if (n > kp) {
         uint64_t x = 0;
-        for (int bit = 63; bit >= 0; --bit) {
-            const uint64_t y = x | ((1ull << bit) - 1ull);
-            if (count_not_above_u64(buf, n, y) < (uint32_t)kp) x |= 1ull << bit;
+        for (int b0 = 62; b0 >= 0; b0 -= 2) {
+            const uint64_t low = (uint64_t(1) << b0) - 1u;
+            const uint64_t d = radix4_digit(buf, n, x | low, x | (uint64_t(1) << b0) | low,
+                                            x | (uint64_t(2) << b0) | low, (uint32_t)kp,
+                                            [](uint64_t v) { return v; });
+            x |= d << b0;
         }
         W = x;
     }
