@@ -39,9 +39,11 @@
 //   warps 2..17 epilogue: thread = query (TMEM lane); warps 2..5 first write
 //               the queries into TMEM; warps 2+4p..5+4p (p = 0..3) read a
 //               quarter of each tile's columns as a 32-column chunk and a
-//               tail (16 + 8 columns for TN = 224, 16 for 192): per chunk
-//               tcgen05.ld, packed fma, the minima of its 8-column groups,
-//               one vote; only groups holding a key below some lane's
+//               tail (16 + 8 columns for TN = 224, 16 for 192): all three
+//               tcgen05.ld in flight at once, one wait, the accumulator released
+//               (its round trip to the issuers is what the pipeline waits on),
+//               then per chunk packed fma in place, the minima of its 8-column
+//               groups, one vote; only groups holding a key below some lane's
 //               threshold are appended.
 // Every mbarrier wait is bounded; on timeout the kernel records an error code
 // in the device error word and winds down without hanging the GPU.
@@ -370,29 +372,27 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads,
             const uint32_t tb = tmem + (uint32_t)b * TN + lane_base;
             const uint32_t nb = (uint32_t)(n_begin + (int64_t)t * TN);
             const int c32 = 32 * part, c16 = 128 + 16 * part, c8 = 192 + 8 * part;
+            // all three loads in flight together, one wait, then the accumulator is released:
+            // the MMA may overwrite it while the keys are formed (in place) and tested
             float va[32], v16[16], v8[8];
             __syncwarp();
             ptx::tmem_ld32(tb + (uint32_t)c32, va);
-            ptx::tmem_wait_ld_regs(va);
-            __syncwarp();
             ptx::tmem_ld16(tb + (uint32_t)c16, v16);
             if (TW == 24) ptx::tmem_ld8(tb + (uint32_t)c8, v8);
-            float key[32];
-            const uint32_t ga = chunk_keys<32, kF8>(va, nrm + c32, scl + c32, m, T, key);
             ptx::tmem_wait_ld();
+            ptx::tie_regs(va);
             ptx::tie_regs(v16);
             if (TW == 24) ptx::tie_regs(v8);
-            // accumulator b fully read: the MMA may overwrite it while the keys are tested
             ptx::tc_fence_before();
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&s.acce[b]);
-            if (__any_sync(0xffffffffu, ga != 0u)) chunk_append<32>(key, ga, T, nb + (uint32_t)c32, out, cap, cnt);
-            float k16[16], k8[8];
-            const uint32_t g16 = chunk_keys<16, kF8>(v16, nrm + c16, scl + c16, m, T, k16);
-            const uint32_t g8 = TW == 24 ? chunk_keys<8, kF8>(v8, nrm + c8, scl + c8, m, T, k8) : 0u;
+            const uint32_t ga = chunk_keys<32, kF8>(va, nrm + c32, scl + c32, m, T, va);
+            if (__any_sync(0xffffffffu, ga != 0u)) chunk_append<32>(va, ga, T, nb + (uint32_t)c32, out, cap, cnt);
+            const uint32_t g16 = chunk_keys<16, kF8>(v16, nrm + c16, scl + c16, m, T, v16);
+            const uint32_t g8 = TW == 24 ? chunk_keys<8, kF8>(v8, nrm + c8, scl + c8, m, T, v8) : 0u;
             if (__any_sync(0xffffffffu, (g16 | g8) != 0u)) {
-                chunk_append<16>(k16, g16, T, nb + (uint32_t)c16, out, cap, cnt);
-                if (TW == 24) chunk_append<8>(k8, g8, T, nb + (uint32_t)c8, out, cap, cnt);
+                chunk_append<16>(v16, g16, T, nb + (uint32_t)c16, out, cap, cnt);
+                if (TW == 24) chunk_append<8>(v8, g8, T, nb + (uint32_t)c8, out, cap, cnt);
             }
             // norm slot ns fully read
             __syncwarp();
