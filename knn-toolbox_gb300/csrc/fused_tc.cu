@@ -117,6 +117,8 @@ __device__ __forceinline__ void tc_fail(const TcArgs& a, const TcSmem& s, int co
 
 __device__ __forceinline__ bool tc_wait(const TcArgs& a, const TcSmem& s, uint64_t* bar, uint32_t parity, int code)
 {
+    // a completed barrier returns before the abort flag is read; a wait that would block sees it first
+    if (ptx::mbar_try_wait(bar, parity)) return true;
     if (*s.abort) return false;
     if (ptx::mbar_wait(bar, parity, kTimeoutNs)) return true;
     tc_fail(a, s, code);
@@ -343,10 +345,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
                             if (a_lo) ptx::mma_tf32_ts(d_tmem, alo, dh, kIdesc, 1u);
                         }
                     }
+                    // after the tile's last MMAs the accumulator-ready commit goes first
+                    if (c == nchunks - 1) ptx::mma_commit(&s.accf[b]);
                     ptx::mma_commit(&s.empty[st]);
                 }
                 if (!ok) break;
-                ptx::mma_commit(&s.accf[b]);
             }
             // all MMAs issued by this thread retire before TMEM is released
             ptx::mma_commit(s.drain);

@@ -97,6 +97,9 @@ struct ScanSmem {
 __device__ __forceinline__ bool scan_wait(const ScanArgs& a, const ScanSmem& s, uint64_t* bar, uint32_t parity,
                                           int code)
 {
+    // a completed barrier returns before the abort flag is read (the flag costs a shared
+    // load on every hand-off otherwise); a wait that would block sees it first
+    if (ptx::mbar_try_wait(bar, parity)) return true;
     if (*s.abort) return false;
     if (ptx::mbar_wait(bar, parity, kTimeoutNs)) return true;
     atomicCAS(a.err, 0, code);
@@ -314,11 +317,13 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads,
                                                  (box | kk) != 0);
                         }
                     }
+                    // after the tile's last MMAs the accumulator-ready commit goes first: the
+                    // epilogue is on the critical path, the producer has the ring's slack
+                    if (c == slots_per_tile - 1) ptx::mma_commit(&s.accf[b]);
                     // the slot is free once every CTA of the cluster has consumed it
                     ptx::mma_commit_mc(&s.empty[st], kClusterMask);
                 }
                 if (!ok) break;
-                ptx::mma_commit(&s.accf[b]);
             }
             // all MMAs issued by this thread retire before TMEM is released
             ptx::mma_commit(s.drain);
