@@ -117,6 +117,11 @@ const char *knns_last_error(void);
 /* Statistics of the calling thread's last successful search. */
 int knns_last_stats(knns_stats *out);
 
+/* Queries of the calling thread's last threshold-scan search that overflowed
+ * their candidate segments and were answered by the fix-up pass (0 when the
+ * scan did not run).  Diagnostic: synchronises the device. */
+int knns_last_fixups(int64_t *out);
+
 /*
  * Stage timings of the searches run with opt->timing = 1 since the last
  * collection, from CUDA events recorded on each search's stream:

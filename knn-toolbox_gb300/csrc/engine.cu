@@ -347,6 +347,7 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
                          dpb, o.scan_boxes);
     const int64_t qt = cdiv(cdiv(Q, kTileQ), 2) * 2;  // query tiles, padded to whole CTA pairs
     const int tn = scan_tile_rows(dpb);
+    const int pc = scan_part_cols(dpb);  // segment columns per tile (the parts are not all equal)
     // levels, finest first: strides kSeedStride, 16 kSeedStride, ... until the sample fits
     // the selector whole
     int64_t st[kMaxSeedLevels];
@@ -384,13 +385,13 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
             v.S = (int)std::min<int64_t>(2, tiles);
             v.len = cdiv(tiles, v.S) * tn;
             v.S = (int)cdiv(v.n, v.len);
-            v.cap = (int)(v.len / kScanParts);
+            v.cap = (int)(v.len / tn * pc);
         } else {
             v.S = seed_splits(qt, tiles, E.sms, kScanMaxSegs / kScanParts);
             v.len = cdiv(tiles, v.S) * tn;
             v.S = (int)cdiv(v.n, v.len);
             const double hits = (double)P->lv[l - 1].j * (double)v.n / (double)P->lv[l - 1].n;
-            v.cap = std::min<int>((int)(v.len / kScanParts), seg_cap(hits / ((double)kScanParts * v.S), 3.0));
+            v.cap = std::min<int>((int)(v.len / tn * pc), seg_cap(hits * pc / ((double)tn * v.S), 3.0));
         }
         P->cand_words = std::max(P->cand_words, (size_t)kScanParts * v.S * Q * v.cap);
         P->cnt_words = std::max(P->cnt_words, (size_t)kScanParts * v.S * Q);
@@ -404,7 +405,7 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
     P->len = cdiv(tiles, P->S) * tn;
     P->S = (int)cdiv(N, P->len);
     const double hm = (double)P->lv[L - 1].j * (double)P->lv[L - 1].stride;
-    P->cap = std::min<int>((int)(P->len / kScanParts), seg_cap(hm / ((double)kScanParts * P->S), 2.0));
+    P->cap = std::min<int>((int)(P->len / tn * pc), seg_cap(hm * pc / ((double)tn * P->S), 2.0));
     P->cand_words = std::max(P->cand_words, (size_t)kScanParts * P->S * Q * P->cap);
     P->cnt_words = std::max(P->cnt_words, (size_t)kScanParts * P->S * Q);
     // fix-up of failed queries: up to 512 on a full wave, the rest (rare) on 8 splits
@@ -1161,6 +1162,24 @@ int knns_last_stats(knns_stats* out)
     if (!out) return KNNS_ERR_INVALID;
     if (!g_have_stats) return set_error(KNNS_ERR_INVALID, "no search has completed on this thread");
     *out = g_last_stats;
+    return KNNS_OK;
+}
+
+int knns_last_fixups(int64_t* out)
+{
+    if (!out) return KNNS_ERR_INVALID;
+    if (!g_have_stats) return set_error(KNNS_ERR_INVALID, "no search has completed on this thread");
+    *out = 0;
+    if (!g_last_stats.scan) return KNNS_OK;
+    Engine* E = nullptr;
+    int rc = get_engine(&E);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(E->mu);
+    if (!E->fail.p) return KNNS_OK;
+    uint32_t n = 0;
+    KNN_CUDA(cudaDeviceSynchronize());
+    KNN_CUDA(cudaMemcpy(&n, E->fail.p, sizeof n, cudaMemcpyDeviceToHost));
+    *out = (int64_t)n;
     return KNNS_OK;
 }
 

@@ -133,6 +133,8 @@ struct ScanArgs {
 int scan_tile_rows(int dpb);
 // rows of the corpus tensor map's box: the share of a tile one CTA of a cluster loads
 int scan_box_rows(int dpb);
+// most columns of one tile that a single candidate segment (epilogue part) collects
+int scan_part_cols(int dpb);
 size_t scan_smem_bytes(int dpb, int bps, int ring, bool fp8 = false);
 // Ring geometry for dpb (want_bps = 0: automatic).  Returns 0 on success.
 int scan_plan(int dpb, int want_bps, int* bps, int* ring, bool fp8 = false);

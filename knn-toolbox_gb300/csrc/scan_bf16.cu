@@ -422,6 +422,9 @@ int scan_tile_rows(int dpb) { return dpb <= 128 ? 224 : 192; }
 
 int scan_box_rows(int dpb) { return scan_tile_rows(dpb) / kCluster; }
 
+// every epilogue part collects the same share of a tile's columns
+int scan_part_cols(int dpb) { return scan_tile_rows(dpb) / kScanParts; }
+
 size_t scan_smem_bytes(int dpb, int bps, int ring, bool fp8)
 {
     const int tn = scan_tile_rows(dpb);

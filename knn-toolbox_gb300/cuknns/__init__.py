@@ -34,7 +34,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_UNSUPPORTED, ERR_DEVICE_TIMEOUT, ERR_NOMEM = rang
 
 # Every symbol include/knn_gb300.h and include/cuknns.h declare.
 EXPORTED = ["knns_default_options", "knns_search_device", "knns_search_host", "knns_check_device",
-            "knns_last_error", "knns_last_stats", "knns_version", "knns_debug_tc_dot_tile",
+            "knns_last_error", "knns_last_stats", "knns_last_fixups", "knns_version", "knns_debug_tc_dot_tile",
             "knns_debug_prep",
             "knns_timing_collect", "knns_timing_collect5", "knns_search_device_noalloc",
             "knns_index_create", "knns_index_search", "knns_index_destroy", "knns_autotune_shortlist",
@@ -102,6 +102,7 @@ def lib():
     L.knns_check_device.argtypes = [vp]
     L.knns_last_error.restype = ctypes.c_char_p
     L.knns_last_stats.argtypes = [ctypes.POINTER(Stats)]
+    L.knns_last_fixups.argtypes = [ctypes.POINTER(ctypes.c_int64)]
     L.knns_debug_tc_dot_tile.argtypes = [vp, i64, vp, i64, ci, vp]
     L.knns_debug_prep.argtypes = [vp, i64, i64, ci, vp, vp, vp, vp, vp]
     L.knns_timing_collect.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
@@ -171,6 +172,13 @@ def timing_collect5():
     n = ctypes.c_int(0)
     _check(lib().knns_timing_collect5(ms, ctypes.byref(n)))
     return ms[0], ms[1], ms[2], ms[3], ms[4], n.value
+
+
+def last_fixups() -> int:
+    """Queries of the last threshold-scan search that the fix-up pass answered (synchronises)."""
+    n = ctypes.c_int64(0)
+    _check(lib().knns_last_fixups(ctypes.byref(n)))
+    return n.value
 
 
 def last_stats() -> dict:

@@ -151,3 +151,26 @@ def test_integer_data_exact_and_reranked_keys(engine, oracle, D, hi):
         assert oracle.recall_at_k(i, oracle.knn_f64(X, Qs, k)[1]) >= 0.99
         got64 = oracle.pair_dist_f64(X, Qs, i)
         assert (np.abs(d - got64) <= DIST_REL * got64 + 1e-6).all()
+
+
+@pytest.mark.parametrize("form", ["int128", "mix96_bf16", "mix256_bf16", "aniso128_fp8", "aniso256_fp8"])
+def test_scan_answers_nearly_every_query(engine, form):
+    # the fix-up pass is exact, so a scan whose segments overflow for every query
+    # (wrong keys, segments sized for another column split) passes every parity
+    # test while running several times slower: bound the fix-up count directly
+    import cuknns.synth as S
+    Q = 1000
+    if form == "int128":
+        X, Qs = S.int_descriptor(300_000, 128, seed=3, nq=Q)
+        kw, k = {}, 100
+    elif form.startswith("mix"):
+        X, Qs = S.gauss_mixture(300_000, int(form[3:].split("_")[0]), seed=2, nq=Q)
+        kw, k = dict(precision=engine.PREC_BF16, shortlist=4), 10
+    else:
+        X, Qs = S.anisotropic(300_000, int(form[5:].split("_")[0]), seed=5, nq=Q)
+        kw, k = dict(precision=engine.PREC_FP8, shortlist=2), 32
+    d, i, st = run(engine, X, Qs, k, **kw)
+    assert st["scan"] == 1
+    fix = engine.last_fixups()
+    assert fix <= Q // 100, (form, fix)
+    assert (np.diff(d, axis=1) >= 0).all()
