@@ -306,6 +306,7 @@ struct ScanPlan {
     ScanLevel lv[kMaxSeedLevels];
     int64_t len = 0;
     int S = 1, cap = 0;
+    int sel_words = 0;  // bound on one query's stored main-pass candidates (selection buffer)
     int64_t fixA_rows = 0, fixA_len = 0, fixB_rows = 0, fixB_len = 0;
     int fixA_S = 1, fixB_S = 1;
     size_t cand_words = 0, cnt_words = 0, part_words = 0, norm_words = 0;
@@ -406,6 +407,11 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
     P->S = (int)cdiv(N, P->len);
     const double hm = (double)P->lv[L - 1].j * (double)P->lv[L - 1].stride;
     P->cap = std::min<int>((int)(P->len / tn * pc), seg_cap(hm * pc / ((double)tn * P->S), 2.0));
+    // a query's main-pass count is about stride x (a Gamma(j) variable): hm + 6 stride sqrt(j)
+    // bounds it but for queries whose strided sample misrepresents them (those fail over to
+    // the fix-up either way); the selection buffer is sized to it, not to its ceiling
+    P->sel_words = (int)std::min<double>(
+        (double)kCandMax, std::ceil((hm + 6.0 * (double)P->lv[L - 1].stride * std::sqrt((double)P->lv[L - 1].j) + 64.0) / 32.0) * 32.0);
     P->cand_words = std::max(P->cand_words, (size_t)kScanParts * P->S * Q * P->cap);
     P->cnt_words = std::max(P->cnt_words, (size_t)kScanParts * P->S * Q);
     // fix-up of failed queries: up to 512 on a full wave, the rest (rare) on 8 splits
@@ -813,6 +819,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         cs.kp = c.kp;
         cs.k = k;
         cs.need = (int)std::min<int64_t>(c.kp, N);
+        cs.buf_words = sp.sel_words;
         cs.rerank = c.rerank;
         cs.corpus = corpus;
         cs.ldc = ldc;

@@ -210,7 +210,10 @@ struct CandSelect {
     // re-rank is then skipped (distance = key + qn[q], the same value it would compute)
     const uint32_t* int_stats = nullptr;  // [0] not-integer flag, [1] max|x| bits (corpus and queries)
     const uint32_t* bf16_inexact = nullptr;
-    int buf_words = 0;  // set by launch_select_cand: per-warp candidate buffer of this launch
+    // per-warp candidate buffer (words): result mode takes it as the caller's bound on one
+    // query's stored candidates (0 = kCandMax; a query above it fails over to the fix-up);
+    // threshold mode sets it from nseg * cap
+    int buf_words = 0;
 };
 cudaError_t launch_select_cand(const CandSelect& c, cudaStream_t s);
 

@@ -137,16 +137,19 @@ select_kernel(const uint64_t* __restrict__ part, int splits, int64_t Q, int kp, 
 
 // ---------------------------------------------------------------- threshold-scan selection
 namespace {
-// rows of candidate vectors staged per re-rank batch: [rows][D + 1] floats
-__host__ __device__ inline int cand_stage_rows(int D) { return D <= 128 ? 32 : 16; }
+// rows of candidate vectors staged per re-rank batch: [rows][D + 1] floats (about 8 KB: the
+// staging area sets the warp's shared memory, hence how many queries run per SM)
+__host__ __device__ inline int cand_stage_rows(int D) { return D <= 128 ? 16 : 8; }
 
 // candidate words a warp can hold: threshold mode (seeding passes) and result mode
 constexpr int kCandThrMax = 1024;
 
-__host__ __device__ inline size_t cand_warp_bytes(int D, bool thr_mode, bool rerank, int buf_words)
+// re-rank: the sorted shortlist cur[0, P) (P = pow2_at_least(kp)) then the staged rows
+__host__ __device__ inline size_t cand_warp_bytes(int D, bool thr_mode, bool rerank, int buf_words, int kp)
 {
     const size_t sel = (size_t)buf_words * 8;
-    const size_t rr = rerank && !thr_mode ? (size_t)kMaxKpTC * 8 + (size_t)cand_stage_rows(D) * (D + 1) * 4 : 0;
+    const size_t rr =
+        rerank && !thr_mode ? (size_t)pow2_at_least(kp) * 8 + (size_t)cand_stage_rows(D) * (D + 1) * 4 : 0;
     const size_t w = sel > rr ? sel : rr;
     return (w + 15) & ~(size_t)15;
 }
@@ -249,7 +252,7 @@ __global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandS
     extern __shared__ __align__(16) unsigned char smem[];
     if (c.skip_if != nullptr && *c.skip_if != 0u) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const size_t wb = cand_warp_bytes(c.D, kThr, c.rerank != 0, c.buf_words);
+    const size_t wb = cand_warp_bytes(c.D, kThr, c.rerank != 0, c.buf_words, c.kp);
     const int buf_max = c.buf_words;
     uint64_t* buf = reinterpret_cast<uint64_t*>(smem + (size_t)warp * wb);
     float* qv = reinterpret_cast<float*>(smem + (size_t)kSelWarps * wb) + (size_t)warp * ((c.D + 3) & ~3);
@@ -375,7 +378,7 @@ __global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandS
         const float* qrow = c.queries + q * c.ldq;
         for (int d = lane; d < c.D; d += 32) qv[d] = __ldg(qrow + d);
         __syncwarp();
-        rerank_staged(cur, kp, c.corpus, c.ldc, qv, c.D, reinterpret_cast<float*>(buf + kMaxKpTC));
+        rerank_staged(cur, kp, c.corpus, c.ldc, qv, c.D, reinterpret_cast<float*>(buf + P));
         warp_sort_smem(cur, P);
         for (int j = lane; j < c.k; j += 32) {
             const uint64_t w = cur[j];
@@ -473,13 +476,17 @@ cudaError_t launch_select_cand(const CandSelect& c_in, cudaStream_t s)
     const bool thr = c.thr_out != nullptr;
     // threshold mode: a query stores at most nseg * cap words, often far fewer than the
     // buffer's limit at the coarse seeding levels; a smaller buffer lets more warps run
-    c.buf_words = thr ? (int)std::min<int64_t>(kCandThrMax, ((int64_t)c.nseg * c.cap + 31) / 32 * 32) : kCandMax;
+    if (thr)
+        c.buf_words = (int)std::min<int64_t>(kCandThrMax, ((int64_t)c.nseg * c.cap + 31) / 32 * 32);
+    else if (c.kp >= 1 && c.kp <= kMaxKpTC)
+        c.buf_words = c.buf_words > 0 ? std::min(kCandMax, std::max((c.buf_words + 31) / 32 * 32, pow2_at_least(c.kp)))
+                                      : kCandMax;
     if (c.nseg < 1 || c.nseg > kScanMaxSegs || c.cap < 1 ||
         (!thr && (c.kp < 1 || c.kp > kMaxKpTC || c.k > c.kp || c.fail_idx == nullptr || c.fail_cnt == nullptr ||
                   (!c.rerank && c.qn == nullptr))) ||
         (thr && (c.thr_rank < 1 || c.thr_rank > kCandThrMax)))
         return cudaErrorInvalidValue;
-    const size_t smem = (size_t)kSelWarps * cand_warp_bytes(c.D, thr, c.rerank != 0, c.buf_words) +
+    const size_t smem = (size_t)kSelWarps * cand_warp_bytes(c.D, thr, c.rerank != 0, c.buf_words, c.kp) +
                         (size_t)kSelWarps * ((c.D + 3) & ~3) * 4;
     const unsigned blocks = (unsigned)((c.Q + kSelWarps - 1) / kSelWarps);
     cudaError_t e;
