@@ -294,6 +294,7 @@ __global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandS
     uint32_t base = 0;
 #pragma unroll
     for (int r = 0; r < kSegPerLane; ++r) {
+        if (32 * r >= c.nseg) break;  // warp-uniform: no segments left
         uint32_t pre = n4[r];
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -335,22 +336,40 @@ __global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandS
         return;
     }
 
-    // the kp-th smallest (key, index) word W (words are distinct: indices are)
+    // a bound W on the words kept: every word not above W is kept, the kp smallest (key,
+    // index) words among them (words are distinct: indices are)
     const int kp = c.kp;
+    const int P = pow2_at_least(kp);
     uint64_t W = kSentinel;
     if (n > kp) {
-        uint64_t x = 0;
-        for (int b0 = 62; b0 >= 0; b0 -= 2) {
-            const uint64_t low = (uint64_t(1) << b0) - 1u;
-            const uint64_t d = radix4_digit(buf, n, x | low, x | (uint64_t(1) << b0) | low,
-                                            x | (uint64_t(2) << b0) | low, (uint32_t)kp,
-                                            [](uint64_t v) { return v; });
-            x |= d << b0;
+        // the kp-th smallest key K (16 rounds over the key half); when the words with keys
+        // up to K fit the sort, all of them are kept and the sort orders K's ties by index
+        uint32_t xk = 0;
+        for (int b0 = 30; b0 >= 0; b0 -= 2) {
+            const uint32_t low = (1u << b0) - 1u;
+            const uint32_t d = radix4_digit(buf, n, xk | low, xk | (1u << b0) | low, xk | (2u << b0) | low,
+                                            (uint32_t)kp, [](uint64_t v) { return (uint32_t)(v >> 32); });
+            xk |= d << b0;
         }
-        W = x;
+        uint32_t le = 0;
+        for (int e = lane; e < n; e += 32) le += (uint32_t)(buf[e] >> 32) <= xk ? 1u : 0u;
+        le = __reduce_add_sync(0xffffffffu, le);
+        if (le <= (uint32_t)P) {
+            W = ((uint64_t)xk << 32) | 0xffffffffull;
+        } else {
+            // many ties at K: the kp-th smallest word itself (its key half is K)
+            uint64_t x = (uint64_t)xk << 32;
+            for (int b0 = 30; b0 >= 0; b0 -= 2) {
+                const uint64_t low = (uint64_t(1) << b0) - 1u;
+                const uint64_t d = radix4_digit(buf, n, x | low, x | (uint64_t(1) << b0) | low,
+                                                x | (uint64_t(2) << b0) | low, (uint32_t)kp,
+                                                [](uint64_t v) { return v; });
+                x |= d << b0;
+            }
+            W = x;
+        }
     }
-    // compact the words not above W (at most kp of them) to the front, then sort them
-    const int P = pow2_at_least(kp);
+    // compact the words not above W (at most P of them) to the front, then sort them
     uint64_t* cur = buf;  // in place: the compacted prefix never overtakes the read position
     uint32_t m = 0;
     for (int e0 = 0; e0 < n; e0 += 32) {
@@ -366,6 +385,9 @@ __global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandS
     for (int j = (int)m + lane; j < P; j += 32) cur[j] = kSentinel;
     __syncwarp();
     warp_sort_smem(cur, P);
+    // the shortlist is cur[0, kp): words past it (ties kept above) are dropped
+    for (int j = kp + lane; j < P; j += 32) cur[j] = kSentinel;
+    __syncwarp();
 
     // exact integer keys: the ranking by key is the ranking by distance, distance = key + ||q||^2
     bool exact = false;
