@@ -175,6 +175,69 @@ __device__ __forceinline__ bool certified_norm(float hi, float lo, int D, float&
     return r + rr + B < h_up && r - rr - B > -h_dn;
 }
 
+// (h, l) += (oh, ol) as float-float: exact TwoSum of the high parts, the low parts and
+// the residual added.  Symmetric: both partners of a butterfly step get the same values
+// (the TwoSum residual is the exact error whatever the operand order).
+__device__ __forceinline__ void ff_add(float& h, float& l, float oh, float ol)
+{
+    float s, t;
+    two_sum(h, oh, s, t);
+    h = s;
+    l = __fadd_rn(__fadd_rn(l, ol), t);
+}
+
+// Sums of kU rows' float-float partials over the warp, transposed: the first log2(kU)
+// levels halve the rows a lane holds (it keeps the rows of its half of the warp and
+// receives its partner's partials of them), the remaining levels are a butterfly within
+// groups of 32 / kU lanes.  Each row is still summed by a complete pairwise tree of depth
+// 5 over the 32 lanes' partials (31 exact TwoSums, low parts added along paths of 5
+// levels), so certified_norm's bound holds as for a plain 32-lane butterfly, at a quarter
+// of the shuffles for four rows.  Lane l ends with row l / (32 / kU), identical across
+// its group.
+template <int kU>
+__device__ __forceinline__ void ff_reduce_rows(const float (&hi)[kU], const float (&lo)[kU], int lane, float& h,
+                                               float& l)
+{
+    static_assert(kU == 1 || kU == 2 || kU == 4, "1, 2 or 4 rows per warp");
+    constexpr unsigned kAll = 0xffffffffu;
+    if constexpr (kU == 4) {
+        const bool up = (lane & 16) != 0;  // keeps rows 2, 3 (else 0, 1)
+        float h0 = up ? hi[2] : hi[0], l0 = up ? lo[2] : lo[0];
+        float h1 = up ? hi[3] : hi[1], l1 = up ? lo[3] : lo[1];
+        const float s0h = up ? hi[0] : hi[2], s0l = up ? lo[0] : lo[2];
+        const float s1h = up ? hi[1] : hi[3], s1l = up ? lo[1] : lo[3];
+        ff_add(h0, l0, __shfl_xor_sync(kAll, s0h, 16), __shfl_xor_sync(kAll, s0l, 16));
+        ff_add(h1, l1, __shfl_xor_sync(kAll, s1h, 16), __shfl_xor_sync(kAll, s1l, 16));
+        const bool up3 = (lane & 8) != 0;  // keeps the second of the two
+        h = up3 ? h1 : h0;
+        l = up3 ? l1 : l0;
+        const float sh = up3 ? h0 : h1, sl = up3 ? l0 : l1;
+        ff_add(h, l, __shfl_xor_sync(kAll, sh, 8), __shfl_xor_sync(kAll, sl, 8));
+    } else if constexpr (kU == 2) {
+        const bool up = (lane & 16) != 0;  // keeps row 1 (else 0)
+        h = up ? hi[1] : hi[0];
+        l = up ? lo[1] : lo[0];
+        const float sh = up ? hi[0] : hi[1], sl = up ? lo[0] : lo[1];
+        ff_add(h, l, __shfl_xor_sync(kAll, sh, 16), __shfl_xor_sync(kAll, sl, 16));
+    } else {
+        h = hi[0];
+        l = lo[0];
+    }
+    constexpr int kFirst = kU == 4 ? 4 : kU == 2 ? 8 : 16;
+#pragma unroll
+    for (int o = kFirst; o > 0; o >>= 1) ff_add(h, l, __shfl_xor_sync(kAll, h, o), __shfl_xor_sync(kAll, l, o));
+}
+
+// v[g] for a lane-dependent g < kU without indexing a register array
+template <int kU>
+__device__ __forceinline__ float pick_row(const float (&v)[kU], int g)
+{
+    float x = v[0];
+#pragma unroll
+    for (int u = 1; u < kU; ++u) x = g == u ? v[u] : x;
+    return x;
+}
+
 template <int kChunks, int kU>
 __global__ void __launch_bounds__(256) prep_rows_kernel(const PrepArgs p)
 {
@@ -206,10 +269,12 @@ __global__ void __launch_bounds__(256) prep_rows_kernel(const PrepArgs p)
                 }
             }
         }
+        // per row: integrality and max |x| (in every lane); rows past n hold zeros and change
+        // nothing
+        float rmx[kU];
+        bool rinteger[kU];
 #pragma unroll
         for (int u = 0; u < kU; ++u) {
-            const int64_t r = base + u;
-            if (r >= p.n) break;  // warp-uniform
             float mx = 0.f;
             int rfrac = 0;
 #pragma unroll
@@ -221,6 +286,15 @@ __global__ void __launch_bounds__(256) prep_rows_kernel(const PrepArgs p)
                     mx = fmaxf(mx, fabsf(x));
                 }
             frac |= rfrac;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            rmx[u] = mx;
+            rinteger[u] = !__any_sync(0xffffffffu, rfrac);
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const int64_t r = base + u;
+            if (r >= p.n) break;  // warp-uniform
             if (p.out != nullptr || p.not_exact != nullptr) {
 #pragma unroll
                 for (int j = 0; j < kChunks; ++j) {
@@ -238,8 +312,7 @@ __global__ void __launch_bounds__(256) prep_rows_kernel(const PrepArgs p)
                 }
             }
             // the row's max |x| (E4M3 scale, int_stats, the integer test of the norm)
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            const float mx = rmx[u];
             mx_all = fmaxf(mx_all, mx);
             if (p.f8 != nullptr) {
                 const float inv = mx > 0.f ? 448.f / mx : 0.f;
@@ -257,12 +330,22 @@ __global__ void __launch_bounds__(256) prep_rows_kernel(const PrepArgs p)
                 }
                 if (lane == 0) p.scales[r] = mx / 448.f;
             }
-            if (p.norms != nullptr) {
-                float f;
-                bool ok;
-                if (!__any_sync(0xffffffffu, rfrac) && (float)D * mx * mx < 16777216.f) {
-                    // integers whose squares sum below 2^24: every partial sum is an exact
-                    // integer, so any order gives the double sum's value
+        }
+        if (p.norms != nullptr) {
+            // the kU rows' norms together: lane l settles row g = l / (32 / kU) of the batch
+            constexpr int kGroup = 32 / kU;
+            const int g = lane / kGroup;
+            bool all_int = true;
+#pragma unroll
+            for (int u = 0; u < kU; ++u) all_int = all_int && rinteger[u] && (float)D * rmx[u] * rmx[u] < 16777216.f;
+            float f;
+            bool ok = true;
+            if (all_int) {
+                // integers whose squares sum below 2^24: every partial sum is an exact integer,
+                // so any order gives the double sum's value
+                float fr[kU];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
                     float s32 = 0.f;
 #pragma unroll
                     for (int j = 0; j < kChunks; ++j)
@@ -270,10 +353,16 @@ __global__ void __launch_bounds__(256) prep_rows_kernel(const PrepArgs p)
                         for (int i = 0; i < 4; ++i) s32 = __fmaf_rn(v[u][j][i], v[u][j][i], s32);
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) s32 = __fadd_rn(s32, __shfl_xor_sync(0xffffffffu, s32, o));
-                    f = s32;
-                    ok = true;
-                } else {
-                    float hi = 0.f, lo = 0.f;
+                    fr[u] = s32;
+                }
+                f = pick_row(fr, g);
+            } else {
+                // float-float partials per lane (exact products split by fma, TwoSum additions)
+                float hi[kU], lo[kU];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    hi[u] = 0.f;
+                    lo[u] = 0.f;
 #pragma unroll
                     for (int j = 0; j < kChunks; ++j)
 #pragma unroll
@@ -282,38 +371,31 @@ __global__ void __launch_bounds__(256) prep_rows_kernel(const PrepArgs p)
                             const float q = __fmul_rn(x, x);
                             const float qe = __fmaf_rn(x, x, -q);
                             float sum, t;
-                            two_sum(hi, q, sum, t);
-                            hi = sum;
-                            lo = __fadd_rn(lo, __fadd_rn(t, qe));
+                            two_sum(hi[u], q, sum, t);
+                            hi[u] = sum;
+                            lo[u] = __fadd_rn(lo[u], __fadd_rn(t, qe));
                         }
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) {
-                        const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
-                        const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
-                        float sum, t;
-                        two_sum(hi, oh, sum, t);
-                        hi = sum;
-                        lo = __fadd_rn(__fadd_rn(lo, ol), t);
-                    }
-                    // every lane holds the same values (the butterfly adds in commutative pairs)
-                    ok = certified_norm(hi, lo, D, f);
-                    if (!ok && mx == 0.f) {  // an all-zero row
-                        ok = true;
-                        f = 0.f;
-                    }
                 }
-                if (lane == 0) {
-                    if (!ok) {
-                        const float* row = p.x + r * p.ld;
-                        double acc = 0.0;
-                        for (int d = 0; d < D; ++d) {
-                            const double a = (double)__ldg(row + d);
-                            acc = __fma_rn(a, a, acc);
-                        }
-                        f = __double2float_rn(acc);
-                    }
-                    p.norms[r] = f;
+                float h, l;
+                ff_reduce_rows<kU>(hi, lo, lane, h, l);
+                ok = certified_norm(h, l, D, f);
+                if (!ok && pick_row(rmx, g) == 0.f) {  // an all-zero row
+                    ok = true;
+                    f = 0.f;
                 }
+            }
+            const int64_t r = base + g;
+            if (lane % kGroup == 0 && r < p.n) {
+                if (!ok) {
+                    const float* row = p.x + r * p.ld;
+                    double acc = 0.0;
+                    for (int d = 0; d < D; ++d) {
+                        const double a = (double)__ldg(row + d);
+                        acc = __fma_rn(a, a, acc);
+                    }
+                    f = __double2float_rn(acc);
+                }
+                p.norms[r] = f;
             }
         }
     }
