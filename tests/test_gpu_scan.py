@@ -84,6 +84,26 @@ def test_duplicate_rows_overflow_and_fixup(engine, oracle, Q):
     np.testing.assert_array_equal(d, od)
 
 
+def test_ties_past_the_sort_at_the_boundary_key(engine, oracle):
+    # Every distinct row appears 48 times (shuffled): with k = 100 (shortlist 112, sort
+    # buffer 128 words) the boundary key K of rank 112 is shared by a whole group, so
+    # the 144 words with keys up to K overflow the sort and the selection resolves K's
+    # ties by a rank search over the index half (lower index first).  The scan itself
+    # answers the queries: no segment overflows.
+    rng = np.random.default_rng(12)
+    base = rng.integers(0, 256, (3000, 64)).astype(np.float32)
+    X = np.repeat(base, 48, axis=0)
+    rng.shuffle(X)
+    Qs = rng.integers(0, 256, (200, 64)).astype(np.float32)
+    k = 100
+    d, i, st = run(engine, X, Qs, k, scan=engine.SCAN_ON)
+    assert st["scan"] == 1 and st["kp"] == 112
+    assert engine.last_fixups() <= 20
+    od, oi = oracle.knn_gemm(X, Qs, k, kp=st["kp"], rerank=True)
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_array_equal(d, od)
+
+
 def test_unrepresentative_sample_fixup(engine, oracle):
     # Only every 32nd row (exactly the finest seeding sample) lies near the
     # queries, so the seeded threshold admits fewer than kp rows and the fix-up
