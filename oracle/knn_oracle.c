@@ -36,8 +36,10 @@
  * fresh rand() data against knn.m with a norm tolerance), MATLAB is absent,
  * and the reference GPU library cannot run on the aarch64 GPU host.  The
  * ranking part of this oracle is therefore "parity unpinned"; only the host
- * merge restatement is pinned against the reference's own compiled merge
- * functions (oracle/ref_merge_pin.cpp, built by oracle/build_ref.sh).
+ * merge restatement is pinned against the reference's own merge functions,
+ * compiled from its sources into oracle/_ref/libref_merge.so by
+ * oracle/build_ref.py (wrappers oracle/ref_merge_bitonic.cu and
+ * oracle/ref_merge_heap.cu) and compared in tests/test_oracle.py.
  */
 #include <math.h>
 #include <stdint.h>

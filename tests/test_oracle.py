@@ -107,3 +107,39 @@ def test_synthetic_generators_are_seeded():
     assert ((a == 0).sum(1) >= 10).all()
     u, _ = S.uniform(100, 128, seed=0)
     assert u.dtype == np.float32 and 0 <= u.min() and u.max() < 1
+
+
+def _ref_merge_lib():
+    # the reference's own host merges, compiled from its sources where they are
+    # mounted (oracle/build_ref.py); absent elsewhere
+    import build_ref
+    if not build_ref.available():
+        pytest.skip("reference sources not mounted: merge pin not built")
+    build_ref.build_if_available()
+    return build_ref.load()
+
+
+@pytest.mark.parametrize("which", ["bitonic", "heap"])
+def test_merge_restatement_pinned_to_reference_code(oracle, which):
+    # mergeResBitonic (src/cuknnBitonic.cu:381-417) and mergeResHeap
+    # (src/cuknnHeap.cu:26-59) run on the same per-stream lists as the oracle's
+    # restatement: list 0 (values and indices, in its unsorted slot order) must match
+    # bit for bit, ties included (a value equal to the current maximum never replaces it)
+    import ctypes
+    fn = getattr(_ref_merge_lib(), "ref_merge_" + which)
+    fp = ctypes.POINTER(ctypes.c_float)
+    fn.argtypes = [fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    fn.restype = None
+    rng = np.random.default_rng(31 if which == "bitonic" else 32)
+    for L, Q, k, tied in [(1, 5, 4, False), (2, 37, 1, True), (4, 37, 16, True), (7, 20, 5, False),
+                          (3, 64, 32, True), (8, 9, 100, False)]:
+        if tied:
+            d = rng.integers(0, 6, (L, Q, k)).astype(np.float32)
+        else:
+            d = rng.standard_normal((L, Q, k)).astype(np.float32)
+        i = rng.permutation(L * Q * k).astype(np.float32).reshape(L, Q, k)
+        rd, ri = d.copy(), i.copy()
+        fn(rd.ctypes.data_as(fp), ri.ctypes.data_as(fp), k, Q, L)
+        od, oi = oracle.merge_replace_max(d, i)
+        np.testing.assert_array_equal(od, rd[0])
+        np.testing.assert_array_equal(oi, ri[0])
