@@ -143,3 +143,12 @@ def test_merge_restatement_pinned_to_reference_code(oracle, which):
         od, oi = oracle.merge_replace_max(d, i)
         np.testing.assert_array_equal(od, rd[0])
         np.testing.assert_array_equal(oi, ri[0])
+
+
+def test_reference_recipe_is_inert_without_the_sources(monkeypatch, tmp_path):
+    # where the reference is not mounted (the GPU host) the recipe builds nothing and
+    # reports it, so build() never depends on the reference
+    import build_ref
+    monkeypatch.setattr(build_ref, "REF", str(tmp_path / "absent"))
+    assert not build_ref.available()
+    assert build_ref.build_if_available() is False
