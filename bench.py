@@ -15,7 +15,14 @@ queries resident in HBM; `e2e` is the same metric through the drop-in C ABI
 (gpuknnsBitonic; knns_search_host for the precision forms) from pinned host
 buffers, host<->device copies included.
 `--impl reference` times the reference's CPU path (demo/knn.m, restated in C
-in oracle/knn_oracle.c) on the host cores on a bounded query sample.
+in oracle/knn_oracle.c) on the host cores, on whole query batches where the
+step budget allows (the default run times the full 10,000-query batch).
+
+The plain-form line also carries `accuracy` (recall@k and the largest relative
+distance error against the FP64 oracle on a query sample, outside the timed
+region) and `forms`: the same workload through the BF16 shortlist form (c from
+the autotuner) and through the plain form on 3xTF32 keys (`tf32_only`), each
+timed like the headline and checked against the same FP64 sample.
 """
 import argparse
 import json
@@ -90,77 +97,44 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-def fp8_peak(peaks, peak_kind):
-    """Dense FP8 E4M3 peak: the driver's measurement when present, else the cuBLASLt FP8
-    GEMM rate measured by --measure-peaks and recorded in profiles/gemm_peaks_gb300.md,
-    else twice the BF16 peak (the nominal ratio).  Returns (TFLOP/s, source)."""
-    if "fp8_tflops" in peaks:
-        return float(peaks["fp8_tflops"]), f"{peak_kind} fp8 dense burst"
-    p = os.path.join(ROOT, "profiles", "gemm_peaks_gb300.md")
-    if os.path.exists(p):
-        for line in open(p):
-            if line.strip().startswith("fp8_e4m3_tflops:"):
-                try:
-                    v = float(line.split(":", 1)[1].strip().split()[0])
-                    return v, "cuBLASLt FP8 E4M3 8192^3 GEMM burst measured on this GPU type (bench.py --measure-peaks)"
-                except ValueError:
-                    break
-    return 2.0 * peaks["bf16_tflops"], f"2 x {peak_kind} bf16 dense burst (nominal FP8:BF16 dense rate 2:1)"
+# DRAM traffic per launch of the dominant kernel, from one ncu capture of each workload
+# (dram__bytes_read.sum + dram__bytes_write.sum; the summaries under profiles/ give the
+# command and, where the capture ran on a cut of the workload, the scaling).
+NCU_TRAFFIC = {
+    ("scan_kernel", "int1m"): 327.7e6,
+    ("scan_kernel", "aniso8m"): 2537.0e6,
+}
 
 
-def measure_peaks():
-    """Dense GEMM rates of cuBLASLt on this GPU: FP8 E4M3 (torch._scaled_mm) and BF16, 8192^3,
-    best of 10 (burst) and back to back for 4 s (sustained).  Prints one JSON line."""
+def fp8_peak_live():
+    """Dense FP8 E4M3 rate of cuBLASLt on this GPU (torch._scaled_mm, 8192^3, best of 5), TFLOP/s,
+    as the roofline denominator of the E4M3 scan; None when the GEMM is unavailable."""
     import torch
     n = 8192
-    dev = torch.device("cuda")
-    a = torch.randn(n, n, device=dev)
-    b = torch.randn(n, n, device=dev)
-    a8 = a.to(torch.float8_e4m3fn)
-    b8 = b.to(torch.float8_e4m3fn).t().contiguous().t()
-    one = torch.tensor(1.0, device=dev)
-    abf, bbf = a.to(torch.bfloat16), b.to(torch.bfloat16)
+    try:
+        dev = torch.device("cuda")
+        a8 = torch.randn(n, n, device=dev).to(torch.float8_e4m3fn)
+        b8 = torch.randn(n, n, device=dev).to(torch.float8_e4m3fn).t().contiguous().t()
+        one = torch.tensor(1.0, device=dev)
 
-    def rate(fn):
+        def fn():
+            return torch._scaled_mm(a8, b8, scale_a=one, scale_b=one, out_dtype=torch.bfloat16)
         for _ in range(3):
             fn()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         best = 1e9
-        for _ in range(10):
+        for _ in range(5):
             e0.record()
             fn()
             e1.record()
             e1.synchronize()
             best = min(best, e0.elapsed_time(e1))
-        t0, reps = time.perf_counter(), 0
-        while time.perf_counter() - t0 < 4.0:
-            for _ in range(20):
-                fn()
-            reps += 20
-            torch.cuda.synchronize()
-        return 2 * n ** 3 / (best / 1e3) / 1e12, 2 * n ** 3 * reps / (time.perf_counter() - t0) / 1e12
-
-    f8b, f8s = rate(lambda: torch._scaled_mm(a8, b8, scale_a=one, scale_b=one, out_dtype=torch.bfloat16))
-    bfb, bfs = rate(lambda: abf @ bbf)
-    print(json.dumps({"gpu": torch.cuda.get_device_name(0), "torch": torch.__version__, "n": n,
-                      "fp8_e4m3_tflops": f8b, "fp8_e4m3_tflops_sustained": f8s,
-                      "bf16_tflops": bfb, "bf16_tflops_sustained": bfs}), flush=True)
-    return 0
-
-
-def profiled_traffic(kernel, workload):
-    """traffic_bytes_per_launch from a committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
-    if not os.path.exists(p):
+        del a8, b8
+        torch.cuda.empty_cache()
+        return 2 * n ** 3 / (best / 1e3) / 1e12
+    except Exception:
         return None
-    for line in open(p):
-        if line.strip().startswith("traffic_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1].strip().split()[0])
-            except ValueError:
-                return None
-    return None
 
 
 class ClockSampler:
@@ -252,6 +226,11 @@ def cpu_baseline(corpus, queries, k, budget_s=12.0):
 
 
 def run_reference(args, w):
+    """The reference's CPU path on the host cores: demo/knn.m restated in C (oracle/knn_oracle.c),
+    every host thread.  Each timed step searches a contiguous block of the workload's queries
+    against the whole corpus: the full batch when the steps fit a budget of about three
+    minutes, else the largest block that does (sized from a 1,000-query probe, large enough
+    that the per-call corpus sweep does not dominate)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
@@ -259,22 +238,22 @@ def run_reference(args, w):
     oracle.build()
     corpus, queries = gen_data(w)
     threads = oracle.max_threads()
-    k = w["k"]
-    # size each step so that warm-up + timed steps end within a few minutes
+    k, Q = w["k"], len(queries)
+    probe = min(Q, 1000)
     t0 = time.perf_counter()
-    oracle.knn_gemm(corpus, queries[:threads], k, nthreads=threads)
-    per_q = (time.perf_counter() - t0) / threads
-    budget = 150.0 / max(1, args.steps + args.warmup)
-    m = int(max(1, min(len(queries), budget / max(per_q, 1e-6))))
-    for s in range(args.warmup):
-        oracle.knn_gemm(corpus, queries[:m], k, nthreads=threads)
+    oracle.knn_gemm(corpus, queries[:probe], k, nthreads=threads)
+    per_q = (time.perf_counter() - t0) / probe
+    budget = 180.0 / max(1, args.steps)
+    m = int(max(probe, min(Q, budget / max(per_q, 1e-9))))
+    for _ in range(args.warmup):  # untimed; a small block each
+        oracle.knn_gemm(corpus, queries[:min(m, 256)], k, nthreads=threads)
     t0 = time.perf_counter()
-    for s in range(args.steps):
-        lo = (s * m) % max(1, len(queries) - m + 1)
+    for s_ in range(args.steps):
+        lo = (s_ * m) % max(1, Q - m + 1)
         oracle.knn_gemm(corpus, queries[lo:lo + m], k, nthreads=threads)
     el = time.perf_counter() - t0
     value = m * args.steps / el
-    sample = (f"{m} queries per step against the full {w['N']} x {w['D']} corpus, "
+    sample = (f"{m} of {Q} queries per step against the full {w['N']} x {w['D']} corpus, "
               f"{threads} host threads, demo/knn.m restated in C (oracle/knn_oracle.c)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "queries/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -333,80 +312,146 @@ def run_gb300(args, w):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    corpus_np, queries_np = gen_data(w, rank)
+    split_corpus = args.split == "corpus" and world > 1
+    # replicas: the same corpus and this rank's own queries; corpus split: this rank's shard of
+    # the corpus and everybody's queries (rank 0's)
+    corpus_np, queries_np = gen_data(w, 0 if split_corpus else rank)
     N, D, Q, k = w["N"], w["D"], w["Q"], w["k"]
-    c = torch.from_numpy(corpus_np).to(dev)
+    if split_corpus:
+        from cuknns import shard as SH
+        r0, r1 = SH.shard_bounds(N, world, rank)
+        c = torch.from_numpy(corpus_np[r0:r1]).to(dev)
+    else:
+        c = torch.from_numpy(corpus_np).to(dev)
     q = torch.from_numpy(queries_np).to(dev)
     dist_out = torch.empty((Q, k), dtype=torch.float32, device=dev)
     idx_out = torch.empty((Q, k), dtype=torch.int32, device=dev)
     stream = torch.cuda.current_stream(dev)
 
     prec = {"exact": cuknns.PREC_EXACT, "bf16": cuknns.PREC_BF16, "fp8": cuknns.PREC_FP8}[args.precision]
-    tuned = None
-    if prec != cuknns.PREC_EXACT and args.shortlist == 0:
-        # shortlist factor c from the autotuner: recall@k against the exact form on a 256-query sample
-        t0 = time.perf_counter()
-        ix = cuknns.Index(c, fp8=prec == cuknns.PREC_FP8)
-        sample = q[:256].contiguous()
-        cf, rec = ix.autotune_shortlist(sample, k, target=0.999, precision=prec)
-        ix.close()
-        torch.cuda.empty_cache()
-        args.shortlist = cf
-        tuned = {"shortlist_c": cf, "sample_recall": rec, "sample_queries": 256, "target": 0.999,
-                 "seconds": time.perf_counter() - t0}
-
     scan_mode = {"auto": cuknns.SCAN_AUTO, "on": cuknns.SCAN_ON, "off": cuknns.SCAN_OFF}[args.scan]
 
-    def step(timing=False):
-        cuknns.search(c, q, k, dist=dist_out, idx=idx_out, stream=stream, check=False, timing=timing,
-                      precision=prec, shortlist=args.shortlist, scan=scan_mode, scan_boxes=args.scan_boxes)
+    def autotune(p):
+        """Shortlist factor c of a precision form: recall@k against the exact form on 256 queries."""
+        t0 = time.perf_counter()
+        ix = cuknns.Index(c, fp8=p == cuknns.PREC_FP8)
+        cf, rec = ix.autotune_shortlist(q[:256].contiguous(), k, target=0.999, precision=p)
+        ix.close()
+        torch.cuda.empty_cache()
+        return cf, {"shortlist_c": cf, "sample_recall": rec, "sample_queries": 256, "target": 0.999,
+                    "seconds": time.perf_counter() - t0}
 
-    for _ in range(args.warmup):
-        step()
-    cuknns.lib().knns_check_device(None)
-    st = cuknns.last_stats()
-    cuknns.timing_collect5()  # drop anything recorded so far
+    tuned = None
+    if prec != cuknns.PREC_EXACT and args.shortlist == 0:
+        args.shortlist, tuned = autotune(prec)
 
     def barrier():
         if dist is not None:
             dist.barrier()
 
-    barrier()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
+    def timed(step, steps):
+        """W untimed steps, then `steps` steps between two CUDA events on the launching stream."""
+        for _ in range(args.warmup):
+            step(False)
+        rc_ = cuknns.lib().knns_check_device(None)
+        if rc_ != 0:
+            raise RuntimeError(cuknns.last_error())
+        st_ = cuknns.last_stats()
+        cuknns.timing_collect5()  # drop anything recorded so far
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(args.steps):
-            step(timing=True)
+        for _ in range(steps):
+            step(True)
         e1.record(stream)
         torch.cuda.synchronize()
-    barrier()
-    el_ms = e0.elapsed_time(e1)
-    prep_ms, seed_ms, fused_ms, select_ms, fix_ms, nt = cuknns.timing_collect5()
-    rc = cuknns.lib().knns_check_device(None)
-    if rc != 0:
-        raise RuntimeError(cuknns.last_error())
-    el_ms = reduce_max(el_ms, dist, dev)
-    value = Q * args.steps * world / (el_ms / 1e3)
+        barrier()
+        stages = cuknns.timing_collect5()
+        rc_ = cuknns.lib().knns_check_device(None)
+        if rc_ != 0:
+            raise RuntimeError(cuknns.last_error())
+        return reduce_max(e0.elapsed_time(e1), dist, dev), stages, st_
 
-    # ---- accuracy against the FP64 oracle on a query sample
-    accuracy = None
-    nrq = args.recall_queries if args.recall_queries else (100 if args.precision != "exact" else 0)
-    if nrq and rank == 0:
+    def search_step(p, shortlist, tf32_only=False):
+        if split_corpus:
+            def step(timing):
+                # this rank's shard, then the all-gather of every rank's Q x k list and the merge
+                d_, i_ = SH.sharded_search(c, r0, q, k, stream=stream, check=False, timing=timing, precision=p,
+                                           shortlist=shortlist, scan=scan_mode, scan_boxes=args.scan_boxes,
+                                           tf32_only=tf32_only)
+                dist_out.copy_(d_)
+                idx_out.copy_(i_)
+            return step
+
+        def step(timing):
+            cuknns.search(c, q, k, dist=dist_out, idx=idx_out, stream=stream, check=False, timing=timing,
+                          precision=p, shortlist=shortlist, scan=scan_mode, scan_boxes=args.scan_boxes,
+                          tf32_only=tf32_only)
+        return step
+
+    # ---- headline: the requested form, inputs resident in HBM
+    with ClockSampler(local) as clk:
+        el_ms, (prep_ms, seed_ms, fused_ms, select_ms, fix_ms, nt), st = timed(
+            search_step(prec, args.shortlist), args.steps)
+    # whole-job throughput: replicas search world x Q queries; a corpus split searches Q
+    value = Q * args.steps * (1 if split_corpus else world) / (el_ms / 1e3)
+
+    # ---- accuracy against the FP64 oracle on a query sample (outside every timed region)
+    nrq = args.recall_queries if args.recall_queries else 100
+    sub = np.linspace(0, Q - 1, min(nrq, Q)).astype(np.int64)
+    exact64 = None
+    if rank == 0 and nrq:
         import oracle
         oracle.build()
-        sub = np.linspace(0, Q - 1, nrq).astype(np.int64)
-        got_i = idx_out[torch.from_numpy(sub).to(dev)].cpu().numpy()
-        got_d = dist_out[torch.from_numpy(sub).to(dev)].cpu().numpy()
-        ex_d, ex_i = oracle.knn_f64(corpus_np, queries_np[sub], k)
+        exact64 = oracle.knn_f64(corpus_np, queries_np[sub], k)
+
+    def accuracy_now():
+        """recall@k and the largest relative distance error of idx_out / dist_out on the sample."""
+        if exact64 is None:
+            return None
+        import oracle
+        ii = torch.from_numpy(sub).to(dev)
+        got_i = idx_out[ii].cpu().numpy()
+        got_d = dist_out[ii].cpu().numpy()
         d64 = oracle.pair_dist_f64(corpus_np, queries_np[sub], got_i)
-        accuracy = {"queries": int(nrq), "recall_at_k": oracle.recall_at_k(got_i, ex_i),
-                    "max_dist_rel_err": float((np.abs(got_d - d64) / np.maximum(d64, 1e-30)).max()),
-                    "oracle": "FP64 direct difference (oracle/knn_oracle.c)"}
+        return {"queries": int(len(sub)), "recall_at_k": oracle.recall_at_k(got_i, exact64[1]),
+                "max_dist_rel_err": float((np.abs(got_d - d64) / np.maximum(d64, 1e-30)).max()),
+                "oracle": "FP64 direct difference (oracle/knn_oracle.c)"}
+
+    accuracy = accuracy_now()
+
+    # ---- the other forms on the same workload (plain form only): BF16 shortlist, 3xTF32 keys
+    forms = None
+    if prec == cuknns.PREC_EXACT and not args.no_forms and not split_corpus:
+        forms = {"exact": {"queries_per_s": value, "accuracy": accuracy,
+                           "path": "threshold scan (BF16 keys, data BF16-exact)" if st["scan"] else "shortlist kernel"}}
+        cf, tuned_bf = autotune(cuknns.PREC_BF16)
+        f_ms, f_stages, f_st = timed(search_step(cuknns.PREC_BF16, cf), args.steps)
+        forms["bf16_shortlist"] = {"queries_per_s": Q * args.steps * world / (f_ms / 1e3),
+                                   "ms_per_step": f_ms / args.steps, "shortlist": f_st["kp"], "autotune": tuned_bf,
+                                   "accuracy": accuracy_now()}
+        t_steps = max(3, min(args.steps, 20))
+        t_ms, t_stages, t_st = timed(search_step(cuknns.PREC_EXACT, 0, tf32_only=True), t_steps)
+        f_c, f_q = lo_tile_fraction(corpus_np), lo_tile_fraction(queries_np)
+        t_fused = (t_stages[1] + t_stages[2]) / max(1, t_stages[5])
+        products = 1.0 + f_c + f_q
+        t_flops = products * 2.0 * N * Q * D * (1.0 + (1.0 / 16.0 if t_st["pilot"] else 0.0))
+        forms["tf32_plain"] = {"queries_per_s": Q * t_steps * world / (t_ms / 1e3), "ms_per_step": t_ms / t_steps,
+                               "steps": t_steps, "kernel": "tc_kernel (3xTF32)",
+                               "products_per_useful_product": products,
+                               "note": "3xTF32 keys; a correction product is skipped where the TF32 low part of the "
+                                       "corpus tile or query tile is zero (exact zeros), as on integer data",
+                               "fused_ms": t_fused,
+                               "tf32_tflops_executed": t_flops / (t_fused / 1e3) / 1e12,
+                               "accuracy": accuracy_now()}
+        forms["bf16_over_tf32"] = forms["bf16_shortlist"]["queries_per_s"] / forms["tf32_plain"]["queries_per_s"]
+        # leave the headline's answers in the output buffers
+        search_step(prec, args.shortlist)(False)
 
     # ---- end to end through the drop-in C ABI from pinned host buffers
     e2e = None
-    e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 20))
+    e2e_steps = 0 if (args.no_e2e or split_corpus) else max(1, min(args.steps, 20))
     if e2e_steps:
         popts = None if prec == cuknns.PREC_EXACT else {"precision": prec, "shortlist": args.shortlist}
         e2e = run_e2e(corpus_np, queries_np, k, Q, world, e2e_steps, barrier, dist, dev, popts)
@@ -424,7 +469,11 @@ def run_gb300(args, w):
         flops = 2.0 * N * Q * D
         if args.precision == "fp8":
             row_bytes = -(-D // 128) * 128
-            peak, peak_src = fp8_peak(peaks, peak_kind)
+            live = fp8_peak_live()
+            if live is not None:
+                peak, peak_src = live, "cuBLASLt FP8 E4M3 8192^3 GEMM burst, measured in this run"
+            else:
+                peak, peak_src = 2.0 * peaks["bf16_tflops"], f"2 x {peak_kind} bf16 dense burst"
             mma = f"e4m3 (kind::f8f6f4, M128 N{224 if row_bytes <= 256 else 192})"
             padded_k = row_bytes
         else:
@@ -460,8 +509,7 @@ def run_gb300(args, w):
     if on_scan and args.precision == "fp8":
         # the same achieved rate against twice the BF16 peak (the nominal FP8:BF16 ratio)
         roof["frac_vs_2x_bf16"] = roof["achieved"] / (2.0 * peaks["bf16_tflops"])
-    tr = profiled_traffic(kern, args.workload)
-    roof["traffic"] = tr
+    roof["traffic"] = NCU_TRAFFIC.get((kern, args.workload))
     roof["kernel"] = kern
     roof["kernel_ms"] = fused_avg_ms
     roof["effective_fp32_tflops"] = 2.0 * N * Q * D / (fused_avg_ms / 1e3) / 1e12
@@ -473,11 +521,13 @@ def run_gb300(args, w):
     cpu = cpu_baseline(corpus_np, queries_np, k) if world == 1 and not args.no_cpu_baseline else None
     line = {"metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": el_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None,
+            "scaling": "strong" if split_corpus else "weak", "vs_baseline": None,
             "dtype": {"exact": "f32", "bf16": "bf16 keys, f32 re-rank", "fp8": "e4m3 keys, f32 re-rank"}[args.precision],
             "data": "synthetic",
             "config": {"workload": w["desc"], "N": N, "Q": Q, "D": D, "k": k,
-                       "parallelism": f"replicas x{world} (queries sharded, corpus replicated)",
+                       "parallelism": (f"corpus split x{world} (contiguous shards, all-gather of Q x k lists, "
+                                       f"device merge)" if split_corpus else
+                                       f"replicas x{world} (queries sharded, corpus replicated)"),
                        "l2": f"inputs larger than L2 ({N * D * 4 / 1e6:.0f} MB FP32 corpus)" if N * D * 4 > 129e6
                        else "working set within L2 (65,536 x 128 corpus)",
                        "algo": {1: "tcgen05", 2: "CUDA-core FP32"}[st["algo"]], "precision": args.precision,
@@ -486,8 +536,8 @@ def run_gb300(args, w):
                        "scan_cap": st["scan_cap"], "scan_ring": st["scan_ring"], "stages": st["stages"]},
             "stage_ms": {"prep": prep_ms / max(1, nt), "seed": seed_ms / max(1, nt), "fused": fused_ms / max(1, nt),
                          "select": select_ms / max(1, nt), "fixup": fix_ms / max(1, nt)},
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "accuracy": accuracy, "autotune": tuned,
-            "gpu_launches": st["launches"] * args.steps,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "accuracy": accuracy, "forms": forms,
+            "autotune": tuned, "gpu_launches": st["launches"] * args.steps,
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
     if dist is not None:
@@ -599,12 +649,26 @@ def main():
     ap.add_argument("--rate", type=float, default=4000.0, help="serving: offered requests per second")
     ap.add_argument("--requests", type=int, default=4000, help="serving: requests in the timed run")
     ap.add_argument("--recall-queries", type=int, default=0,
-                    help="measure recall@k and distance error against the FP64 oracle on this many queries")
-    ap.add_argument("--measure-peaks", action="store_true",
-                    help="time cuBLASLt FP8 E4M3 and BF16 8192^3 GEMMs on this GPU and print them")
+                    help="queries of the FP64-oracle accuracy sample (0 = 100)")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="plain form: skip the BF16-shortlist and 3xTF32 comparison runs")
+    ap.add_argument("--split", default="queries", choices=["queries", "corpus"],
+                    help="N > 1 GPUs: replicas with their own queries (weak scaling), or one query batch "
+                         "against a corpus split across the GPUs (strong scaling: all-gather + merge)")
     args = ap.parse_args()
-    if args.measure_peaks:
-        return measure_peaks()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one process per GPU: launch the ranks ourselves
+        import socket
+        with socket.socket() as sk:
+            sk.bind(("127.0.0.1", 0))
+            port = sk.getsockname()[1]
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", str(args.gpus),
+               "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + sys.argv[1:]
+        return subprocess.call(cmd)
+    if world != args.gpus:
+        print(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={world}", file=sys.stderr)
+        return 2
     if args.warmup < 3:
         args.warmup = 3
     w = WORKLOADS[args.workload]

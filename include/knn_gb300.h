@@ -39,7 +39,8 @@ extern "C" {
 /* precision of the ranking keys */
 #define KNNS_PREC_EXACT 0 /* FP32-accurate keys (BF16 products when the data are BF16-exact, else 3xTF32) */
 #define KNNS_PREC_BF16 1  /* BF16 keys pick a shortlist of c*k per query, re-ranked by exact distance
-                             (tensor cores, D <= 256, c*k <= 128) */
+                             (tensor cores, D <= 256; c*k <= 128, or up to 512 on corpora of at least
+                             16384 rows, where the threshold scan keeps the shortlist) */
 #define KNNS_PREC_FP8 2   /* FP8 E4M3 keys (per-row absmax scales, FP32 accumulation) pick the shortlist
                              on the threshold scan, re-ranked by exact distance; same limits as BF16.
                              Where the scan does not run (N below its threshold, KNNS_SCAN_OFF) and
@@ -69,7 +70,10 @@ typedef struct knns_options {
                         per device block; 0 = automatic: the whole corpus when it fits in free device memory,
                         else blocks sized to it.  Each block is searched and merged into the running top-k
                         by (distance, index): results are identical to one search over the whole corpus */
-    int reserved[3];
+    int tf32_only;   /* exact form: 1 = 3xTF32 keys even for data that are exact in BF16 (the BF16
+                        tensor-core shortcut and the threshold scan stand down); results are the same,
+                        the kernels slower -- a measurement switch for comparing the two key types */
+    int reserved[2];
 } knns_options;
 
 typedef struct knns_stats {
@@ -107,6 +111,20 @@ int knns_search_device(const float *corpus, int64_t N, int64_t ldc, const float 
  */
 int knns_search_host(const float *corpus, int64_t N, const float *queries, int64_t Q, int D, int k,
                      float *dist, int32_t *idx, const knns_options *opt);
+
+/*
+ * Merge of two per-query result lists on the device, by (distance, index): the
+ * first `have` entries of run (Q x k) and the first kb entries of blk (Q x kb,
+ * indices shifted by `offset`) -> the first min(k, have + kb) entries of their
+ * union into out (Q x k; must not alias the inputs).  Both inputs sorted as the
+ * search returns them.  It is the exchange step of a corpus split across GPUs
+ * (every rank's top-k over its shard, gathered, merged) and of corpus blocks
+ * streamed through one GPU -- the reference merges its per-stream corpus chunks
+ * on the host instead (mergeResBitonic, src/cuknnBitonic.cu:381-417, called at
+ * :586-589).  Asynchronous on `stream`.
+ */
+int knns_merge_topk(const float *run_d, const int32_t *run_i, int have, const float *blk_d, const int32_t *blk_i,
+                    int kb, int32_t offset, int64_t Q, int k, float *out_d, int32_t *out_i, void *stream);
 
 /* Synchronise `stream` and report a kernel-side bounded-wait timeout, if any. */
 int knns_check_device(void *stream);
@@ -155,14 +173,25 @@ int knns_timing_collect5(double ms[5], int *count);
  * norms (4 * roundup(N, 128) bytes), the thresholds (4 * Q bytes) and at least
  * one split of shortlists (8 * Q * kp bytes, kp = k + max(8, k/8) rounded up to
  * 16, at least 32); larger problems are rejected with KNNS_ERR_UNSUPPORTED and
- * a message.  The first call on a device looks the array's address up
- * (cudaGetSymbolAddress), so make it before any stream capture.  Every call
- * shares the array: calls whose GPU work overlaps (other streams, other host
- * threads) race on it and must be serialised by the caller.  The function
- * calls no cudaMalloc, cudaFree or allocating library routine.
+ * a message.  k up to 512 is served, as by knns_search_device's CUDA-core
+ * path (the re-rank margin is dropped where it would pass 512 entries).  The
+ * first call on a device looks the array's address up (cudaGetSymbolAddress);
+ * under CUDA's default lazy module loading that first lookup is also what
+ * loads the array into device memory, so the first call can still take
+ * 8 MiB of HBM.  Make it -- or call knns_noalloc_prepare -- once per device
+ * at start-up, before another allocator takes the HBM and before any stream
+ * capture.  Every call shares the array: calls whose GPU work overlaps
+ * (other streams, other host threads) race on it and must be serialised by
+ * the caller.  The cached address belongs to the device's primary context:
+ * do not use the entry point across a cudaDeviceReset.  The function calls
+ * no cudaMalloc, cudaFree or allocating library routine.
  */
 int knns_search_device_noalloc(const float *corpus, int64_t N, int64_t ldc, const float *queries, int64_t Q,
                                int64_t ldq, int D, int k, float *dist, int32_t *idx, void *stream);
+
+/* Set-up of knns_search_device_noalloc on the current device only: looks up (and so
+   loads) its scratch array, which the first search would otherwise do.  Idempotent. */
+int knns_noalloc_prepare(void);
 
 /*
  * Resident index (no counterpart in the reference, whose drivers copy the corpus
@@ -186,7 +215,7 @@ void knns_index_destroy(knns_index *index);
  * Shortlist autotuner of the precision forms (precision KNNS_PREC_BF16 or
  * KNNS_PREC_FP8): searches the given device queries (a sample of the
  * workload) with the exact form and with the form's keys at
- * shortlist factors c = 2, 4, 8 (while c*k <= 128), and returns in *c_out the
+ * shortlist factors c = 2, 4, 8 (while c*k <= 512), and returns in *c_out the
  * smallest c whose recall@k against the exact form reaches `target` (else the
  * largest tried), its recall in *recall_out.  Synchronises `stream`; needs an
  * index with TF32 copies unless the data are BF16-exact.
@@ -198,8 +227,11 @@ int knns_autotune_shortlist(knns_index *index, const float *queries, int64_t Q, 
  * Serving form (no counterpart in the reference): a request server over a
  * resident index.  Requests of uneven size (1..max_batch queries, host memory,
  * copied at submit) and k (1..128) arrive at any time from any thread; one worker
- * thread packs the pending requests that share the oldest request's k into
- * launches of at most max_batch queries, keeps `slots` launches in flight on
+ * thread packs pending requests, oldest first, into launches of at most
+ * max_batch queries -- in the exact form requests of any k (the launch runs the
+ * largest k and each request keeps the first k of its sorted rows), in the
+ * BF16 / FP8 forms those that share the oldest request's k (their shortlist is
+ * c*k) -- keeps `slots` launches in flight on
  * their own streams and workspaces (a batch formed while another runs overlaps
  * it on the device), and runs each launch as a CUDA graph captured once per
  * (size bucket, k) and slot (buckets: powers of two from 32 to max_batch).  With
@@ -232,6 +264,16 @@ void knns_server_destroy(knns_server *server);
 
 /* Library version as 10000*major + 100*minor + patch. */
 int knns_version(void);
+
+/*
+ * Test hook of the bounded waits: the next search on any thread runs its
+ * shortlist kernels (the tensor-core path) with every barrier wait bounded by
+ * timeout_us and with their copy engines idle, so the waits run out: each
+ * kernel records KNNS_ERR_DEVICE_TIMEOUT, winds down (nothing is in flight) and
+ * returns; knns_check_device then reports it and the context stays usable.
+ * The search's results are undefined.  0 < timeout_us <= 10 s.
+ */
+int knns_debug_stall_next_search(int64_t timeout_us);
 
 /*
  * Test hook: raw 3xTF32 dot products of the first 128 queries against the

@@ -8,6 +8,7 @@
 // N*Q-sized distance buffers, and the corpus blocking by free memory.  The
 // corpus stays resident; the work is split across CTAs instead of streams.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -28,6 +29,9 @@
 namespace knn {
 
 static thread_local std::string g_last_error;
+// test hook (knns_debug_stall_next_search): wait bound of the next search's shortlist kernels,
+// whose producers then issue no copy; 0 = off
+static std::atomic<uint64_t> g_test_stall_ns{0};
 static thread_local knns_stats g_last_stats;
 static thread_local bool g_have_stats = false;
 
@@ -168,6 +172,8 @@ static int encode_rows_bf16(CUtensorMap* m, const void* base, int64_t rows, int6
 }
 
 // ---------------------------------------------------------------- planning
+// smallest corpus the threshold scan runs on when asked to (KNNS_SCAN_ON, long shortlists)
+constexpr int64_t kScanMinRowsForced = 16384;
 static inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 static inline int round32(int x) { return (x + 31) & ~31; }
 static inline int round16(int x) { return (x + 15) & ~15; }
@@ -216,9 +222,14 @@ int resolve_config(const Engine& E, int64_t N, int64_t Q, int D, int k, const kn
         c->dpf = c->fp8 ? ((D + 127) & ~127) / 2 : 0;
         const int cf = o.shortlist > 0 ? o.shortlist : 4;
         c->kp = o.kp > 0 ? o.kp : std::max(32, round16(k * cf));
-        if (c->kp % 16 != 0 || c->kp < k || c->kp > kMaxKpTC)
+        if (c->kp % 16 != 0 || c->kp < k || c->kp > kMaxKpScan)
             return set_error(KNNS_ERR_UNSUPPORTED, "%s shortlist of %d entries (k=%d) outside [k, %d]", name, c->kp, k,
-                             kMaxKpTC);
+                             kMaxKpScan);
+        // shortlists above kMaxKpTC live only on the threshold scan (global candidate segments)
+        if (c->kp > kMaxKpTC && (N < kScanMinRowsForced || o.scan == KNNS_SCAN_OFF))
+            return set_error(KNNS_ERR_UNSUPPORTED,
+                             "%s shortlist of %d entries needs the threshold scan (N >= %d, scan not off); "
+                             "at most %d entries otherwise", name, c->kp, kScanMinRowsForced, kMaxKpTC);
         c->algo = KNNS_ALGO_TC;
         c->dp = kChunkK;  // TF32 operands unused
         c->dpb = dpb;
@@ -278,11 +289,11 @@ int resolve_config(const Engine& E, int64_t N, int64_t Q, int D, int k, const kn
 // Seeding: the main scan needs, per query, a threshold T with at least kp keys
 // below it (then every top-kp candidate is collected) and few more.  Nested
 // corpus samples give it, coarse to fine: level l keeps every stride_l-th row
-// (stride kSeedStride for the finest level, 16x more per coarser level, the
+// (stride s for the finest level -- seed_stride below --, 16x more per coarser level, the
 // coarsest small enough to keep every key).  Each level collects the keys below
 // the previous level's threshold and picks the key of rank j_l as its own.  With
 // m = j_next / 16 (the expected rank, in this level's sample, of the key of
-// rank j_next in the next one; m = kp / kSeedStride for the finest level)
+// rank j_next in the next one; m = kp / s for the finest level)
 // j = 2m + 4 sqrt(m) + 1 leaves a chance of roughly 1e-5 that fewer than j_next
 // keys fall below the threshold at the next level.  Queries for which that
 // happens in the main pass (and any whose segments overflow) are found by the
@@ -292,8 +303,21 @@ constexpr int kMaxSeedLevels = 6;
 // Finest sampling stride: a coarser sample makes seeding cheaper and the main
 // pass collect more candidates (about 2 kp + 4 sqrt(kp * stride) per query);
 // 32 gave the lowest seeding + scan + selection time on the 1M x 128 and the
-// 4M x 96 workloads (16 and 64 were each slower on one of them).
+// 4M x 96 workloads (16 and 64 were each slower on one of them).  Long
+// shortlists take a finer stride, so that a query's main-pass candidates
+// (mean + six standard deviations) still fit the selection's buffer.
 constexpr int64_t kSeedStride = 32;
+
+static int64_t seed_stride(int kp)
+{
+    int64_t s = kSeedStride;
+    while (s > 4) {
+        const double mean = 2.0 * kp + 4.0 * std::sqrt((double)kp * s), spread = 6.0 * std::sqrt(2.0 * kp * s);
+        if (mean + spread + 64.0 <= (double)kCandMax) break;
+        s /= 2;
+    }
+    return s;
+}
 
 struct ScanLevel {
     int64_t n = 0, stride = 1, len = 0, n_pad = 0;
@@ -302,6 +326,7 @@ struct ScanLevel {
 
 struct ScanPlan {
     int bps = 0, ring = 0;
+    int64_t stride0 = 0;  // finest seeding stride
     int levels = 0;
     ScanLevel lv[kMaxSeedLevels];
     int64_t len = 0;
@@ -309,6 +334,7 @@ struct ScanPlan {
     int sel_words = 0;  // bound on one query's stored main-pass candidates (selection buffer)
     int64_t fixA_rows = 0, fixA_len = 0, fixB_rows = 0, fixB_len = 0;
     int fixA_S = 1, fixB_S = 1;
+    bool simt_fix = false;  // the fix-up runs on the CUDA-core kernel (shortlist above kMaxKpTC)
     size_t cand_words = 0, cnt_words = 0, part_words = 0, norm_words = 0;
 };
 
@@ -346,14 +372,14 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
     if (scan_plan(dpb, o.scan_boxes, &P->bps, &P->ring, fp8) != 0)
         return set_error(KNNS_ERR_UNSUPPORTED, "threshold scan: no ring geometry for %d BF16 columns with %d boxes per slot",
                          dpb, o.scan_boxes);
-    const int64_t qt = cdiv(cdiv(Q, kTileQ), 2) * 2;  // query tiles, padded to whole CTA pairs
+    const int64_t qt = cdiv(Q, kTileQ);  // query tiles
     const int tn = scan_tile_rows(dpb);
     const int pc = scan_part_cols(dpb);  // segment columns per tile (the parts are not all equal)
-    // levels, finest first: strides kSeedStride, 16 kSeedStride, ... until the sample fits
-    // the selector whole
+    // levels, finest first: strides s, 16 s, ... until the sample fits the selector whole
+    P->stride0 = seed_stride(kp);
     int64_t st[kMaxSeedLevels];
     int L = 0;
-    for (int64_t stride = kSeedStride;; stride *= 16) {
+    for (int64_t stride = P->stride0;; stride *= 16) {
         if (L == kMaxSeedLevels) return set_error(KNNS_ERR_UNSUPPORTED, "threshold scan: corpus too large to seed");
         st[L++] = stride;
         if (cdiv(N, stride) <= kCandMax / 2) break;
@@ -367,7 +393,7 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
         v.n_pad = cdiv(v.n, kScanTileN) * kScanTileN + kScanTileN;  // >= one tile past the view
     }
     // ranks, finest to coarsest
-    double m = (double)kp / (double)kSeedStride;
+    double m = (double)kp / (double)P->stride0;
     for (int l = L - 1; l >= 0; --l) {
         ScanLevel& v = P->lv[l];
         v.j = std::min<int>((int)v.n, seed_rank(m));
@@ -414,15 +440,20 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
         (double)kCandMax, std::ceil((hm + 6.0 * (double)P->lv[L - 1].stride * std::sqrt((double)P->lv[L - 1].j) + 64.0) / 32.0) * 32.0);
     P->cand_words = std::max(P->cand_words, (size_t)kScanParts * P->S * Q * P->cap);
     P->cnt_words = std::max(P->cnt_words, (size_t)kScanParts * P->S * Q);
-    // fix-up of failed queries: up to 512 on a full wave, the rest (rare) on 8 splits
-    const int64_t tiles128 = cdiv(N, kTileN);
-    P->fixA_rows = std::min<int64_t>(Q, 4 * kTileQ);
-    P->fixA_S = (int)std::max<int64_t>(1, std::min<int64_t>(tiles128, E.sms / cdiv(P->fixA_rows, kTileQ)));
-    P->fixA_len = cdiv(tiles128, P->fixA_S) * kTileN;
+    // fix-up of failed queries: up to 512 on a full wave, the rest (rare) on 8 splits; shortlists
+    // above the tensor-core kernel's kMaxKpTC go to the CUDA-core kernel in tiles of 32 queries
+    // (exact FP32 keys): the first 32 failed queries on a wave of splits, the rest on 8
+    P->simt_fix = kp > kMaxKpTC;
+    const int ft = P->simt_fix ? kSimtTileN : kTileN;
+    const int fq = P->simt_fix ? 32 : kTileQ;
+    const int64_t tilesF = cdiv(N, ft);
+    P->fixA_rows = std::min<int64_t>(Q, P->simt_fix ? fq : 4 * kTileQ);
+    P->fixA_S = (int)std::max<int64_t>(1, std::min<int64_t>(tilesF, E.sms / cdiv(P->fixA_rows, fq)));
+    P->fixA_len = cdiv(tilesF, P->fixA_S) * ft;
     P->fixA_S = (int)cdiv(N, P->fixA_len);
     P->fixB_rows = Q - P->fixA_rows;
-    P->fixB_S = (int)std::min<int64_t>(tiles128, 8);
-    P->fixB_len = cdiv(tiles128, P->fixB_S) * kTileN;
+    P->fixB_S = (int)std::min<int64_t>(tilesF, 8);
+    P->fixB_len = cdiv(tilesF, P->fixB_S) * ft;
     P->fixB_S = (int)cdiv(N, P->fixB_len);
     P->part_words = std::max((size_t)P->fixA_S * P->fixA_rows * kp, (size_t)P->fixB_S * P->fixB_rows * kp);
     return KNNS_OK;
@@ -431,7 +462,7 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
 // ---------------------------------------------------------------- search
 int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const float* queries, int64_t Q, int64_t ldq,
                int D, int k, float* dist, int32_t* idx, float* idx_f, const knns_options& o, cudaStream_t s,
-               knns_stats* st, const PreparedCorpus* pc, bool capture)
+               knns_stats* st, const PreparedCorpus* pc, bool capture, const float* host_corpus)
 {
     if (N <= 0 || D <= 0 || k <= 0 || Q < 0) return set_error(KNNS_ERR_INVALID, "invalid sizes N=%lld Q=%lld D=%d k=%d",
                                                                (long long)N, (long long)Q, D, k);
@@ -449,6 +480,9 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     }
     // the precision forms: BF16 / E4M3 keys only, always re-ranked
     const bool bf16_only = c.precision == KNNS_PREC_BF16 || c.precision == KNNS_PREC_FP8;
+    const uint64_t stall_ns = capture ? 0 : g_test_stall_ns.exchange(0);
+    if (host_corpus != nullptr && (pc != nullptr || capture || ldc != D))
+        return set_error(KNNS_ERR_INVALID, "a corpus streamed from the host needs pitch D and no prepared index");
 
     // The threshold scan serves BF16 keys on large corpora: always in the BF16
     // precision form, and in the exact form when the data turn out BF16-exact
@@ -456,7 +490,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     ScanPlan sp;
     bool scan = false;
     if (c.algo == KNNS_ALGO_TC && o.scan != KNNS_SCAN_OFF && E.cc >= 100 && c.dpb <= 256 && c.rerank) {
-        const int64_t min_n = o.scan == KNNS_SCAN_ON ? 16384 : 131072;
+        const int64_t min_n = (o.scan == KNNS_SCAN_ON || c.kp > kMaxKpTC) ? kScanMinRowsForced : 131072;
         if (N >= min_n) {
             rc = plan_scan(E, N, Q, c.fp8 ? c.dpf : c.dpb, c.kp, o, &sp, c.fp8);
             if (rc) return rc;
@@ -575,8 +609,53 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         ws += E.qbf.cap + E.cand.cap + E.cnt.cap + E.tq.cap + E.cnv.cap + E.fail.cap;
     }
     ws += E.part.cap + E.thr2.cap;
+    // corpus still in host memory: with the threshold scan it is copied in blocks of whole
+    // main-scan splits (each prepared and scanned as soon as it lands), the seeding sample
+    // (every sp.stride0-th row, the rows the seeding levels read) ahead of them; without the
+    // scan the search simply starts once the whole copy has landed
+    const bool streamed = host_corpus != nullptr && scan;
+    const int64_t smp_n = streamed ? cdiv(N, sp.stride0) : 0;
+    const int64_t smp_pad = cdiv(smp_n, kScanTileN) * kScanTileN + kScanTileN;
+    if (streamed) {
+        rc = E.smp.ensure((size_t)smp_n * D * sizeof(float));
+        if (!rc) rc = E.smp_cn.ensure((size_t)smp_pad * sizeof(float));
+        if (!rc) rc = E.smp_bf.ensure((size_t)smp_n * c.dpb * 2);
+        if (!rc && f8) rc = E.smp_f8.ensure((size_t)smp_n * c.dpf * 2);
+        if (!rc && f8) rc = E.smp_cs.ensure((size_t)smp_pad * sizeof(float));
+        if (rc) return rc;
+    }
+    constexpr int kHostBlocks = 8;
+    const int blk_splits = streamed ? (int)cdiv(sp.S, std::min(sp.S, kHostBlocks)) : 0;  // main-scan splits per block
+    const int nblk = streamed ? (int)cdiv(sp.S, blk_splits) : 0;
 
     if (!capture) KNN_CUDA(cudaStreamWaitEvent(s, E.last_done, 0));
+    // ordering events: [0] start, [1] sample landed, [2 + b] block b landed, [2 + nblk + b]
+    // block b prepared, [2 + 2 nblk + b] block b scanned
+    auto oev = [&](int i) -> cudaEvent_t { return E.order_event(i); };
+    if (host_corpus != nullptr) {
+        cudaStream_t cs_ = E.copy_stream();
+        if (!cs_ || !oev(2 + 3 * std::max(nblk, 1))) return set_error(KNNS_ERR_CUDA, "stream or event creation failed");
+        // the copies overwrite the device corpus only once the previous search is done with it
+        KNN_CUDA(cudaEventRecord(oev(0), s));
+        KNN_CUDA(cudaStreamWaitEvent(cs_, oev(0), 0));
+        if (streamed) {
+            KNN_CUDA(cudaMemcpy2DAsync(E.smp.p, (size_t)D * sizeof(float), host_corpus,
+                                       (size_t)sp.stride0 * D * sizeof(float), (size_t)D * sizeof(float),
+                                       (size_t)smp_n, cudaMemcpyHostToDevice, cs_));
+            KNN_CUDA(cudaEventRecord(oev(1), cs_));
+            for (int b = 0; b < nblk; ++b) {
+                const int64_t r0 = (int64_t)b * blk_splits * sp.len, r1 = std::min(N, r0 + blk_splits * sp.len);
+                KNN_CUDA(cudaMemcpyAsync(const_cast<float*>(corpus) + r0 * D, host_corpus + r0 * D,
+                                         (size_t)(r1 - r0) * D * sizeof(float), cudaMemcpyHostToDevice, cs_));
+                KNN_CUDA(cudaEventRecord(oev(2 + b), cs_));
+            }
+        } else {
+            KNN_CUDA(cudaMemcpyAsync(const_cast<float*>(corpus), host_corpus, (size_t)N * D * sizeof(float),
+                                     cudaMemcpyHostToDevice, cs_));
+            KNN_CUDA(cudaEventRecord(oev(2), cs_));
+            KNN_CUDA(cudaStreamWaitEvent(s, oev(2), 0));
+        }
+    }
     cudaEvent_t tv[Engine::kTimingEvents] = {};
     if (o.timing && E.timing_slot(tv) != KNNS_OK) return KNNS_ERR_CUDA;
     auto mark = [&](int i) -> int {
@@ -603,9 +682,12 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     } else {
         KNN_CUDA(cudaMemsetAsync(words, 0, 5 * sizeof(uint32_t), s));
     }
+    // 3xTF32 keys on request: the data count as not BF16-exact (the preparation only ORs into the word)
+    if (o.tf32_only && !bf16_only) KNN_CUDA(cudaMemsetAsync(words + 1, 0x01, 1, s));
     if (c.algo == KNNS_ALGO_TC) {
-        // one pass per input: BF16 copy, exactness test, integrality, norms
-        if (!pc) {
+        // one pass per input: BF16 copy, exactness test, integrality, norms (a streamed corpus:
+        // block by block as the blocks land, below)
+        if (!pc && !streamed) {
             KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, c.dpb, E.bf.p, cn, n_pad, not_exact, s, int_stats,
                                       f8 ? E.f8.p : nullptr, 2 * c.dpf, f8 ? (float*)E.cs.p : nullptr));
             ++launches;
@@ -617,7 +699,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
             KNN_CUDA(launch_prep_rows(queries, Q, ldq, D, c.dpb, scan ? E.qbf.p : nullptr, qn, Q, not_exact, s,
                                       int_stats));
         ++launches;
-        if (!bf16_only && !pc) {
+        if (!bf16_only && !pc && !streamed) {
             // the TF32 split runs only for data that is not BF16-exact
             KNN_CUDA(launch_split(corpus, N, ldc, D, c.dp, (float*)E.hi.p, (float*)E.lo.p, flags, any_lo, not_exact,
                                   s));
@@ -670,6 +752,8 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
             a.dp = c.dp;
             a.kp = kp;
             a.stages = stages;
+            a.timeout_ns = stall_ns;
+            a.test_stall = stall_ns != 0;
             // both precisions are launched; the one that does not match the data returns at once
             if (!bf16_only) {
                 KNN_CUDA(launch_tc(a, splits, false, s));
@@ -689,7 +773,11 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     // in the exact form with the scan on, the shortlist path's selections run only for TF32 data
     const uint32_t* old_gate = scan ? not_exact : nullptr;
 
-    if (run_old) {
+    // The shortlist path (TF32 keys in the exact form; gated on the device by the data's
+    // BF16-exactness when the scan is on).  With a streamed corpus it runs once every block
+    // has landed and been prepared.
+    auto old_path = [&]() -> int {
+        if (!run_old) return KNNS_OK;
         if (pilot) {
             float* cn_s = (float*)E.cn_s.p;
             KNN_CUDA(launch_gather_norms(cn, ns, sample_stride, cn_s, ns_pad, s));
@@ -735,7 +823,9 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
                                    c.rerank ? nullptr : (const float*)E.qn.p, dist, idx, idx_f, s, ex2));
             ++launches;
         }
-    }
+        return KNNS_OK;
+    };
+    if (!streamed && (rc = old_path())) return rc;
 
     if (!scan) {
         for (int i = 2; i <= 5; ++i)
@@ -761,10 +851,13 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         a.ring = sp.ring;
         a.fp8 = f8 ? 1 : 0;
         a.qs = f8 ? (const float*)E.qs.p : nullptr;
-        auto scan_pass = [&](int64_t nview, int64_t stride, const float* cn_view, const float* cs_view,
-                             const float* thr, int splits, int64_t split_len, int cap) -> int {
+        // one scan over rows 0, stride, 2*stride, ... (nview of them) of the operand copy at src;
+        // grid rows are the splits split0 .. split0 + splits - 1, launched on stream ls
+        auto scan_pass = [&](const void* src, int64_t nview, int64_t stride, const float* cn_view,
+                             const float* cs_view, const float* thr, int splits, int64_t split_len, int cap,
+                             int split0 = 0, cudaStream_t ls = nullptr) -> int {
             // the map moves bytes: E4M3 rows are described as rows of 16-bit units
-            int r = encode_rows_bf16(&a.tm_c, f8 ? f8_p : bf_p, nview, sdp, stride * sdp, scan_box_rows(sdp));
+            int r = encode_rows_bf16(&a.tm_c, src, nview, sdp, stride * sdp, scan_box_rows(sdp));
             if (r) return r;
             a.cn = cn_view;
             a.cs = cs_view;
@@ -772,7 +865,8 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
             a.N = nview;
             a.split_len = split_len;
             a.cap = cap;
-            KNN_CUDA(launch_scan(a, splits, s));
+            a.split0 = split0;
+            KNN_CUDA(launch_scan(a, splits, ls ? ls : s));
             ++launches;
             return KNNS_OK;
         };
@@ -784,18 +878,35 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         cs.D = D;
         // seeding, coarse to fine: level l keeps the keys below the previous level's
         // threshold (the coarsest keeps every key) and yields the key of rank j_l
+        // (a streamed corpus: the levels read the sample copied ahead of the corpus, whose
+        // row r is corpus row sp.stride0 * r -- the same rows, prepared by the same pass)
+        const void* key_src = f8 ? f8_p : bf_p;
+        const float* lv_cn = cn;
+        const float* lv_cs = cs_p;
+        int64_t lv_div = 1;
+        if (streamed) {
+            KNN_CUDA(cudaStreamWaitEvent(s, oev(1), 0));
+            KNN_CUDA(launch_prep_rows((const float*)E.smp.p, smp_n, D, D, c.dpb, E.smp_bf.p, (float*)E.smp_cn.p,
+                                      smp_pad, not_exact, s, int_stats, f8 ? E.smp_f8.p : nullptr, 2 * c.dpf,
+                                      f8 ? (float*)E.smp_cs.p : nullptr));
+            ++launches;
+            key_src = f8 ? E.smp_f8.p : E.smp_bf.p;
+            lv_cn = (const float*)E.smp_cn.p;
+            lv_cs = (const float*)E.smp_cs.p;
+            lv_div = sp.stride0;
+        }
         float* cnv = (float*)E.cnv.p;
         float* csv = f8 ? (float*)E.csv.p : nullptr;
         const float* T = nullptr;
         for (int l = 0; l < sp.levels; ++l) {
             const ScanLevel& v = sp.lv[l];
-            KNN_CUDA(launch_gather_norms(cn, v.n, v.stride, cnv, v.n_pad, s));
+            KNN_CUDA(launch_gather_norms(lv_cn, v.n, v.stride / lv_div, cnv, v.n_pad, s));
             if (f8) {
                 // scales of the sample rows, 0 for padding (whose +inf norms keep their keys at +inf)
-                KNN_CUDA(launch_gather_norms(cs_p, v.n, v.stride, csv, v.n_pad, s, 0.f));
+                KNN_CUDA(launch_gather_norms(lv_cs, v.n, v.stride / lv_div, csv, v.n_pad, s, 0.f));
                 ++launches;
             }
-            if ((rc = scan_pass(v.n, v.stride, cnv, csv, T, v.S, v.len, v.cap))) return rc;
+            if ((rc = scan_pass(key_src, v.n, v.stride / lv_div, cnv, csv, T, v.S, v.len, v.cap))) return rc;
             cs.nseg = kScanParts * v.S;
             cs.cap = v.cap;
             cs.thr_out = Tbuf[l & 1];
@@ -809,7 +920,39 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         }
         if ((rc = mark(2))) return rc;
         // main pass
-        if ((rc = scan_pass(N, 1, cn, cs_p, T, sp.S, sp.len, sp.cap))) return rc;
+        if (!streamed) {
+            if ((rc = scan_pass(f8 ? f8_p : bf_p, N, 1, cn, cs_p, T, sp.S, sp.len, sp.cap))) return rc;
+        } else {
+            // block by block: prepared on the search stream once landed, scanned on a worker
+            // stream (blocks scanned on the two workers overlap each other's tails)
+            for (int b = 0; b < nblk; ++b) {
+                const int64_t r0 = (int64_t)b * blk_splits * sp.len, r1 = std::min(N, r0 + blk_splits * sp.len);
+                const bool last = b == nblk - 1;
+                KNN_CUDA(cudaStreamWaitEvent(s, oev(2 + b), 0));
+                KNN_CUDA(launch_prep_rows(corpus + r0 * D, r1 - r0, D, D, c.dpb, (char*)E.bf.p + (size_t)r0 * c.dpb * 2,
+                                          cn + r0, last ? n_pad - r0 : r1 - r0, not_exact, s, int_stats,
+                                          f8 ? (char*)E.f8.p + (size_t)r0 * c.dpf * 2 : nullptr, 2 * c.dpf,
+                                          f8 ? (float*)E.cs.p + r0 : nullptr));
+                ++launches;
+                KNN_CUDA(cudaEventRecord(oev(2 + nblk + b), s));
+                cudaStream_t w = E.worker_stream(b % Engine::kScanWorkers);
+                if (!w) return set_error(KNNS_ERR_CUDA, "stream creation failed");
+                KNN_CUDA(cudaStreamWaitEvent(w, oev(2 + nblk + b), 0));
+                const int sb = std::min(blk_splits, sp.S - b * blk_splits);
+                if ((rc = scan_pass(f8 ? f8_p : bf_p, N, 1, cn, cs_p, T, sb, sp.len, sp.cap, b * blk_splits, w)))
+                    return rc;
+                KNN_CUDA(cudaEventRecord(oev(2 + 2 * nblk + b), w));
+            }
+            for (int b = 0; b < nblk; ++b) KNN_CUDA(cudaStreamWaitEvent(s, oev(2 + 2 * nblk + b), 0));
+            // what needs the whole corpus: the TF32 copies and the shortlist path (gated on the
+            // data's BF16-exactness in the exact form)
+            if (!bf16_only) {
+                KNN_CUDA(launch_split(corpus, N, ldc, D, c.dp, (float*)E.hi.p, (float*)E.lo.p, flags, any_lo,
+                                      not_exact, s));
+                ++launches;
+            }
+            if ((rc = old_path())) return rc;
+        }
         if ((rc = mark(3))) return rc;
         KNN_CUDA(cudaMemsetAsync(fail_cnt, 0, sizeof(uint32_t), s));
         cs.nseg = kScanParts * sp.S;
@@ -841,6 +984,21 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         // (launches whose rows are all past the failure count return at once)
         auto fix_pass = [&](int64_t qbase, int64_t rows, int splits, int64_t split_len) -> int {
             if (rows <= 0) return KNNS_OK;
+            if (sp.simt_fix) {
+                // long shortlists: the CUDA-core kernel with exact FP32 keys, compacted rows
+                uint32_t* thr2 = (uint32_t*)E.thr2.p;
+                KNN_CUDA(cudaMemsetAsync(thr2, 0xFF, rows * sizeof(uint32_t), s));
+                KNN_CUDA(launch_simt(corpus, N, ldc, cn, queries, rows, ldq, D, c.kp, 32, split_len, splits, part,
+                                     thr2, s, nullptr, fail_idx, fail_cnt, qbase));
+                SelectExtra ex;
+                ex.qmap = fail_idx;
+                ex.qcount = fail_cnt;
+                ex.qbase = qbase;
+                KNN_CUDA(launch_select(part, splits, rows, c.kp, k, corpus, ldc, queries, ldq, D, c.rerank,
+                                       c.rerank ? nullptr : (const float*)E.qn.p, dist, idx, idx_f, s, ex));
+                launches += 2;
+                return KNNS_OK;
+            }
             TcArgs t;
             memset(&t, 0, sizeof(t));
             int r = encode_rows_bf16(&t.tm_bf, bf_p, N, c.dpb, c.dpb);
@@ -1044,11 +1202,11 @@ int search_host(const float* corpus, int64_t N, const float* queries, int64_t Q,
     if ((rc = E->out_idx.ensure(std::max(ob * 4, (size_t)4)))) return rc;
     cudaEvent_t t0 = E->t0(), t1 = E->t1();
     KNN_CUDA(cudaEventRecord(t0, s));
-    KNN_CUDA(cudaMemcpyAsync(E->in_corpus.p, corpus, cb, cudaMemcpyHostToDevice, s));
     if (qb) KNN_CUDA(cudaMemcpyAsync(E->in_queries.p, queries, qb, cudaMemcpyHostToDevice, s));
+    // the corpus is copied by the search itself, in blocks that overlap its computation
     rc = run_search(*E, (const float*)E->in_corpus.p, N, D, (const float*)E->in_queries.p, Q, D, D, k,
                     dist ? (float*)E->out_dist.p : nullptr, idx ? (int32_t*)E->out_idx.p : nullptr,
-                    idx_f_host ? (float*)E->out_idx.p : nullptr, o, s, st);
+                    idx_f_host ? (float*)E->out_idx.p : nullptr, o, s, st, nullptr, false, corpus);
     if (rc) return rc;
     if (dist && ob) KNN_CUDA(cudaMemcpyAsync(dist, E->out_dist.p, ob * 4, cudaMemcpyDeviceToHost, s));
     if (idx && ob) KNN_CUDA(cudaMemcpyAsync(idx, E->out_idx.p, ob * 4, cudaMemcpyDeviceToHost, s));
@@ -1081,6 +1239,33 @@ cudaStream_t Engine::host_stream()
         if (cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking) != cudaSuccess) stream_ = nullptr;
     }
     return stream_;
+}
+
+cudaStream_t Engine::copy_stream()
+{
+    if (!copy_) {
+        if (cudaStreamCreateWithFlags(&copy_, cudaStreamNonBlocking) != cudaSuccess) copy_ = nullptr;
+    }
+    return copy_;
+}
+
+cudaStream_t Engine::worker_stream(int i)
+{
+    if (i < 0 || i >= kScanWorkers) return nullptr;
+    if (!workers_[i]) {
+        if (cudaStreamCreateWithFlags(&workers_[i], cudaStreamNonBlocking) != cudaSuccess) workers_[i] = nullptr;
+    }
+    return workers_[i];
+}
+
+cudaEvent_t Engine::order_event(int i)
+{
+    while ((int)order_.size() <= i) {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+        order_.push_back(e);
+    }
+    return order_[(size_t)i];
 }
 
 cudaEvent_t Engine::t0()
@@ -1191,6 +1376,27 @@ int knns_last_fixups(int64_t* out)
 }
 
 int knns_version(void) { return 100; }
+
+int knns_merge_topk(const float* run_d, const int32_t* run_i, int have, const float* blk_d, const int32_t* blk_i,
+                    int kb, int32_t offset, int64_t Q, int k, float* out_d, int32_t* out_i, void* stream)
+{
+    clear_error();
+    if (Q < 0 || k < 1 || have < 0 || have > k || kb < 0 || kb > k)
+        return set_error(KNNS_ERR_INVALID, "merge: bad sizes Q=%lld k=%d have=%d kb=%d", (long long)Q, k, have, kb);
+    if (Q > 0 && (!out_d || !out_i || (have > 0 && (!run_d || !run_i)) || (kb > 0 && (!blk_d || !blk_i))))
+        return set_error(KNNS_ERR_INVALID, "merge: null pointer");
+    KNN_CUDA(launch_merge_topk(run_d, run_i, have, blk_d, blk_i, kb, offset, Q, k, out_d, out_i, nullptr,
+                               (cudaStream_t)stream));
+    return KNNS_OK;
+}
+
+int knns_debug_stall_next_search(int64_t timeout_us)
+{
+    clear_error();
+    if (timeout_us <= 0 || timeout_us > 10000000) return set_error(KNNS_ERR_INVALID, "timeout outside (0, 10 s]");
+    g_test_stall_ns.store((uint64_t)timeout_us * 1000u);
+    return KNNS_OK;
+}
 
 static int timing_collect(double ms[Engine::kTimingEvents - 1], int* count)
 {
@@ -1321,7 +1527,7 @@ int knns_autotune_shortlist(knns_index* ix, const float* queries, int64_t Q, int
     int last_c = 0;
     for (int c : {2, 4, 8}) {
         if (rc) break;
-        if ((int64_t)c * k > kMaxKpTC && c != 2) break;  // the shortlist holds at most kMaxKpTC entries
+        if ((int64_t)c * k > kMaxKpScan && c != 2) break;  // the shortlist holds at most kMaxKpScan entries
         rc = run(precision, c, got);
         if (rc) break;
         int64_t hit = 0;

@@ -53,6 +53,9 @@ struct Engine {
     DevBuf in_corpus, in_queries, out_dist, out_idx;
     // corpus blocks of host-buffer searches: two running top-k lists (distances, indices)
     DevBuf mrg;
+    // host-buffer searches with the threshold scan: the seeding sample (every 32nd corpus row)
+    // copied ahead of the corpus, and its norms, BF16 copy, E4M3 codes and scales
+    DevBuf smp, smp_cn, smp_bf, smp_f8, smp_cs;
     // stage timing: kTimingEvents events per timed search (start, after prep,
     // after threshold seeding, after the main fused kernel, after the main
     // selection, end)
@@ -63,10 +66,17 @@ struct Engine {
     cudaStream_t host_stream();
     cudaEvent_t t0();
     cudaEvent_t t1();
+    // host-buffer searches: the stream that copies the corpus in, the streams that scan the
+    // blocks already landed, and a pool of ordering events (null on failure)
+    static constexpr int kScanWorkers = 2;
+    cudaStream_t copy_stream();
+    cudaStream_t worker_stream(int i);
+    cudaEvent_t order_event(int i);
 
   private:
-    cudaStream_t stream_ = nullptr;
+    cudaStream_t stream_ = nullptr, copy_ = nullptr, workers_[kScanWorkers] = {};
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    std::vector<cudaEvent_t> order_;
 };
 
 // A corpus prepared once and kept resident (the serving index): BF16 copy,
@@ -92,9 +102,15 @@ int resolve_config(const Engine& E, int64_t N, int64_t Q, int D, int k, const kn
 // pc (optional): the corpus arrives prepared (its preparation is skipped).
 // capture: the call is being captured into a CUDA graph: no host-side event
 // ordering against earlier calls (the caller serialises its stream).
+// host_corpus (optional): the corpus is still in host memory (N x D, contiguous rows) and
+// `corpus` is its device destination (ldc = D): the search copies it in on the engine's copy
+// stream -- the threshold scan's seeding sample first, then blocks aligned to the main scan's
+// splits -- and prepares and scans each block as soon as it has landed, so the copy overlaps
+// the computation.  Results are identical to a search of the resident corpus.
 int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const float* queries, int64_t Q, int64_t ldq,
                int D, int k, float* dist, int32_t* idx, float* idx_f, const knns_options& o, cudaStream_t s,
-               knns_stats* st, const PreparedCorpus* pc = nullptr, bool capture = false);
+               knns_stats* st, const PreparedCorpus* pc = nullptr, bool capture = false,
+               const float* host_corpus = nullptr);
 int prepare_corpus(Engine& E, PreparedCorpus* pc, const float* corpus, int64_t N, int64_t ldc, int D, bool tf32,
                    cudaStream_t s, bool fp8 = false);
 int check_device_error(Engine& E, cudaStream_t s);

@@ -34,9 +34,16 @@ __global__ void __launch_bounds__(kThreads)
 simt_kernel(const float* __restrict__ corpus, int64_t N, int64_t ldc, const float* __restrict__ cn,
             const float* __restrict__ queries, int64_t Q, int64_t ldq, int D, int kp,
             int64_t split_len, uint64_t* __restrict__ part, uint32_t* __restrict__ thr_g_all,
-            const uint32_t* __restrict__ tile_redo)
+            const uint32_t* __restrict__ tile_redo, const int32_t* __restrict__ qmap,
+            const uint32_t* __restrict__ qcount, int64_t qbase)
 {
     if (tile_redo != nullptr && tile_redo[blockIdx.x] == 0u) return;
+    // compacted rows: row r is query qmap[qbase + r], present while qbase + r < *qcount
+    int64_t qvalid = Q;
+    if (qcount != nullptr) {
+        qvalid = min(Q, (int64_t)*qcount - qbase);
+        if ((int64_t)blockIdx.x * QPB >= qvalid) return;
+    }
     constexpr int RQ = QPB / 16;
     extern __shared__ __align__(16) unsigned char smem[];
     float* qs = reinterpret_cast<float*>(smem);
@@ -60,8 +67,8 @@ simt_kernel(const float* __restrict__ corpus, int64_t N, int64_t ldc, const floa
 
     const bool owner = tid < QPB;
     const int64_t q = q0 + tid;
-    LaneState st{0, q < Q ? __int_as_float(0x7f800000) : -__int_as_float(0x7f800000)};
-    uint32_t* thr_g = (owner && q < Q) ? thr_g_all : nullptr;
+    LaneState st{0, q < qvalid ? __int_as_float(0x7f800000) : -__int_as_float(0x7f800000)};
+    uint32_t* thr_g = (owner && q < qvalid) ? thr_g_all : nullptr;
     const int tx = tid & 15, ty = tid >> 4;
 
     for (int64_t n0 = n_begin; n0 < n_end; n0 += kNT) {
@@ -75,7 +82,10 @@ simt_kernel(const float* __restrict__ corpus, int64_t N, int64_t ldc, const floa
             for (int i = tid; i < QPB * kKC; i += kThreads) {
                 int q = i / kKC, d = i - q * kKC;
                 float val = 0.f;
-                if (q0 + q < Q && d0 + d < D) val = __ldg(queries + (q0 + q) * ldq + d0 + d);
+                if (q0 + q < qvalid && d0 + d < D) {
+                    const int64_t src = qmap != nullptr ? (int64_t)__ldg(qmap + qbase + q0 + q) : q0 + q;
+                    val = __ldg(queries + src * ldq + d0 + d);
+                }
                 qs[d * (QPB + 4) + q] = val;
             }
             for (int i = tid; i < kNT * kKC; i += kThreads) {
@@ -131,7 +141,7 @@ simt_kernel(const float* __restrict__ corpus, int64_t N, int64_t ldc, const floa
     if (owner) st = flush_all(v, tid, st);
     __syncthreads();
     uint64_t* out = part + ((size_t)blockIdx.y * Q + q0) * kp;
-    const int64_t nq = min((int64_t)QPB, Q - q0);
+    const int64_t nq = min((int64_t)QPB, qvalid - q0);
     for (int64_t i = tid; i < nq * kp; i += kThreads) out[i] = v.list[i];
 }
 
@@ -143,8 +153,9 @@ size_t simt_smem_bytes(int qpb, int kp)
 cudaError_t launch_simt(const float* corpus, int64_t N, int64_t ldc, const float* cn,
                         const float* queries, int64_t Q, int64_t ldq, int D, int kp, int qpb,
                         int64_t split_len, int splits, uint64_t* part, uint32_t* thr_g, cudaStream_t s,
-                        const uint32_t* tile_redo)
+                        const uint32_t* tile_redo, const int32_t* qmap, const uint32_t* qcount, int64_t qbase)
 {
+    if ((qmap == nullptr) != (qcount == nullptr) || qbase < 0) return cudaErrorInvalidValue;
     size_t smem = simt_smem_bytes(qpb, kp);
     dim3 grid((unsigned)((Q + qpb - 1) / qpb), (unsigned)splits);
     if (qpb == 128) {
@@ -152,13 +163,13 @@ cudaError_t launch_simt(const float* corpus, int64_t N, int64_t ldc, const float
                                              (int)smem);
         if (e != cudaSuccess) return e;
         simt_kernel<128><<<grid, kThreads, smem, s>>>(corpus, N, ldc, cn, queries, Q, ldq, D, kp,
-                                                      split_len, part, thr_g, tile_redo);
+                                                      split_len, part, thr_g, tile_redo, qmap, qcount, qbase);
     } else {
         cudaError_t e = cudaFuncSetAttribute(simt_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
         simt_kernel<32><<<grid, kThreads, smem, s>>>(corpus, N, ldc, cn, queries, Q, ldq, D, kp,
-                                                     split_len, part, thr_g, tile_redo);
+                                                     split_len, part, thr_g, tile_redo, qmap, qcount, qbase);
     }
     return cudaGetLastError();
 }

@@ -56,7 +56,7 @@ constexpr int kStagePitch = 33;                    // staged keys: [4 warps][32 
 constexpr uint32_t kKeyStageBytes = 4u * 32u * kStagePitch * 4u;
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kAccCol = 256;
-constexpr uint64_t kTimeoutNs = 4000000000ull;
+constexpr uint64_t kTimeoutNs = 4000000000ull;  // bound of every barrier wait unless TcArgs names another
 constexpr uint32_t kIdesc = ptx::idesc_tf32(kTileQ, kTileN);
 constexpr uint32_t kIdescBf16 = ptx::idesc_bf16(kTileQ, kTileN);
 constexpr int kBoxElemsBf16 = 64;                  // bf16 elements per 128-byte swizzle row
@@ -115,12 +115,14 @@ __device__ __forceinline__ void tc_fail(const TcArgs& a, const TcSmem& s, int co
     *s.abort = 1;
 }
 
+__device__ __forceinline__ uint64_t tc_timeout(const TcArgs& a) { return a.timeout_ns ? a.timeout_ns : kTimeoutNs; }
+
 __device__ __forceinline__ bool tc_wait(const TcArgs& a, const TcSmem& s, uint64_t* bar, uint32_t parity, int code)
 {
     // a completed barrier returns before the abort flag is read; a wait that would block sees it first
     if (ptx::mbar_try_wait(bar, parity)) return true;
     if (*s.abort) return false;
-    if (ptx::mbar_wait(bar, parity, kTimeoutNs)) return true;
+    if (ptx::mbar_wait(bar, parity, tc_timeout(a))) return true;
     tc_fail(a, s, code);
     return false;
 }
@@ -257,7 +259,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
 
     if (warp == 0) {
         // ------------------------------------------------------------ producer
-        if (lane == 0) {
+        // (test_stall: no copy is ever issued, so the first data wait of the MMA issuer and the
+        // epilogue's accumulator wait run out: the bounded-wait wind-down is exercised, with
+        // nothing in flight)
+        if (lane == 0 && !a.test_stall) {
             int it = 0;
             bool ok = true;
             const int64_t tile0 = n_begin / kTileN;
@@ -296,7 +301,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
                 // let copies already issued land before the CTA winds down
                 const int first = it - nslot > 0 ? it - nslot : 0;
                 for (int j = first; j < it; ++j)
-                    ptx::mbar_wait(&s.full[j % nslot], (uint32_t)(j / nslot) & 1u, kTimeoutNs);
+                    ptx::mbar_wait(&s.full[j % nslot], (uint32_t)(j / nslot) & 1u, tc_timeout(a));
             }
         }
     } else if (warp == 1) {
@@ -353,7 +358,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(const __grid_constant
             }
             // all MMAs issued by this thread retire before TMEM is released
             ptx::mma_commit(s.drain);
-            ptx::mbar_wait(s.drain, 0, kTimeoutNs);
+            ptx::mbar_wait(s.drain, 0, tc_timeout(a));
         }
     } else {
         // ------------------------------------------------------------ epilogue

@@ -54,10 +54,13 @@ cudaError_t launch_prep_rows(const float* x, int64_t n, int64_t ld, int D, int d
 // CUDA-core FP32 fused distance + shortlist.  qpb in {32, 128}.
 size_t simt_smem_bytes(int qpb, int kp);
 // tile_redo (optional): a CTA runs only when tile_redo[blockIdx.x] != 0.
+// qmap / qcount / qbase (optional, together): compacted rows, as for TcArgs -- row r of the
+// launch (r < Q) is query qmap[qbase + r], present only when qbase + r < *qcount.
 cudaError_t launch_simt(const float* corpus, int64_t N, int64_t ldc, const float* cn,
                         const float* queries, int64_t Q, int64_t ldq, int D, int kp, int qpb,
                         int64_t split_len, int splits, uint64_t* part, uint32_t* thr_g, cudaStream_t s,
-                        const uint32_t* tile_redo = nullptr);
+                        const uint32_t* tile_redo = nullptr, const int32_t* qmap = nullptr,
+                        const uint32_t* qcount = nullptr, int64_t qbase = 0);
 
 // Tensor-core 3xTF32 fused distance + shortlist (tcgen05, TMA, TMEM).
 struct TcArgs {
@@ -88,6 +91,8 @@ struct TcArgs {
     int dpb;                  // D rounded up to 64 (BF16 boxes)
     int kp;
     int stages;
+    uint64_t timeout_ns;      // bound of every barrier wait (0: 4 s)
+    int test_stall;           // test hook: the producer issues no copy, so the waits run out
 };
 size_t tc_smem_bytes(int kp, int stages);
 int tc_max_stages(int kp);
@@ -128,10 +133,11 @@ struct ScanArgs {
     int bps;                   // K-boxes per ring slot (divides dpb/64)
     int ring;                  // ring slots
     int fp8;                   // keys from E4M3 operands with per-row scales
+    int split0;                // first split of this launch (grid row y is split split0 + y)
 };
 // corpus rows per tile (MMA N): 224 for dpb <= 128, 192 for dpb <= 256
 int scan_tile_rows(int dpb);
-// rows of the corpus tensor map's box: the share of a tile one CTA of a cluster loads
+// rows of the corpus tensor map's box (one whole tile)
 int scan_box_rows(int dpb);
 // most columns of one tile that a single candidate segment (epilogue part) collects
 int scan_part_cols(int dpb);
@@ -179,6 +185,7 @@ cudaError_t launch_select(const uint64_t* part, int splits, int64_t Q, int kp, i
 //    trusted (overflow, total < need, total > kCandMax) is appended to
 //    fail_idx (count in *fail_cnt) and gets no result.
 constexpr int kCandMax = 2048;
+constexpr int kMaxKpScan = 512;  // longest shortlist the threshold scan's selection keeps
 constexpr int kScanMaxSegs = 512;  // candidate segments per query (splits x kScanParts)
 struct CandSelect {
     const uint64_t* cand = nullptr;

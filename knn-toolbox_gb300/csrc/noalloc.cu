@@ -14,6 +14,7 @@
 // library keeps until the process exits.  It runs the CUDA-core fused kernel
 // (the tensor-core kernel needs TF32 copies of the corpus, too large for a
 // fixed array) followed by the shortlist merge / re-rank kernel.
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -42,7 +43,11 @@ inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Device address of the scratch array on the current device.  In host code
 // the array's name is only a host-side stand-in, so the address is looked up
-// once per device (with that device current) and cached.
+// once per device (with that device current) and cached.  Under lazy module
+// loading (the CUDA default) this first lookup is also what loads the module
+// and reserves the array's device memory.  The cached address belongs to the
+// device's primary context: after a cudaDeviceReset it is stale (as is every
+// buffer the engine keeps), so the entry point is not to be used across one.
 int scratch_address(void** out)
 {
     int dev = 0;
@@ -68,6 +73,13 @@ using namespace knn;
 
 extern "C" {
 
+int knns_noalloc_prepare(void)
+{
+    clear_error();
+    void* p = nullptr;
+    return scratch_address(&p);
+}
+
 int knns_search_device_noalloc(const float* corpus, int64_t N, int64_t ldc, const float* queries, int64_t Q,
                                int64_t ldq, int D, int k, float* dist, int32_t* idx, void* stream)
 {
@@ -80,7 +92,10 @@ int knns_search_device_noalloc(const float* corpus, int64_t N, int64_t ldc, cons
     if (!corpus || (Q > 0 && !queries)) return set_error(KNNS_ERR_INVALID, "null input pointer");
     if (Q == 0) return KNNS_OK;
 
-    const int kp = auto_kp(k, 1);
+    // the shortlist of the regular entry point's CUDA-core path: k plus the re-rank margin,
+    // without the margin where that would pass the kernel's 512 entries
+    int kp = auto_kp(k, 1);
+    if (kp > 512 && k <= 512) kp = std::max((k + 15) & ~15, 32);
     if (kp > 512) return set_error(KNNS_ERR_UNSUPPORTED, "k=%d needs a shortlist above 512 entries", k);
     const int qtile = kp <= 128 ? 128 : 32;
     const int64_t n_pad = cdiv64(N, 128) * 128;

@@ -21,14 +21,12 @@
 // for up to 128 BF16 columns, 192 for up to 256.  Tensor memory holds two
 // TN-column FP32 accumulators and the A operand (this CTA's queries) in the
 // remaining dpb/2 columns, so shared memory carries only the corpus tiles
-// (a ring of whole tiles where three fit) and their norms.
-// Clusters of two CTAs (neighbouring query tiles, same corpus split) share
-// every corpus tile: each CTA loads half of each box's rows with a multicast
-// TMA into both, and each MMA commit releases the slot in both.
+// (a ring of whole tiles where three fit) and their norms.  Every CTA loads
+// its own corpus tiles (CTAs of neighbouring query tiles read the same tiles
+// from L2 at about the same time).
 // Warp roles (608 threads):
-//   warp 0      producer: per tile its half of the corpus K-boxes (2-D TMA
-//               multicast, 64 bf16 x TN/2 rows, 128-byte swizzle) and the
-//               corpus norms (1-D bulk copy);
+//   warp 0      producer: per tile the corpus K-boxes (2-D TMA, 64 bf16 x TN
+//               rows, 128-byte swizzle) and the corpus norms (1-D bulk copy);
 //   warp 1      TMEM owner (512 columns) and MMA issuer of the even tiles
 //               (tcgen05.mma kind::f16 / kind::f8f6f4, A from TMEM, B from
 //               shared memory) into accumulator 0;
@@ -63,11 +61,6 @@ constexpr int kEpiWarps = 4 * kScanParts;  // 4 TMEM lane quarters x kScanParts 
 constexpr int kIssuers = 2;                 // MMA issuing threads (warps 1 and 2 + kEpiWarps)
 constexpr int kScanThreads = 32 * (1 + kIssuers + kEpiWarps);
 constexpr int kNormSlots = 8;
-// CTAs per cluster: the cluster's CTAs work on neighbouring query tiles of the
-// same corpus split; each TMA-loads 1/kCluster of every corpus box's rows and
-// multicasts it to all of them, so L2 delivers each tile once per cluster.
-constexpr int kCluster = 2;
-constexpr uint16_t kClusterMask = (1u << kCluster) - 1u;
 constexpr uint32_t kCtrlBytes = 512;
 constexpr uint32_t kTmemCols = 512;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
@@ -166,15 +159,13 @@ __device__ __forceinline__ void chunk_append(const float (&key)[W], uint32_t gm,
 }
 
 template <int TN, bool kF8>
-__global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads, 1)
+__global__ void __launch_bounds__(kScanThreads, 1)
     scan_kernel(const __grid_constant__ ScanArgs a)
 {
     constexpr int TW = TN / kScanParts - 32;  // tail columns per epilogue part (24 or 16)
     constexpr uint32_t kBoxB = box_bytes(TN);
     constexpr uint32_t kIdesc = kF8 ? ptx::idesc_e4m3(kTileQ, TN) : ptx::idesc_bf16(kTileQ, TN);
     constexpr uint32_t kACol = 2u * TN;  // A operand columns [kACol, kACol + dpb/2)
-    constexpr int kPieceRows = TN / kCluster;  // rows of every box this CTA loads for the cluster
-    static_assert(kPieceRows % 8 == 0, "pieces of whole 8-row swizzle atoms");
     static_assert(TW == 24 || TW == 16, "tail chunk of 16 or 24 columns");
 
     extern __shared__ __align__(1024) unsigned char sm[];
@@ -210,14 +201,15 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads,
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int64_t q0 = (int64_t)blockIdx.x * kTileQ;
-    const int64_t n_begin = (int64_t)blockIdx.y * a.split_len;
+    const int split = a.split0 + (int)blockIdx.y;
+    const int64_t n_begin = (int64_t)split * a.split_len;
     const int64_t n_end = min(a.N, n_begin + a.split_len);
     const int ntiles = n_end > n_begin ? (int)((n_end - n_begin + TN - 1) / TN) : 0;
 
     if (tid == 0) {
         for (int i = 0; i < R; ++i) {
             ptx::mbar_init(&s.full[i], 1);
-            ptx::mbar_init(&s.empty[i], kCluster);  // one MMA commit from every CTA of the cluster
+            ptx::mbar_init(&s.empty[i], 1);
         }
         for (int b = 0; b < 2; ++b) {
             ptx::mbar_init(&s.accf[b], 1);
@@ -241,9 +233,6 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads,
     __syncthreads();
     ptx::tc_fence_after();
     const uint32_t tmem = *s.tmem_holder;
-    // every CTA's barriers are initialised before any multicast copy or commit reaches them
-    ptx::cluster_sync();
-    const uint32_t crank = ptx::cluster_ctarank();
 
     if (warp == 0) {
         // ------------------------------------------------------------ producer
@@ -257,11 +246,9 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads,
                     const uint32_t ph = (uint32_t)(it / R) & 1u;
                     if (!scan_wait(a, s, &s.empty[st], ph ^ 1u, kDevTimeoutProducer)) { ok = false; break; }
                     unsigned char* dst = s.ring + (size_t)st * slot_bytes;
-                    // this CTA's piece of every box, multicast: the slot fills when all pieces land
                     ptx::mbar_arrive_expect_tx(&s.full[st], slot_bytes);
                     for (int bx = 0; bx < bps; ++bx)
-                        ptx::tma_load_2d_mc(dst + (size_t)bx * kBoxB + crank * (kPieceRows * 128u), &a.tm_c, &s.full[st],
-                                            (c * bps + bx) * 64, (int)(n0 + crank * kPieceRows), kClusterMask);
+                        ptx::tma_load_2d(dst + (size_t)bx * kBoxB, &a.tm_c, &s.full[st], (c * bps + bx) * 64, (int)n0);
                 }
                 if (!ok) break;
                 // norms (needed by the epilogue only, after the MMAs); the array is padded
@@ -320,8 +307,7 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads,
                     // after the tile's last MMAs the accumulator-ready commit goes first: the
                     // epilogue is on the critical path, the producer has the ring's slack
                     if (c == slots_per_tile - 1) ptx::mma_commit(&s.accf[b]);
-                    // the slot is free once every CTA of the cluster has consumed it
-                    ptx::mma_commit_mc(&s.empty[st], kClusterMask);
+                    ptx::mma_commit(&s.empty[st]);
                 }
                 if (!ok) break;
             }
@@ -357,7 +343,7 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads,
         // padding lanes of the last query tile collect nothing
         const float T = valid ? (a.thr ? __ldg(a.thr + q) : __int_as_float(0x7f800000)) : -__int_as_float(0x7f800000);
         const float m = kF8 ? -2.0f * (valid ? __ldg(a.qs + q) : 0.f) : -2.0f;
-        const size_t seg = (size_t)blockIdx.y * kScanParts + part;
+        const size_t seg = (size_t)split * kScanParts + part;
         uint64_t* out = a.cand + (seg * (size_t)a.Q + (size_t)(valid ? q : 0)) * (size_t)a.cap;
         uint32_t cnt = 0;
         const uint32_t cap = (uint32_t)a.cap;
@@ -413,14 +399,12 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kScanThreads,
         __syncwarp();
         ptx::tmem_dealloc(tmem, kTmemCols);
     }
-    // no CTA leaves while another may still multicast into it or arrive on its barriers
-    ptx::cluster_sync();
 }
 }  // namespace
 
 int scan_tile_rows(int dpb) { return dpb <= 128 ? 224 : 192; }
 
-int scan_box_rows(int dpb) { return scan_tile_rows(dpb) / kCluster; }
+int scan_box_rows(int dpb) { return scan_tile_rows(dpb); }
 
 // every epilogue part collects the same share of a tile's columns
 int scan_part_cols(int dpb) { return scan_tile_rows(dpb) / kScanParts; }
@@ -473,15 +457,14 @@ cudaError_t launch_scan(const ScanArgs& a, int splits, cudaStream_t st)
     const int tn = scan_tile_rows(a.dpb);
     const bool f8 = a.fp8 != 0;
     if (a.dpb % 64 != 0 || nbox < 1 || nbox > 4 || a.bps < 1 || nbox % a.bps != 0 || a.ring < 2 ||
-        a.ring > kScanMaxRing || a.split_len % tn != 0 || a.cap < 1 || splits < 1 || a.qbf == nullptr ||
+        a.ring > kScanMaxRing || a.split_len % tn != 0 || a.cap < 1 || splits < 1 || a.split0 < 0 || a.qbf == nullptr ||
         a.ksteps < 1 || a.ksteps > 4 * nbox || (f8 && (a.cs == nullptr || a.qs == nullptr)))
         return cudaErrorInvalidValue;
     const size_t smem = scan_smem_bytes(a.dpb, a.bps, a.ring, f8);
     if (smem > kScanSmemLimit) return cudaErrorInvalidValue;
     if (a.Q <= 0) return cudaSuccess;
-    // whole clusters: a padding query tile (all rows past Q) still loads its share of the corpus
     const int64_t qt = (a.Q + kTileQ - 1) / kTileQ;
-    dim3 grid((unsigned)((qt + kCluster - 1) / kCluster * kCluster), (unsigned)splits);
+    dim3 grid((unsigned)qt, (unsigned)splits);
     if (tn == 224) return f8 ? launch_scan_t<224, true>(a, grid, smem, st) : launch_scan_t<224, false>(a, grid, smem, st);
     return f8 ? launch_scan_t<192, true>(a, grid, smem, st) : launch_scan_t<192, false>(a, grid, smem, st);
 }

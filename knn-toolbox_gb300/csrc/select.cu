@@ -500,11 +500,11 @@ cudaError_t launch_select_cand(const CandSelect& c_in, cudaStream_t s)
     // buffer's limit at the coarse seeding levels; a smaller buffer lets more warps run
     if (thr)
         c.buf_words = (int)std::min<int64_t>(kCandThrMax, ((int64_t)c.nseg * c.cap + 31) / 32 * 32);
-    else if (c.kp >= 1 && c.kp <= kMaxKpTC)
+    else if (c.kp >= 1 && c.kp <= kMaxKpScan)
         c.buf_words = c.buf_words > 0 ? std::min(kCandMax, std::max((c.buf_words + 31) / 32 * 32, pow2_at_least(c.kp)))
                                       : kCandMax;
     if (c.nseg < 1 || c.nseg > kScanMaxSegs || c.cap < 1 ||
-        (!thr && (c.kp < 1 || c.kp > kMaxKpTC || c.k > c.kp || c.fail_idx == nullptr || c.fail_cnt == nullptr ||
+        (!thr && (c.kp < 1 || c.kp > kMaxKpScan || c.k > c.kp || c.fail_idx == nullptr || c.fail_cnt == nullptr ||
                   (!c.rerank && c.qn == nullptr))) ||
         (thr && (c.thr_rank < 1 || c.thr_rank > kCandThrMax)))
         return cudaErrorInvalidValue;

@@ -6,8 +6,13 @@
 // and k arrive at any time (knns_server_submit) and one worker thread packs
 // them into launches:
 //   * admission: a request is admitted into a batch when it fits the batch's
-//     workspace (at most max_batch queries per launch; one k per launch, so a
-//     request's computation is the one it would get alone);
+//     workspace (at most max_batch queries per launch).  In the exact form
+//     requests of different k share a launch: it runs with the largest k of its
+//     requests and each request keeps the first k of its rows -- the results
+//     are sorted by (distance, index), so that prefix is the request's own
+//     top-k, the one it gets alone.  In the BF16 / FP8 forms the shortlist
+//     length is c*k, so a launch takes one k (a request's recall is then the
+//     one it gets alone);
 //   * slots: `slots` batches are in flight at once, each on its own stream with
 //     its own workspace, so a batch formed while another runs overlaps it on the
 //     device; as a slot completes, its requests are answered and the slot takes
@@ -315,9 +320,14 @@ void knns_server::complete(Slot& sl, int status, const char* err)
         for (size_t i = 0; i < sl.batch.size(); ++i) {
             Request& r = *sl.batch[i];
             if (status == KNNS_OK) {
+                // rows of the launch's k; the request keeps the first r.k of each
                 const int64_t o = sl.offs[i];
-                r.dist.assign(sl.h_dist + o * sl.k, sl.h_dist + (o + r.Q) * sl.k);
-                r.idx.assign(sl.h_idx + o * sl.k, sl.h_idx + (o + r.Q) * sl.k);
+                r.dist.resize((size_t)r.Q * r.k);
+                r.idx.resize((size_t)r.Q * r.k);
+                for (int64_t q = 0; q < r.Q; ++q) {
+                    memcpy(r.dist.data() + q * r.k, sl.h_dist + (o + q) * sl.k, (size_t)r.k * sizeof(float));
+                    memcpy(r.idx.data() + q * r.k, sl.h_idx + (o + q) * sl.k, (size_t)r.k * sizeof(int32_t));
+                }
             } else if (r.error.empty()) {
                 r.error = err ? err : "";
             }
@@ -352,13 +362,17 @@ void knns_server::run()
             return;
         }
         Slot* fs = free_slot();
-        // admit, oldest first, the pending requests with the oldest request's k that fit one launch
-        const int k = pending.front()->k;
+        // admit, oldest first, the pending requests that fit one launch: any k in the exact
+        // form (the launch runs the largest), the oldest request's k in the precision forms
+        const bool mix_k = cfg.precision == KNNS_PREC_EXACT;
+        const int k0 = pending.front()->k;
+        int k = k0;
         std::vector<std::shared_ptr<Request>> take;
         int64_t total = 0;
         for (auto it = pending.begin(); it != pending.end();) {
-            if ((*it)->k == k && total + (*it)->Q <= cfg.max_batch) {
+            if ((mix_k || (*it)->k == k0) && total + (*it)->Q <= cfg.max_batch) {
                 total += (*it)->Q;
+                k = std::max(k, (*it)->k);
                 take.push_back(*it);
                 it = pending.erase(it);
             } else {

@@ -84,32 +84,6 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* m, uin
         : "memory");
 }
 
-// Multicast variant: the box lands at the same shared-memory offset in every CTA
-// of the cluster named in cta_mask, each completing its own mbarrier at `bar`'s offset.
-__device__ __forceinline__ void tma_load_2d_mc(void* dst, const CUtensorMap* m, uint64_t* bar, int x, int y,
-                                               uint16_t cta_mask)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
-        " [%0], [%1, {%2, %3}], [%4], %5;"
-        ::"r"(smem_u32(dst)), "l"((uint64_t)m), "r"(x), "r"(y), "r"(smem_u32(bar)), "h"(cta_mask)
-        : "memory");
-}
-
-// ---------------------------------------------------------------- cluster
-__device__ __forceinline__ uint32_t cluster_ctarank()
-{
-    uint32_t r;
-    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-    return r;
-}
-
-// Every thread of every CTA of the cluster arrives and waits (release / acquire).
-__device__ __forceinline__ void cluster_sync()
-{
-    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-
 // ---------------------------------------------------------------- tcgen05
 __device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols)
 {
@@ -174,15 +148,6 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar)
 {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                  : "memory");
-}
-
-// As mma_commit, arriving on the mbarrier at `bar`'s offset in every CTA of cta_mask.
-__device__ __forceinline__ void mma_commit_mc(uint64_t* bar, uint16_t cta_mask)
-{
-    asm volatile(
-        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
-        ::"r"(smem_u32(bar)), "h"(cta_mask)
-        : "memory");
 }
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }

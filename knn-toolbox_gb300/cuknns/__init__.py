@@ -33,10 +33,11 @@ SCAN_AUTO, SCAN_ON, SCAN_OFF = 0, 1, 2
 OK, ERR_INVALID, ERR_CUDA, ERR_UNSUPPORTED, ERR_DEVICE_TIMEOUT, ERR_NOMEM = range(6)
 
 # Every symbol include/knn_gb300.h and include/cuknns.h declare.
-EXPORTED = ["knns_default_options", "knns_search_device", "knns_search_host", "knns_check_device",
+EXPORTED = ["knns_default_options", "knns_search_device", "knns_search_host", "knns_check_device", "knns_merge_topk",
             "knns_last_error", "knns_last_stats", "knns_last_fixups", "knns_version", "knns_debug_tc_dot_tile",
+            "knns_debug_stall_next_search",
             "knns_debug_prep",
-            "knns_timing_collect", "knns_timing_collect5", "knns_search_device_noalloc",
+            "knns_timing_collect", "knns_timing_collect5", "knns_search_device_noalloc", "knns_noalloc_prepare",
             "knns_index_create", "knns_index_search", "knns_index_destroy", "knns_autotune_shortlist",
             "knns_server_default_config", "knns_server_create", "knns_server_submit", "knns_server_wait",
             "knns_server_stats", "knns_server_destroy", "knns_server_warmup",
@@ -53,7 +54,8 @@ class Options(ctypes.Structure):
     _fields_ = [("algo", ctypes.c_int), ("splits", ctypes.c_int), ("rerank", ctypes.c_int),
                 ("kp", ctypes.c_int), ("timing", ctypes.c_int), ("pilot", ctypes.c_int),
                 ("precision", ctypes.c_int), ("shortlist", ctypes.c_int), ("scan", ctypes.c_int),
-                ("scan_boxes", ctypes.c_int), ("block_rows", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+                ("scan_boxes", ctypes.c_int), ("block_rows", ctypes.c_int), ("tf32_only", ctypes.c_int),
+                ("reserved", ctypes.c_int * 2)]
 
 
 class Stats(ctypes.Structure):
@@ -100,14 +102,17 @@ def lib():
     L.knns_search_device.argtypes = [vp, i64, i64, vp, i64, i64, ci, ci, vp, vp, ctypes.POINTER(Options), vp]
     L.knns_search_host.argtypes = [vp, i64, vp, i64, ci, ci, vp, vp, ctypes.POINTER(Options)]
     L.knns_check_device.argtypes = [vp]
+    L.knns_merge_topk.argtypes = [vp, vp, ci, vp, vp, ci, ctypes.c_int32, i64, ci, vp, vp, vp]
     L.knns_last_error.restype = ctypes.c_char_p
     L.knns_last_stats.argtypes = [ctypes.POINTER(Stats)]
     L.knns_last_fixups.argtypes = [ctypes.POINTER(ctypes.c_int64)]
     L.knns_debug_tc_dot_tile.argtypes = [vp, i64, vp, i64, ci, vp]
+    L.knns_debug_stall_next_search.argtypes = [i64]
     L.knns_debug_prep.argtypes = [vp, i64, i64, ci, vp, vp, vp, vp, vp]
     L.knns_timing_collect.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
     L.knns_timing_collect5.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
     L.knns_search_device_noalloc.argtypes = [vp, i64, i64, vp, i64, i64, ci, ci, vp, vp, vp]
+    L.knns_noalloc_prepare.argtypes = []
     L.knns_index_create.argtypes = [vp, i64, i64, ci, ci, ctypes.POINTER(vp), vp]
     L.knns_index_search.argtypes = [vp, vp, i64, i64, ci, vp, vp, ctypes.POINTER(Options), vp]
     L.knns_autotune_shortlist.argtypes = [vp, vp, i64, i64, ci, ci, ctypes.c_double, ctypes.POINTER(ctypes.c_int),
@@ -146,7 +151,7 @@ def _check(rc):
 
 
 def options(algo=ALGO_AUTO, splits=0, rerank=True, kp=0, timing=False, pilot=True, precision=PREC_EXACT,
-            shortlist=0, scan=SCAN_AUTO, scan_boxes=0, block_rows=0) -> Options:
+            shortlist=0, scan=SCAN_AUTO, scan_boxes=0, block_rows=0, tf32_only=False) -> Options:
     o = Options()
     lib().knns_default_options(ctypes.byref(o))
     o.algo, o.splits, o.rerank, o.kp = int(algo), int(splits), int(bool(rerank)), int(kp)
@@ -155,6 +160,7 @@ def options(algo=ALGO_AUTO, splits=0, rerank=True, kp=0, timing=False, pilot=Tru
     o.precision, o.shortlist = int(precision), int(shortlist)
     o.scan, o.scan_boxes = int(scan), int(scan_boxes)
     o.block_rows = int(block_rows)
+    o.tf32_only = int(bool(tf32_only))
     return o
 
 
@@ -195,7 +201,7 @@ def last_stats() -> dict:
 
 def search(corpus, queries, k, *, dist=None, idx=None, algo=ALGO_AUTO, splits=0, rerank=True, kp=0,
            stream=None, check=True, timing=False, pilot=True, precision=PREC_EXACT, shortlist=0, scan=SCAN_AUTO,
-           scan_boxes=0):
+           scan_boxes=0, tf32_only=False):
     """kNN on CUDA tensors (float32, rows contiguous).  Returns (dist[Q,k] f32, idx[Q,k] i32)."""
     import torch
     assert corpus.is_cuda and queries.is_cuda, "search() takes device tensors"
@@ -209,7 +215,8 @@ def search(corpus, queries, k, *, dist=None, idx=None, algo=ALGO_AUTO, splits=0,
     if idx is None:
         idx = torch.empty((Q, k), dtype=torch.int32, device=corpus.device)
     s = torch.cuda.current_stream(corpus.device) if stream is None else stream
-    o = options(algo, splits, rerank, kp, timing, pilot, precision, shortlist, scan, scan_boxes)
+    o = options(algo, splits, rerank, kp, timing, pilot, precision, shortlist, scan, scan_boxes,
+                tf32_only=tf32_only)
     rc = lib().knns_search_device(corpus.data_ptr(), N, corpus.stride(0), queries.data_ptr(), Q,
                                   queries.stride(0), D, k, dist.data_ptr(), idx.data_ptr(), ctypes.byref(o),
                                   ctypes.c_void_p(s.cuda_stream))
@@ -217,6 +224,27 @@ def search(corpus, queries, k, *, dist=None, idx=None, algo=ALGO_AUTO, splits=0,
     if check:
         _check(lib().knns_check_device(ctypes.c_void_p(s.cuda_stream)))
     return dist, idx
+
+
+def merge_topk(run_d, run_i, have, blk_d, blk_i, kb, k, offset=0, stream=None):
+    """Merge two per-query result lists on the device by (distance, index) (knns_merge_topk).
+
+    run_d / run_i: Q x k (first `have` columns used); blk_d / blk_i: Q x kb, indices shifted by
+    `offset`.  Returns new (dist Q x k, idx Q x k) CUDA tensors holding min(k, have + kb) entries.
+    """
+    import torch
+    Q = run_d.shape[0] if have > 0 else blk_d.shape[0]
+    dev = (run_d if have > 0 else blk_d).device
+    out_d = torch.full((Q, k), float("inf"), dtype=torch.float32, device=dev)
+    out_i = torch.full((Q, k), -1, dtype=torch.int32, device=dev)
+    for t, cols in ((run_d, k), (run_i, k), (blk_d, kb), (blk_i, kb)):
+        assert t is None or (t.is_cuda and t.is_contiguous() and t.shape == (Q, cols)), "merge_topk operands"
+    s = torch.cuda.current_stream(dev) if stream is None else stream
+    ptr = (lambda t: t.data_ptr() if t is not None else None)
+    _check(lib().knns_merge_topk(ptr(run_d) if have else None, ptr(run_i) if have else None, have,
+                                 ptr(blk_d) if kb else None, ptr(blk_i) if kb else None, kb, int(offset), Q, k,
+                                 out_d.data_ptr(), out_i.data_ptr(), ctypes.c_void_p(s.cuda_stream)))
+    return out_d, out_i
 
 
 def search_host(corpus, queries, k, *, algo=ALGO_AUTO, splits=0, rerank=True, kp=0, **opts):

@@ -43,3 +43,54 @@ def test_block_rows_validation(engine):
     d1, i1 = engine.search_host(X, Qs, 40, block_rows=10)
     np.testing.assert_array_equal(i1, i0)
     np.testing.assert_array_equal(d1, d0)
+
+
+@pytest.mark.parametrize("kind,N,D,k,prec", [("int", 400_003, 128, 100, "exact"), ("int", 150_000, 64, 16, "bf16"),
+                                             ("aniso", 300_001, 256, 32, "fp8"), ("uniform", 200_000, 96, 10, "bf16"),
+                                             ("uniform", 180_000, 32, 20, "exact")])
+def test_host_search_overlapping_copy_equals_resident(engine, kind, N, D, k, prec):
+    # Host-buffer searches on the threshold-scan path copy the corpus in blocks (the seeding
+    # sample first) and prepare and scan each block as it lands; the answers must be those of
+    # the same search on the resident corpus, bit for bit -- including FP32 data in the exact
+    # form, where the scan stands down and the TF32 path runs after the last block.
+    import torch
+    import cuknns.synth as S
+    if kind == "aniso":
+        X, Qs = S.anisotropic(N, D, seed=N, nq=300)
+    else:
+        X, Qs = data(kind, N, 300, D, N + D)
+    p = {"exact": engine.PREC_EXACT, "bf16": engine.PREC_BF16, "fp8": engine.PREC_FP8}[prec]
+    hx = torch.from_numpy(X).pin_memory().numpy()
+    hq = torch.from_numpy(Qs).pin_memory().numpy()
+    for _ in range(2):  # the second call reuses the engine's buffers and streams
+        d1, i1 = engine.search_host(hx, hq, k, precision=p, shortlist=2 if prec != "exact" else 0)
+    st = engine.last_stats()
+    d0, i0 = engine.search(torch.from_numpy(X).cuda(), torch.from_numpy(Qs).cuda(), k, precision=p,
+                           shortlist=2 if prec != "exact" else 0)
+    assert st["scan"] == 1
+    np.testing.assert_array_equal(i1, i0.cpu().numpy())
+    np.testing.assert_array_equal(d1, d0.cpu().numpy())
+
+
+@pytest.mark.parametrize("kind,N,shards,k", [("int", 300_000, 4, 100), ("uniform", 70_000, 3, 16),
+                                             ("int", 250, 3, 100)])
+def test_corpus_shards_merged_on_device_equal_whole(engine, kind, N, shards, k):
+    # The multi-GPU corpus split, its ranks run one after another on this GPU: each shard is
+    # searched, its indices made global, and the per-shard lists merged in rank order by the
+    # device merge (knns_merge_topk) -- the answer of one search over the whole corpus.
+    import torch
+    from cuknns import shard as S
+    X, Qs = data(kind, N, 200, 64, N + k)
+    c, q = torch.from_numpy(X).cuda(), torch.from_numpy(Qs).cuda()
+    ds, idxs, counts = [], [], []
+    for r in range(shards):
+        r0, r1 = S.shard_bounds(N, shards, r)
+        d, i = S.sharded_search(c[r0:r1], r0, q, k)  # no process group: this rank's padded list
+        ds.append(d)
+        idxs.append(i)
+        counts.append(min(k, r1 - r0))
+    d1, i1 = S.merge_rank_lists(ds, idxs, counts, k, lambda rd, ri, h, bd, bi, kb, kk:
+                                engine.merge_topk(rd, ri, h, bd, bi, kb, kk))
+    d0, i0 = engine.search(c, q, k)
+    np.testing.assert_array_equal(i1.cpu().numpy(), i0.cpu().numpy())
+    np.testing.assert_array_equal(d1.cpu().numpy(), d0.cpu().numpy())

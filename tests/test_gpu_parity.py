@@ -316,3 +316,21 @@ def test_bf16_shortlist_on_bf16_exact_data_is_exact(engine, oracle):
     od, oi = oracle.knn_gemm(X, Qs, k, kp=st["kp"], rerank=True)
     np.testing.assert_array_equal(i, oi)
     np.testing.assert_array_equal(d, od)
+
+
+# ---------------------------------------------------------------- 3xTF32 keys on request
+@pytest.mark.parametrize("N", [20000, 150000])
+def test_tf32_only_gives_the_same_answers(engine, oracle, N):
+    # integer data are exact in BF16: by default the BF16 kernels (the threshold scan at
+    # N >= 131072) rank them; tf32_only sends them through the 3xTF32 kernel instead,
+    # whose keys are exact on this data as well -- same answers, bit for bit
+    import cuknns.synth as S
+    X, Qs = S.int_descriptor(N, 128, seed=12, nq=257)
+    k = 100
+    d0, i0, st0 = run(engine, X, Qs, k)
+    d1, i1, st1 = run(engine, X, Qs, k, tf32_only=True)
+    np.testing.assert_array_equal(i0, i1)
+    np.testing.assert_array_equal(d0, d1)
+    od, oi = oracle.knn_gemm(X, Qs, k, kp=st1["kp"], rerank=True)
+    np.testing.assert_array_equal(i1, oi)
+    np.testing.assert_array_equal(d1, od)

@@ -194,3 +194,53 @@ def test_scan_answers_nearly_every_query(engine, form):
     fix = engine.last_fixups()
     assert fix <= Q // 100, (form, fix)
     assert (np.diff(d, axis=1) >= 0).all()
+
+
+# ---------------------------------------------------------------- shortlists above 128 (precision forms)
+@pytest.mark.parametrize("form,D,k,c", [("bf16", 128, 100, 2), ("bf16", 96, 100, 4), ("fp8", 256, 64, 4),
+                                        ("bf16", 64, 500, 1)])
+def test_precision_forms_long_shortlists(engine, oracle, form, D, k, c):
+    # c*k above 128 (up to 512): the shortlist lives only in the scan's candidate segments;
+    # recall against FP64 and exact distances as for the short lists
+    import cuknns.synth as S
+    if form == "fp8":
+        X, Qs = S.anisotropic(150_000, D, seed=D + k, nq=200)
+        p = engine.PREC_FP8
+    else:
+        X, Qs = S.gauss_mixture(150_000, D, seed=D + k, nq=200, centres=512)
+        p = engine.PREC_BF16
+    kp = (max(32, c * k) + 15) // 16 * 16 if c > 1 else 512
+    d, i, st = run(engine, X, Qs, k, precision=p, shortlist=c, kp=kp if c == 1 else 0)
+    assert st["scan"] == 1 and st["kp"] == kp and st["kp"] > 128
+    ex = oracle.knn_f64(X, Qs, k)
+    assert oracle.recall_at_k(i, ex[1]) >= 0.99
+    got64 = oracle.pair_dist_f64(X, Qs, i)
+    assert (np.abs(d - got64) <= DIST_REL * got64 + 1e-6).all()
+    assert (np.diff(d, axis=1) >= 0).all()
+    assert engine.last_fixups() <= 2
+
+
+@pytest.mark.parametrize("Q", [20, 100])
+def test_long_shortlist_fixup_on_cuda_cores(engine, oracle, Q):
+    # Duplicated rows overflow every segment, so every query fails the scan; with a shortlist
+    # above 128 the fix-up is the CUDA-core kernel with exact keys, compacted to the failed
+    # queries (100 > 32 also runs its second launch).  Integer data: bit-exact.
+    rng = np.random.default_rng(9)
+    base = rng.integers(0, 64, (10, 64)).astype(np.float32)
+    X = np.repeat(base, 3000, axis=0)
+    rng.shuffle(X)
+    Qs = base[rng.integers(0, 10, Q)]
+    k = 100
+    d, i, st = run(engine, X, Qs, k, precision=engine.PREC_BF16, shortlist=2)
+    assert st["scan"] == 1 and st["kp"] == 208
+    assert engine.last_fixups() == Q
+    od, oi = oracle.knn_gemm(X, Qs, k, kp=st["kp"], rerank=True)
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_array_equal(d, od)
+
+
+def test_long_shortlist_needs_the_scan(engine):
+    X, Qs = ints(5000, 10, 32, 3)
+    with pytest.raises(engine.KnnsError) as e:
+        run(engine, X, Qs, 100, precision=engine.PREC_BF16, shortlist=2)
+    assert e.value.code == engine.ERR_UNSUPPORTED

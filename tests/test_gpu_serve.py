@@ -65,13 +65,20 @@ def _requests(rng, n, D, hi=256):
     return out
 
 
-@pytest.mark.parametrize("slots,autotune", [(2, False), (1, True)])
-def test_server_results_equal_alone(engine, slots, autotune):
-    X, _ = ints(200_000, 1, 64, 11)
+@pytest.mark.parametrize("slots,autotune,kind", [(2, False, "int"), (1, True, "int"), (2, False, "uniform")])
+def test_server_results_equal_alone(engine, slots, autotune, kind):
+    # requests of k 1, 10 and 100 share launches (the launch runs the largest k, each request
+    # keeps the first k of its rows): every answer must still be the one the request gets alone
+    if kind == "int":
+        X, _ = ints(200_000, 1, 64, 11)
+    else:
+        X = np.random.default_rng(11).random((200_000, 64), dtype=np.float32)
     c = cuda(X)
     ix = engine.Index(c)
     rng = np.random.default_rng(12)
     reqs = _requests(rng, 60, 64)
+    if kind == "uniform":
+        reqs = [(rng.random(q.shape, dtype=np.float32), k) for q, k in reqs]
     srv = engine.Server(ix, slots=slots, max_batch=512, autotune=autotune)
     results = {}
     lock = threading.Lock()

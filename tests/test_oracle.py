@@ -146,9 +146,30 @@ def test_merge_restatement_pinned_to_reference_code(oracle, which):
 
 
 def test_reference_recipe_is_inert_without_the_sources(monkeypatch, tmp_path):
-    # where the reference is not mounted (the GPU host) the recipe builds nothing and
+    # with neither a mounted reference nor a staged copy the recipe builds nothing and
     # reports it, so build() never depends on the reference
     import build_ref
-    monkeypatch.setattr(build_ref, "REF", str(tmp_path / "absent"))
+    monkeypatch.setenv("KNN_REFERENCE_DIR", str(tmp_path / "absent"))
+    monkeypatch.setattr(build_ref, "MOUNT", str(tmp_path / "absent"))
+    monkeypatch.setattr(build_ref, "STAGED", str(tmp_path / "staged"))
     assert not build_ref.available()
+    assert build_ref.stage() is False
     assert build_ref.build_if_available() is False
+
+
+def test_reference_recipe_stages_unmodified_sources(monkeypatch, tmp_path):
+    # a reference tree named by KNN_REFERENCE_DIR is staged file for file, byte for byte
+    import build_ref
+    ref = tmp_path / "ref"
+    for f in build_ref.FILES:
+        (ref / f).parent.mkdir(parents=True, exist_ok=True)
+        (ref / f).write_bytes(("// " + f + "\n").encode())
+    monkeypatch.setenv("KNN_REFERENCE_DIR", str(ref))
+    monkeypatch.setattr(build_ref, "MOUNT", str(tmp_path / "absent"))
+    monkeypatch.setattr(build_ref, "STAGED", str(tmp_path / "staged"))
+    assert build_ref.mounted_dir() == str(ref)
+    assert build_ref.stage() is True
+    for f in build_ref.FILES:
+        assert (tmp_path / "staged" / f).read_bytes() == (ref / f).read_bytes()
+    monkeypatch.delenv("KNN_REFERENCE_DIR")
+    assert build_ref.source_dir() == str(tmp_path / "staged")

@@ -34,9 +34,13 @@ def _noalloc(engine, c, q, k, stream):
 def test_noalloc_matches_search_device_two_calls(engine, oracle):
     import torch
     stream = torch.cuda.current_stream()
+    # the set-up a caller makes at start-up, before handing the HBM to its own allocator
+    assert engine.lib().knns_noalloc_prepare() == engine.OK, engine.last_error()
     rng = np.random.default_rng(2027)
-    shapes = [(20000, 300, 96, 16), (9000, 150, 43, 100)]
-    for N, Q, D, k in shapes:  # two calls in a row, different sizes: stale scratch must not leak
+    # calls in a row, different sizes: stale scratch must not leak; k = 500 is served as by
+    # the regular entry point (shortlist without the re-rank margin)
+    shapes = [(20000, 300, 96, 16), (9000, 150, 43, 100), (6000, 40, 32, 500)]
+    for N, Q, D, k in shapes:
         X = rng.random((N, D), dtype=np.float32)
         Qs = rng.random((Q, D), dtype=np.float32)
         c = torch.from_numpy(X).cuda()
