@@ -379,7 +379,7 @@ def run_gb300(args, w):
                 # this rank's shard, then the all-gather of every rank's Q x k list and the merge
                 d_, i_ = SH.sharded_search(c, r0, q, k, stream=stream, check=False, timing=timing, precision=p,
                                            shortlist=shortlist, scan=scan_mode, scan_boxes=args.scan_boxes,
-                                           tf32_only=tf32_only)
+                                           tf32_only=tf32_only, scan_accs=args.scan_accs)
                 dist_out.copy_(d_)
                 idx_out.copy_(i_)
             return step
@@ -387,7 +387,7 @@ def run_gb300(args, w):
         def step(timing):
             cuknns.search(c, q, k, dist=dist_out, idx=idx_out, stream=stream, check=False, timing=timing,
                           precision=p, shortlist=shortlist, scan=scan_mode, scan_boxes=args.scan_boxes,
-                          tf32_only=tf32_only)
+                          tf32_only=tf32_only, scan_accs=args.scan_accs)
         return step
 
     # ---- headline: the requested form, inputs resident in HBM
@@ -474,12 +474,12 @@ def run_gb300(args, w):
                 peak, peak_src = live, "cuBLASLt FP8 E4M3 8192^3 GEMM burst, measured in this run"
             else:
                 peak, peak_src = 2.0 * peaks["bf16_tflops"], f"2 x {peak_kind} bf16 dense burst"
-            mma = f"e4m3 (kind::f8f6f4, M128 N{224 if row_bytes <= 256 else 192})"
+            mma = f"e4m3 (kind::f8f6f4, M128 N{96 if args.scan_accs == 4 else (224 if row_bytes <= 256 else 192)})"
             padded_k = row_bytes
         else:
             padded_k = -(-D // 64) * 64
             peak, peak_src = peaks["bf16_tflops"], f"{peak_kind} bf16 dense burst"
-            mma = f"bf16 (kind::f16, M128 N{224 if padded_k <= 128 else 192})"
+            mma = f"bf16 (kind::f16, M128 N{96 if args.scan_accs == 4 else (224 if padded_k <= 128 else 192)})"
         roof = {"bound": "tensor", "achieved": flops / (fused_avg_ms / 1e3) / 1e12, "peak": peak,
                 "unit": "TFLOP/s", "peak_source": peak_src, "mma_kind": mma, "products_per_useful_product": 1.0,
                 "flops_per_launch": flops, "padded_k": int(padded_k)}
@@ -646,6 +646,8 @@ def main():
     ap.add_argument("--scan", default="auto", choices=["auto", "on", "off"],
                     help="threshold-scan path for BF16 keys (auto: corpora of 131,072 rows and more)")
     ap.add_argument("--scan-boxes", type=int, default=0, help="threshold scan: K boxes per ring slot (0 = auto)")
+    ap.add_argument("--scan-accs", type=int, default=0, choices=[0, 2, 4],
+                    help="threshold scan: tensor-memory accumulators (0 = auto)")
     ap.add_argument("--rate", type=float, default=4000.0, help="serving: offered requests per second")
     ap.add_argument("--requests", type=int, default=4000, help="serving: requests in the timed run")
     ap.add_argument("--recall-queries", type=int, default=0,

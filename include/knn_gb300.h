@@ -33,7 +33,9 @@ extern "C" {
 
 /* kernel families */
 #define KNNS_ALGO_AUTO 0 /* tensor cores when the shape allows, else CUDA cores */
-#define KNNS_ALGO_TC 1   /* tcgen05 3xTF32 fused distance + shortlist (D <= 128, shortlist <= 128) */
+#define KNNS_ALGO_TC 1   /* tcgen05 tensor cores: BF16 keys for data exact in BF16, else 3xTF32; D <= 128
+                            with shortlists <= 128 on any corpus, any D (to 4096) and shortlists up to 512
+                            on corpora of at least 16384 rows (the 3xTF32 threshold scan) */
 #define KNNS_ALGO_SIMT 2 /* CUDA-core FP32 fused distance + shortlist (any D, shortlist <= 512) */
 
 /* precision of the ranking keys */
@@ -73,7 +75,9 @@ typedef struct knns_options {
     int tf32_only;   /* exact form: 1 = 3xTF32 keys even for data that are exact in BF16 (the BF16
                         tensor-core shortcut and the threshold scan stand down); results are the same,
                         the kernels slower -- a measurement switch for comparing the two key types */
-    int reserved[2];
+    int scan_accs;   /* threshold scan: tensor-memory accumulators, 2 (tiles of 224 corpus rows; 192
+                        above 128 BF16 columns) or 4 (tiles of 96); 0 = automatic */
+    int reserved[1];
 } knns_options;
 
 typedef struct knns_stats {

@@ -174,6 +174,10 @@ static int encode_rows_bf16(CUtensorMap* m, const void* base, int64_t rows, int6
 // ---------------------------------------------------------------- planning
 // smallest corpus the threshold scan runs on when asked to (KNNS_SCAN_ON, long shortlists)
 constexpr int64_t kScanMinRowsForced = 16384;
+// accumulators of the threshold scan when the options leave it open
+constexpr int kScanAccsAuto = 2;
+// widest rows the 3xTF32 scan takes (its K loop has no limit; the TF32 copies cost 8 bytes a value)
+constexpr int kTscanMaxDp = 4096;
 static inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 static inline int round32(int x) { return (x + 31) & ~31; }
 static inline int round16(int x) { return (x + 15) & ~15; }
@@ -252,6 +256,22 @@ int resolve_config(const Engine& E, int64_t N, int64_t Q, int D, int k, const kn
     int algo = o.algo;
     const int dp = (int)round32(D);
     const bool tc_ok = E.cc >= 100 && dp <= kMaxDpTC;
+    // Rows wider than 128 or k above 128 (shapes of the shortlist kernel's limits) go to the
+    // 3xTF32 threshold scan on corpora large enough to seed its thresholds
+    const bool wide = dp > kMaxDpTC || round16(k) > kMaxKpTC;
+    const bool tscan_ok = E.cc >= 100 && o.scan != KNNS_SCAN_OFF && N >= kScanMinRowsForced && dp <= kTscanMaxDp &&
+                          c->kp <= kMaxKpScan && wide;
+    if ((algo == KNNS_ALGO_AUTO || algo == KNNS_ALGO_TC) && tscan_ok) {
+        c->algo = KNNS_ALGO_TC;
+        c->tscan = true;
+        c->dp = dp;
+        c->dpb = (D + 63) & ~63;
+        c->qtile = kTileQ;
+        c->stages = 0;
+        c->splits = 0;  // planned by the scan
+        c->split_len = 0;
+        return KNNS_OK;
+    }
     if (algo == KNNS_ALGO_AUTO) {
         if (tc_ok && c->kp > kMaxKpTC && round16(k) <= kMaxKpTC && o.kp <= 0) c->kp = std::max(round16(k), 32);
         algo = (tc_ok && c->kp <= kMaxKpTC) ? KNNS_ALGO_TC : KNNS_ALGO_SIMT;
@@ -325,7 +345,7 @@ struct ScanLevel {
 };
 
 struct ScanPlan {
-    int bps = 0, ring = 0;
+    int bps = 0, ring = 0, accs = 2;
     int64_t stride0 = 0;  // finest seeding stride
     int levels = 0;
     ScanLevel lv[kMaxSeedLevels];
@@ -366,15 +386,27 @@ static int seg_cap(double per_seg, double sigmas)
 
 static int seed_rank(double m) { return (int)std::ceil(2.0 * m + 4.0 * std::sqrt(m)) + 1; }
 
+// tf32: the plan of the 3xTF32 scan (tiles of 128 rows, 32 columns per segment; fix-up on the
+// CUDA-core kernel); otherwise of the BF16 / E4M3 scan of row width dpb.
 static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, const knns_options& o, ScanPlan* P,
-                     bool fp8)
+                     bool fp8, bool tf32 = false)
 {
-    if (scan_plan(dpb, o.scan_boxes, &P->bps, &P->ring, fp8) != 0)
-        return set_error(KNNS_ERR_UNSUPPORTED, "threshold scan: no ring geometry for %d BF16 columns with %d boxes per slot",
-                         dpb, o.scan_boxes);
+    if (o.scan_accs != 0 && o.scan_accs != 2 && o.scan_accs != 4)
+        return set_error(KNNS_ERR_INVALID, "threshold scan: %d accumulators (2 or 4)", o.scan_accs);
+    int tn = 128, pc = 32;
+    if (tf32) {
+        P->accs = 4;
+        P->ring = tscan_ring();
+    } else {
+        P->accs = o.scan_accs ? o.scan_accs : kScanAccsAuto;
+        if (scan_plan(dpb, o.scan_boxes, &P->bps, &P->ring, fp8, P->accs) != 0)
+            return set_error(KNNS_ERR_UNSUPPORTED,
+                             "threshold scan: no ring geometry for %d BF16 columns with %d boxes per slot", dpb,
+                             o.scan_boxes);
+        tn = scan_tile_rows(dpb, P->accs);
+        pc = scan_part_cols(dpb, P->accs);  // segment columns per tile
+    }
     const int64_t qt = cdiv(Q, kTileQ);  // query tiles
-    const int tn = scan_tile_rows(dpb);
-    const int pc = scan_part_cols(dpb);  // segment columns per tile (the parts are not all equal)
     // levels, finest first: strides s, 16 s, ... until the sample fits the selector whole
     P->stride0 = seed_stride(kp);
     int64_t st[kMaxSeedLevels];
@@ -443,7 +475,7 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
     // fix-up of failed queries: up to 512 on a full wave, the rest (rare) on 8 splits; shortlists
     // above the tensor-core kernel's kMaxKpTC go to the CUDA-core kernel in tiles of 32 queries
     // (exact FP32 keys): the first 32 failed queries on a wave of splits, the rest on 8
-    P->simt_fix = kp > kMaxKpTC;
+    P->simt_fix = kp > kMaxKpTC || tf32;
     const int ft = P->simt_fix ? kSimtTileN : kTileN;
     const int fq = P->simt_fix ? 32 : kTileQ;
     const int64_t tilesF = cdiv(N, ft);
@@ -456,6 +488,174 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
     P->fixB_len = cdiv(tilesF, P->fixB_S) * ft;
     P->fixB_S = (int)cdiv(N, P->fixB_len);
     P->part_words = std::max((size_t)P->fixA_S * P->fixA_rows * kp, (size_t)P->fixB_S * P->fixB_rows * kp);
+    return KNNS_OK;
+}
+
+// ---------------------------------------------------------------- 3xTF32 threshold scan
+// The exact form for rows wider than 128 or k above 128: corpus and query norms and TF32
+// hi / lo copies, threshold seeding over nested corpus samples, the main scan, the selection
+// with the exact re-rank, and the CUDA-core fix-up of the queries the scan could not answer.
+static int run_tscan(Engine& E, const Config& c, const float* corpus, int64_t N, int64_t ldc, const float* queries,
+                     int64_t Q, int64_t ldq, int D, int k, float* dist, int32_t* idx, float* idx_f,
+                     const knns_options& o, cudaStream_t s, knns_stats* st, const PreparedCorpus* pc, bool capture)
+{
+    ScanPlan sp;
+    int rc = plan_scan(E, N, Q, c.dpb, c.kp, o, &sp, false, true);
+    if (rc) return rc;
+    const int dp = c.dp;
+    if (pc && (!pc->tf32 || pc->dp != dp))
+        return set_error(KNNS_ERR_INVALID, "the exact form needs an index prepared with TF32 copies of this width");
+    const int64_t n_pad = cdiv(N, kScanTileN) * kScanTileN + kScanTileN;
+    if (!pc) {
+        rc = E.cn.ensure(n_pad * sizeof(float));
+        if (!rc) rc = E.hi.ensure((size_t)N * dp * sizeof(float));
+        if (!rc) rc = E.lo.ensure((size_t)N * dp * sizeof(float));
+        if (!rc) rc = E.loflags.ensure(((size_t)cdiv(N, 128) + 4) * sizeof(uint32_t));
+        if (rc) return rc;
+    }
+    rc = E.qn.ensure(Q * sizeof(float));
+    if (!rc) rc = E.qhi.ensure((size_t)Q * dp * sizeof(float));
+    if (!rc) rc = E.qlo.ensure((size_t)Q * dp * sizeof(float));
+    if (!rc) rc = E.qlof.ensure(((size_t)cdiv(Q, 128) + 4) * sizeof(uint32_t));
+    if (!rc) rc = E.words.ensure(8 * sizeof(uint32_t));
+    if (!rc) rc = E.tq.ensure((size_t)2 * Q * sizeof(float));
+    if (!rc) rc = E.cand.ensure(sp.cand_words * sizeof(uint64_t));
+    if (!rc) rc = E.cnt.ensure(sp.cnt_words * sizeof(uint32_t));
+    if (!rc) rc = E.cnv.ensure(sp.norm_words * sizeof(float));
+    if (!rc) rc = E.fail.ensure((size_t)(Q + 1) * sizeof(uint32_t));
+    if (!rc) rc = E.part.ensure(sp.part_words * sizeof(uint64_t));
+    if (!rc) rc = E.thr2.ensure(Q * sizeof(uint32_t));
+    if (rc) return rc;
+    const size_t ws = (pc ? 0 : E.cn.cap + E.hi.cap + E.lo.cap + E.loflags.cap) + E.qn.cap + E.qhi.cap + E.qlo.cap +
+                      E.tq.cap + E.cand.cap + E.cnt.cap + E.cnv.cap + E.fail.cap + E.part.cap + E.thr2.cap;
+    float* cn = (float*)(pc ? pc->cn.p : E.cn.p);
+    const float* hi = (const float*)(pc ? pc->hi.p : E.hi.p);
+    const float* lo = (const float*)(pc ? pc->lo.p : E.lo.p);
+    uint32_t* cflags = (uint32_t*)(pc ? pc->tiles.p : E.loflags.p);
+    float* qn = (float*)E.qn.p;
+    uint32_t* words = (uint32_t*)E.words.p;
+
+    if (!capture) KNN_CUDA(cudaStreamWaitEvent(s, E.last_done, 0));
+    cudaEvent_t tv[Engine::kTimingEvents] = {};
+    if (o.timing && E.timing_slot(tv) != KNNS_OK) return KNNS_ERR_CUDA;
+    auto mark = [&](int i) -> int {
+        if (tv[i]) KNN_CUDA(cudaEventRecord(tv[i], s));
+        return KNNS_OK;
+    };
+    if ((rc = mark(0))) return rc;
+    int launches = 0;
+    KNN_CUDA(cudaMemsetAsync(words, 0, 4 * sizeof(uint32_t), s));
+    if (!pc) {
+        KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, 0, nullptr, cn, n_pad, nullptr, s));
+        KNN_CUDA(launch_split(corpus, N, ldc, D, dp, (float*)E.hi.p, (float*)E.lo.p, cflags, words, nullptr, s));
+        launches += 2;
+    }
+    KNN_CUDA(launch_prep_rows(queries, Q, ldq, D, 0, nullptr, qn, Q, nullptr, s));
+    KNN_CUDA(launch_split(queries, Q, ldq, D, dp, (float*)E.qhi.p, (float*)E.qlo.p, (uint32_t*)E.qlof.p, words + 1,
+                          nullptr, s));
+    launches += 2;
+    if ((rc = mark(1))) return rc;
+
+    TscanArgs a;
+    memset(&a, 0, sizeof(a));
+    if ((rc = encode_rows(&a.tm_qhi, (const float*)E.qhi.p, Q, dp, dp))) return rc;
+    if ((rc = encode_rows(&a.tm_qlo, (const float*)E.qlo.p, Q, dp, dp))) return rc;
+    a.qlo_flags = (const uint32_t*)E.qlof.p;
+    a.cand = (uint64_t*)E.cand.p;
+    a.cnt = (uint32_t*)E.cnt.p;
+    a.err = (int*)E.err.p;
+    a.Q = Q;
+    a.dp = dp;
+    a.ring = sp.ring;
+    // one scan over rows 0, stride, 2*stride, ... of the corpus (nview of them)
+    auto tscan_pass = [&](int64_t nview, int64_t stride, const float* cn_view, const float* thr, int splits,
+                          int64_t split_len, int cap, const uint32_t* flags) -> int {
+        int r = encode_rows(&a.tm_chi, hi, nview, dp, stride * dp);
+        if (!r) r = encode_rows(&a.tm_clo, lo, nview, dp, stride * dp);
+        if (r) return r;
+        a.cn = cn_view;
+        a.thr = thr;
+        a.N = nview;
+        a.split_len = split_len;
+        a.cap = cap;
+        a.clo_flags = flags;
+        KNN_CUDA(launch_tscan(a, splits, s));
+        ++launches;
+        return KNNS_OK;
+    };
+    float* Tbuf[2] = {(float*)E.tq.p, (float*)E.tq.p + Q};
+    uint32_t* fail_cnt = (uint32_t*)E.fail.p;
+    int32_t* fail_idx = (int32_t*)E.fail.p + 1;
+    CandSelect cs;
+    cs.cand = (const uint64_t*)E.cand.p;
+    cs.cnt = (const uint32_t*)E.cnt.p;
+    cs.Q = Q;
+    cs.D = D;
+    float* cnv = (float*)E.cnv.p;
+    const float* T = nullptr;
+    for (int l = 0; l < sp.levels; ++l) {
+        const ScanLevel& v = sp.lv[l];
+        KNN_CUDA(launch_gather_norms(cn, v.n, v.stride, cnv, v.n_pad, s));
+        if ((rc = tscan_pass(v.n, v.stride, cnv, T, v.S, v.len, v.cap, nullptr))) return rc;
+        cs.nseg = kScanParts * v.S;
+        cs.cap = v.cap;
+        cs.thr_out = Tbuf[l & 1];
+        cs.thr_rank = v.j;
+        cs.thr_fallback = T;
+        KNN_CUDA(launch_select_cand(cs, s));
+        launches += 2;
+        T = Tbuf[l & 1];
+        cnv += v.n_pad;
+    }
+    if ((rc = mark(2))) return rc;
+    if ((rc = tscan_pass(N, 1, cn, T, sp.S, sp.len, sp.cap, cflags))) return rc;
+    if ((rc = mark(3))) return rc;
+    KNN_CUDA(cudaMemsetAsync(fail_cnt, 0, sizeof(uint32_t), s));
+    cs.nseg = kScanParts * sp.S;
+    cs.cap = sp.cap;
+    cs.thr_out = nullptr;
+    cs.thr_fallback = nullptr;
+    cs.kp = c.kp;
+    cs.k = k;
+    cs.need = (int)std::min<int64_t>(c.kp, N);
+    cs.buf_words = sp.sel_words;
+    cs.rerank = c.rerank;
+    cs.corpus = corpus;
+    cs.ldc = ldc;
+    cs.queries = queries;
+    cs.ldq = ldq;
+    cs.qn = qn;
+    cs.out_dist = dist;
+    cs.out_idx = idx;
+    cs.out_idx_f = idx_f;
+    cs.fail_idx = fail_idx;
+    cs.fail_cnt = fail_cnt;
+    KNN_CUDA(launch_select_cand(cs, s));
+    ++launches;
+    if ((rc = mark(4))) return rc;
+    // fix-up: the queries the scan could not answer, on the CUDA-core kernel (exact FP32 keys),
+    // compacted; launches whose rows are all past the failure count return at once
+    auto fix_pass = [&](int64_t qbase, int64_t rows, int splits, int64_t split_len) -> int {
+        if (rows <= 0) return KNNS_OK;
+        uint32_t* thr2 = (uint32_t*)E.thr2.p;
+        KNN_CUDA(cudaMemsetAsync(thr2, 0xFF, rows * sizeof(uint32_t), s));
+        KNN_CUDA(launch_simt(corpus, N, ldc, cn, queries, rows, ldq, D, c.kp, 32, split_len, splits,
+                             (uint64_t*)E.part.p, thr2, s, nullptr, fail_idx, fail_cnt, qbase));
+        SelectExtra ex;
+        ex.qmap = fail_idx;
+        ex.qcount = fail_cnt;
+        ex.qbase = qbase;
+        KNN_CUDA(launch_select((const uint64_t*)E.part.p, splits, rows, c.kp, k, corpus, ldc, queries, ldq, D,
+                               c.rerank, c.rerank ? nullptr : qn, dist, idx, idx_f, s, ex));
+        launches += 2;
+        return KNNS_OK;
+    };
+    if ((rc = fix_pass(0, sp.fixA_rows, sp.fixA_S, sp.fixA_len))) return rc;
+    if ((rc = fix_pass(sp.fixA_rows, sp.fixB_rows, sp.fixB_S, sp.fixB_len))) return rc;
+    if ((rc = mark(5))) return rc;
+    if (!capture) KNN_CUDA(cudaEventRecord(E.last_done, s));
+    if (st)
+        *st = knns_stats{c.algo, sp.S, c.kp, 0, launches, 1, (int64_t)ws, 1, sp.S, sp.cap, 100 * sp.ring};
     return KNNS_OK;
 }
 
@@ -483,6 +683,22 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     const uint64_t stall_ns = capture ? 0 : g_test_stall_ns.exchange(0);
     if (host_corpus != nullptr && (pc != nullptr || capture || ldc != D))
         return set_error(KNNS_ERR_INVALID, "a corpus streamed from the host needs pitch D and no prepared index");
+    if (c.tscan) {
+        if (host_corpus != nullptr) {
+            // the whole corpus lands before the search starts (no overlap on this path)
+            cudaStream_t cs_ = E.copy_stream();
+            cudaEvent_t e0 = E.order_event(0), e1 = E.order_event(1);
+            if (!cs_ || !e0 || !e1) return set_error(KNNS_ERR_CUDA, "stream or event creation failed");
+            KNN_CUDA(cudaStreamWaitEvent(s, E.last_done, 0));
+            KNN_CUDA(cudaEventRecord(e0, s));
+            KNN_CUDA(cudaStreamWaitEvent(cs_, e0, 0));
+            KNN_CUDA(cudaMemcpyAsync(const_cast<float*>(corpus), host_corpus, (size_t)N * D * sizeof(float),
+                                     cudaMemcpyHostToDevice, cs_));
+            KNN_CUDA(cudaEventRecord(e1, cs_));
+            KNN_CUDA(cudaStreamWaitEvent(s, e1, 0));
+        }
+        return run_tscan(E, c, corpus, N, ldc, queries, Q, ldq, D, k, dist, idx, idx_f, o, s, st, pc, capture);
+    }
 
     // The threshold scan serves BF16 keys on large corpora: always in the BF16
     // precision form, and in the exact form when the data turn out BF16-exact
@@ -849,6 +1065,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         a.ksteps = f8 ? (D + 31) / 32 : (D + 15) / 16;
         a.bps = sp.bps;
         a.ring = sp.ring;
+        a.accs = sp.accs;
         a.fp8 = f8 ? 1 : 0;
         a.qs = f8 ? (const float*)E.qs.p : nullptr;
         // one scan over rows 0, stride, 2*stride, ... (nview of them) of the operand copy at src;
@@ -857,7 +1074,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
                              const float* cs_view, const float* thr, int splits, int64_t split_len, int cap,
                              int split0 = 0, cudaStream_t ls = nullptr) -> int {
             // the map moves bytes: E4M3 rows are described as rows of 16-bit units
-            int r = encode_rows_bf16(&a.tm_c, src, nview, sdp, stride * sdp, scan_box_rows(sdp));
+            int r = encode_rows_bf16(&a.tm_c, src, nview, sdp, stride * sdp, scan_box_rows(sdp, sp.accs));
             if (r) return r;
             a.cn = cn_view;
             a.cs = cs_view;
@@ -1064,7 +1281,6 @@ int prepare_corpus(Engine& E, PreparedCorpus* pc, const float* corpus, int64_t N
     if (E.cc < 100) return set_error(KNNS_ERR_UNSUPPORTED, "a prepared corpus needs sm_100+");
     const int dpb = (D + 63) & ~63, dp = (D + 31) & ~31;
     if (dpb > 256) return set_error(KNNS_ERR_UNSUPPORTED, "a prepared corpus needs D <= 256");
-    tf32 = tf32 && dp <= kMaxDpTC;
     const int64_t n_pad = cdiv(N, kScanTileN) * kScanTileN + kScanTileN;
     int rc = pc->cn.ensure(n_pad * sizeof(float));
     if (!rc) rc = pc->bf.ensure((size_t)N * dpb * 2);

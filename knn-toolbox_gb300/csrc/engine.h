@@ -33,6 +33,8 @@ struct Config {
     // E4M3 keys (KNNS_PREC_FP8): the scan's row width in 16-bit units, (D rounded up to 128) / 2
     bool fp8 = false;
     int dpf = 0;
+    // exact form on the 3xTF32 threshold scan (rows wider than 128, or shortlists over 128)
+    bool tscan = false;
 };
 
 struct Engine {
@@ -47,6 +49,8 @@ struct Engine {
     DevBuf qbf, cand, cnt, tq, cnv, fail;
     // E4M3 keys: corpus codes and row scales, query scales, sample scales
     DevBuf f8, cs, qs, csv;
+    // 3xTF32 scan: the queries' TF32 hi / lo copies and the low-part flags of their tiles
+    DevBuf qhi, qlo, qlof;
     // per-search flag words: [0] some corpus tile has a TF32 low part, [1] corpus or
     // queries not BF16-exact, [2] some value not an integer, [3] max |x| (float bits), [4] zero
     DevBuf words;

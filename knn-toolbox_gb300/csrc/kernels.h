@@ -134,17 +134,45 @@ struct ScanArgs {
     int ring;                  // ring slots
     int fp8;                   // keys from E4M3 operands with per-row scales
     int split0;                // first split of this launch (grid row y is split split0 + y)
+    int accs;                  // TMEM accumulators: 2 (tiles of 224 / 192 rows) or 4 (tiles of 96)
 };
-// corpus rows per tile (MMA N): 224 for dpb <= 128, 192 for dpb <= 256
-int scan_tile_rows(int dpb);
+// corpus rows per tile (MMA N): with 2 accumulators 224 for dpb <= 128, 192 for dpb <= 256;
+// with 4 accumulators 96
+int scan_tile_rows(int dpb, int accs);
 // rows of the corpus tensor map's box (one whole tile)
-int scan_box_rows(int dpb);
+int scan_box_rows(int dpb, int accs);
 // most columns of one tile that a single candidate segment (epilogue part) collects
-int scan_part_cols(int dpb);
-size_t scan_smem_bytes(int dpb, int bps, int ring, bool fp8 = false);
+int scan_part_cols(int dpb, int accs);
+size_t scan_smem_bytes(int dpb, int bps, int ring, bool fp8, int accs);
 // Ring geometry for dpb (want_bps = 0: automatic).  Returns 0 on success.
-int scan_plan(int dpb, int want_bps, int* bps, int* ring, bool fp8 = false);
+int scan_plan(int dpb, int want_bps, int* bps, int* ring, bool fp8, int accs);
 cudaError_t launch_scan(const ScanArgs& a, int splits, cudaStream_t s);
+
+// Tensor-core 3xTF32 threshold scan (csrc/scan_tf32.cu): 128 queries x 128-row corpus
+// tiles, K in chunks of 32 FP32 columns, both operands from shared memory (any D, a
+// multiple of 32 after padding); the candidate segments are those of the BF16 scan
+// (kScanParts per split, 32 columns of every tile each).
+struct TscanArgs {
+    CUtensorMap tm_qhi, tm_qlo;   // queries hi / lo [Q][dp] fp32, box {32, 128}, 128B swizzle
+    CUtensorMap tm_chi, tm_clo;   // corpus hi / lo view [N][dp] fp32, same boxes
+    const float* cn;              // [>= N + 128] corpus norms of the view, +inf padding
+    const float* thr;             // [Q] thresholds (null: +inf, every key collected)
+    const uint32_t* qlo_flags;    // [query tiles] 1 when the tile has a nonzero low part (null: all)
+    const uint32_t* clo_flags;    // [128-row tiles of the view] same for the corpus (null: all)
+    uint64_t* cand;               // [splits*kScanParts][Q][cap]
+    uint32_t* cnt;                // [splits*kScanParts][Q]
+    int* err;                     // device error word
+    int64_t Q;
+    int64_t N;
+    int64_t split_len;            // multiple of 128
+    int cap;
+    int dp;                       // D rounded up to 32
+    int split0;                   // first split of this launch
+    int ring;                     // ring slots (tscan_ring())
+};
+size_t tscan_smem_bytes(int ring);
+int tscan_ring();
+cudaError_t launch_tscan(const TscanArgs& a, int splits, cudaStream_t s);
 
 // Merge of the per-split shortlists, optional exact re-rank, final top-k.
 // Extra modes (all optional):

@@ -52,6 +52,7 @@
 #include <cuda_runtime.h>
 #include "common.cuh"
 #include "kernels.h"
+#include "scan_common.cuh"
 #include "tc_ptx.cuh"
 
 namespace knn {
@@ -61,6 +62,7 @@ constexpr int kEpiWarps = 4 * kScanParts;  // 4 TMEM lane quarters x kScanParts 
 constexpr int kIssuers = 2;                 // MMA issuing threads (warps 1 and 2 + kEpiWarps)
 constexpr int kScanThreads = 32 * (1 + kIssuers + kEpiWarps);
 constexpr int kNormSlots = 8;
+constexpr int kMaxAcc = 4;  // TMEM accumulators (barrier slots reserved for the largest variant)
 constexpr uint32_t kCtrlBytes = 512;
 constexpr uint32_t kTmemCols = 512;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
@@ -100,73 +102,24 @@ __device__ __forceinline__ bool scan_wait(const ScanArgs& a, const ScanSmem& s, 
     return false;
 }
 
-// Minimum of 8 keys (four min instructions).
-__device__ __forceinline__ float min8(const float* k)
-{
-    return fminf(ptx::fmin3(ptx::fmin3(k[0], k[1], k[2]), ptx::fmin3(k[3], k[4], k[5]), k[6]), k[7]);
-}
-
-// Keys ||c||^2 - 2 q.c of a W-column chunk and the mask of its 8-column groups
-// that hold a key below the lane's threshold.  BF16: q.c = acc, m = -2;
-// E4M3: q.c = s_q s_c acc with m = -2 s_q and the corpus scales s_c at scl.
-template <int W, bool kF8>
-__device__ __forceinline__ uint32_t chunk_keys(const float (&v)[W], const float* nrm, const float* scl, float m,
-                                               float T, float (&key)[W])
-{
-    const float4* n4 = reinterpret_cast<const float4*>(nrm);
-    const float4* s4 = reinterpret_cast<const float4*>(scl);
-#pragma unroll
-    for (int u = 0; u < W / 4; ++u) {
-        const float4 c = n4[u];
-        if (kF8) {
-            const float4 sc = s4[u];
-            float t0, t1, t2, t3;
-            ptx::mul2(t0, t1, v[4 * u], v[4 * u + 1], sc.x, sc.y);
-            ptx::mul2(t2, t3, v[4 * u + 2], v[4 * u + 3], sc.z, sc.w);
-            ptx::fma2(key[4 * u], key[4 * u + 1], t0, t1, m, c.x, c.y);
-            ptx::fma2(key[4 * u + 2], key[4 * u + 3], t2, t3, m, c.z, c.w);
-        } else {
-            ptx::fma2(key[4 * u], key[4 * u + 1], v[4 * u], v[4 * u + 1], m, c.x, c.y);
-            ptx::fma2(key[4 * u + 2], key[4 * u + 3], v[4 * u + 2], v[4 * u + 3], m, c.z, c.w);
-        }
-    }
-    uint32_t gm = 0;
-#pragma unroll
-    for (int g = 0; g < W / 8; ++g) gm |= (min8(key + 8 * g) < T ? 1u : 0u) << g;
-    return gm;
-}
-
-// Append the keys below T of the flagged groups, in increasing corpus index.
-// Words hold the raw key bits above the index; the selection maps them to
-// ordered keys.
-template <int W>
-__device__ __forceinline__ void chunk_append(const float (&key)[W], uint32_t gm, float T, uint32_t base,
-                                             uint64_t* out, uint32_t cap, uint32_t& cnt)
-{
-#pragma unroll
-    for (int g = 0; g < W / 8; ++g) {
-        if ((gm >> g) & 1u) {
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const float k = key[8 * g + j];
-                const bool h = k < T;
-                if (h && cnt < cap)
-                    out[cnt] = ((uint64_t)__float_as_uint(k) << 32) | (uint64_t)(base + (uint32_t)(8 * g + j));
-                cnt += h ? 1u : 0u;
-            }
-        }
-    }
-}
-
-template <int TN, bool kF8>
+template <int TN, int kNacc, bool kF8>
 __global__ void __launch_bounds__(kScanThreads, 1)
     scan_kernel(const __grid_constant__ ScanArgs a)
 {
-    constexpr int TW = TN / kScanParts - 32;  // tail columns per epilogue part (24 or 16)
+    // Each epilogue part reads TN / 4 columns of a tile as up to three chunks, every
+    // TMEM load at a multiple of its own width: [W1 p, W1 p + W1), [B2 + W2 p, ...) and
+    // [B3 + W3 p, ...): 32 + 16 + 8 (TN = 224), 32 + 16 (192), 16 + 8 (96)
+    constexpr int PC = TN / kScanParts;
+    constexpr int W1 = PC >= 32 ? 32 : 16;
+    constexpr int W2 = W1 / 2;
+    constexpr int W3 = PC - W1 - W2;
+    constexpr int B2 = kScanParts * W1;
+    constexpr int B3 = B2 + kScanParts * W2;
+    static_assert(W3 == 0 || W3 == W2 / 2, "chunks of halving widths");
+    static_assert(kNacc * TN % 32 == 0 && TN % 32 == 0, "accumulators at 32-column boundaries");
     constexpr uint32_t kBoxB = box_bytes(TN);
     constexpr uint32_t kIdesc = kF8 ? ptx::idesc_e4m3(kTileQ, TN) : ptx::idesc_bf16(kTileQ, TN);
-    constexpr uint32_t kACol = 2u * TN;  // A operand columns [kACol, kACol + dpb/2)
-    static_assert(TW == 24 || TW == 16, "tail chunk of 16 or 24 columns");
+    constexpr uint32_t kACol = (uint32_t)kNacc * TN;  // A operand columns [kACol, kACol + dpb/2)
 
     extern __shared__ __align__(1024) unsigned char sm[];
     // device-side path choice: the kernel runs only when *skip_if == 0
@@ -190,8 +143,8 @@ __global__ void __launch_bounds__(kScanThreads, 1)
     s.full = bars;
     s.empty = bars + kScanMaxRing;
     s.accf = bars + 2 * kScanMaxRing;
-    s.acce = s.accf + 2;
-    s.nfull = s.acce + 2;
+    s.acce = s.accf + kMaxAcc;
+    s.nfull = s.acce + kMaxAcc;
     s.nempty = s.nfull + kNormSlots;
     s.aready = s.nempty + kNormSlots;
     s.drain = s.aready + 1;
@@ -211,7 +164,7 @@ __global__ void __launch_bounds__(kScanThreads, 1)
             ptx::mbar_init(&s.full[i], 1);
             ptx::mbar_init(&s.empty[i], 1);
         }
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < kNacc; ++b) {
             ptx::mbar_init(&s.accf[b], 1);
             ptx::mbar_init(&s.acce[b], kEpiWarps);
         }
@@ -270,16 +223,16 @@ __global__ void __launch_bounds__(kScanThreads, 1)
         }
     } else if (warp == 1 || warp == 2 + kEpiWarps) {
         // ------------------------------------------------------------ MMA issuers
-        // issuer i takes the tiles t = i (mod 2), i.e. accumulator i; each commit
-        // tracks only its own thread's MMAs
+        // issuer i takes the tiles t = i (mod 2), into accumulator t mod kNacc; each
+        // commit tracks only its own thread's MMAs
         if (lane == 0) {
             const int iss = warp == 1 ? 0 : 1;
             bool ok = scan_wait(a, s, s.aready, 0, kDevTimeoutAload);
             ptx::tc_fence_after();
             const uint32_t a_tmem = tmem + kACol;
             for (int t = iss; t < ntiles && ok; t += kIssuers) {
-                const int b = t & 1;
-                const uint32_t use = (uint32_t)(t >> 1);
+                const int b = t % kNacc;
+                const uint32_t use = (uint32_t)(t / kNacc);
                 if (!scan_wait(a, s, &s.acce[b], (use & 1u) ^ 1u, kDevTimeoutMma)) { ok = false; break; }
                 ptx::tc_fence_after();
                 const uint32_t d_tmem = tmem + (uint32_t)b * TN;
@@ -348,42 +301,42 @@ __global__ void __launch_bounds__(kScanThreads, 1)
         uint32_t cnt = 0;
         const uint32_t cap = (uint32_t)a.cap;
         for (int t = 0; t < ntiles; ++t) {
-            const int b = t & 1;
-            const uint32_t use = (uint32_t)(t >> 1);
+            const int b = t % kNacc;
+            const uint32_t use = (uint32_t)(t / kNacc);
             const int ns = t % kNormSlots;
             // warp-uniform outcome: tcgen05.ld below is warp-collective
             const bool ok = scan_wait(a, s, &s.accf[b], use & 1u, kDevTimeoutEpilogue) &&
                             scan_wait(a, s, &s.nfull[ns], (uint32_t)(t / kNormSlots) & 1u, kDevTimeoutEpilogue);
             if (!__all_sync(0xffffffffu, ok)) break;
             ptx::tc_fence_after();
-            // this part's columns, every TMEM load at a multiple of its own width:
-            // [32p, 32p+32) then the tail [128+16p, 128+16p+16) and, for TN = 224, [192+8p, 192+8p+8)
+            // this part's columns (see the chunk layout above)
             const float* nrm = s.norms + ns * TN;
             const float* scl = scales + ns * TN;
             const uint32_t tb = tmem + (uint32_t)b * TN + lane_base;
             const uint32_t nb = (uint32_t)(n_begin + (int64_t)t * TN);
-            const int c32 = 32 * part, c16 = 128 + 16 * part, c8 = 192 + 8 * part;
-            // all three loads in flight together, one wait, then the accumulator is released:
+            const int c1 = W1 * part, c2 = B2 + W2 * part, c3 = B3 + W3 * part;
+            // all loads in flight together, one wait, then the accumulator is released:
             // the MMA may overwrite it while the keys are formed (in place) and tested
-            float va[32], v16[16], v8[8];
+            float va[W1], vb[W2], vc[W3 > 0 ? W3 : 4];
             __syncwarp();
-            ptx::tmem_ld32(tb + (uint32_t)c32, va);
-            ptx::tmem_ld16(tb + (uint32_t)c16, v16);
-            if (TW == 24) ptx::tmem_ld8(tb + (uint32_t)c8, v8);
+            ptx::tmem_ld<W1>(tb + (uint32_t)c1, va);
+            ptx::tmem_ld<W2>(tb + (uint32_t)c2, vb);
+            if constexpr (W3 > 0) ptx::tmem_ld<W3>(tb + (uint32_t)c3, vc);
             ptx::tmem_wait_ld();
             ptx::tie_regs(va);
-            ptx::tie_regs(v16);
-            if (TW == 24) ptx::tie_regs(v8);
+            ptx::tie_regs(vb);
+            if constexpr (W3 > 0) ptx::tie_regs(vc);
             ptx::tc_fence_before();
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&s.acce[b]);
-            const uint32_t ga = chunk_keys<32, kF8>(va, nrm + c32, scl + c32, m, T, va);
-            if (__any_sync(0xffffffffu, ga != 0u)) chunk_append<32>(va, ga, T, nb + (uint32_t)c32, out, cap, cnt);
-            const uint32_t g16 = chunk_keys<16, kF8>(v16, nrm + c16, scl + c16, m, T, v16);
-            const uint32_t g8 = TW == 24 ? chunk_keys<8, kF8>(v8, nrm + c8, scl + c8, m, T, v8) : 0u;
-            if (__any_sync(0xffffffffu, (g16 | g8) != 0u)) {
-                chunk_append<16>(v16, g16, T, nb + (uint32_t)c16, out, cap, cnt);
-                if (TW == 24) chunk_append<8>(v8, g8, T, nb + (uint32_t)c8, out, cap, cnt);
+            const uint32_t ga = chunk_keys<W1, kF8>(va, nrm + c1, scl + c1, m, T, va);
+            if (__any_sync(0xffffffffu, ga != 0u)) chunk_append<W1>(va, ga, T, nb + (uint32_t)c1, out, cap, cnt);
+            const uint32_t gb = chunk_keys<W2, kF8>(vb, nrm + c2, scl + c2, m, T, vb);
+            uint32_t gc = 0u;
+            if constexpr (W3 > 0) gc = chunk_keys<W3, kF8>(vc, nrm + c3, scl + c3, m, T, vc);
+            if (__any_sync(0xffffffffu, (gb | gc) != 0u)) {
+                chunk_append<W2>(vb, gb, T, nb + (uint32_t)c2, out, cap, cnt);
+                if constexpr (W3 > 0) chunk_append<W3>(vc, gc, T, nb + (uint32_t)c3, out, cap, cnt);
             }
             // norm slot ns fully read
             __syncwarp();
@@ -402,24 +355,30 @@ __global__ void __launch_bounds__(kScanThreads, 1)
 }
 }  // namespace
 
-int scan_tile_rows(int dpb) { return dpb <= 128 ? 224 : 192; }
+// two accumulators of 224 columns (192 above 128 BF16 columns), or four of 96 (any width up to
+// 256): tensor memory holds the accumulators at 32-column boundaries and the A operand after them
+int scan_tile_rows(int dpb, int accs)
+{
+    if (accs == 4) return 96;
+    return dpb <= 128 ? 224 : 192;
+}
 
-int scan_box_rows(int dpb) { return scan_tile_rows(dpb); }
+int scan_box_rows(int dpb, int accs) { return scan_tile_rows(dpb, accs); }
 
 // every epilogue part collects the same share of a tile's columns
-int scan_part_cols(int dpb) { return scan_tile_rows(dpb) / kScanParts; }
+int scan_part_cols(int dpb, int accs) { return scan_tile_rows(dpb, accs) / kScanParts; }
 
-size_t scan_smem_bytes(int dpb, int bps, int ring, bool fp8)
+size_t scan_smem_bytes(int dpb, int bps, int ring, bool fp8, int accs)
 {
-    const int tn = scan_tile_rows(dpb);
+    const int tn = scan_tile_rows(dpb, accs);
     return (size_t)ring * bps * box_bytes(tn) + norm_bytes(tn, fp8) + kCtrlBytes;
 }
 
-int scan_plan(int dpb, int want_bps, int* bps, int* ring, bool fp8)
+int scan_plan(int dpb, int want_bps, int* bps, int* ring, bool fp8, int accs)
 {
     const int nbox = dpb / 64;
-    if (dpb % 64 != 0 || nbox < 1 || nbox > 4) return -1;
-    const int tn = scan_tile_rows(dpb);
+    if (dpb % 64 != 0 || nbox < 1 || nbox > 4 || (accs != 2 && accs != 4)) return -1;
+    const int tn = scan_tile_rows(dpb, accs);
     const size_t fixed = norm_bytes(tn, fp8) + kCtrlBytes;
     auto slots = [&](int b) {
         return (int)std::min<size_t>(kScanMaxRing, (kScanSmemLimit - fixed) / ((size_t)b * box_bytes(tn)));
@@ -442,31 +401,35 @@ int scan_plan(int dpb, int want_bps, int* bps, int* ring, bool fp8)
     return 0;
 }
 
-template <int TN, bool kF8>
+template <int TN, int kNacc, bool kF8>
 static cudaError_t launch_scan_t(const ScanArgs& a, dim3 grid, size_t smem, cudaStream_t st)
 {
-    cudaError_t e = cudaFuncSetAttribute(scan_kernel<TN, kF8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(scan_kernel<TN, kNacc, kF8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
     if (e != cudaSuccess) return e;
-    scan_kernel<TN, kF8><<<grid, kScanThreads, smem, st>>>(a);
+    scan_kernel<TN, kNacc, kF8><<<grid, kScanThreads, smem, st>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_scan(const ScanArgs& a, int splits, cudaStream_t st)
 {
     const int nbox = a.dpb / 64;
-    const int tn = scan_tile_rows(a.dpb);
+    if (a.accs != 2 && a.accs != 4) return cudaErrorInvalidValue;
+    const int tn = scan_tile_rows(a.dpb, a.accs);
     const bool f8 = a.fp8 != 0;
     if (a.dpb % 64 != 0 || nbox < 1 || nbox > 4 || a.bps < 1 || nbox % a.bps != 0 || a.ring < 2 ||
         a.ring > kScanMaxRing || a.split_len % tn != 0 || a.cap < 1 || splits < 1 || a.split0 < 0 || a.qbf == nullptr ||
         a.ksteps < 1 || a.ksteps > 4 * nbox || (f8 && (a.cs == nullptr || a.qs == nullptr)))
         return cudaErrorInvalidValue;
-    const size_t smem = scan_smem_bytes(a.dpb, a.bps, a.ring, f8);
+    const size_t smem = scan_smem_bytes(a.dpb, a.bps, a.ring, f8, a.accs);
     if (smem > kScanSmemLimit) return cudaErrorInvalidValue;
     if (a.Q <= 0) return cudaSuccess;
     const int64_t qt = (a.Q + kTileQ - 1) / kTileQ;
     dim3 grid((unsigned)qt, (unsigned)splits);
-    if (tn == 224) return f8 ? launch_scan_t<224, true>(a, grid, smem, st) : launch_scan_t<224, false>(a, grid, smem, st);
-    return f8 ? launch_scan_t<192, true>(a, grid, smem, st) : launch_scan_t<192, false>(a, grid, smem, st);
+    if (tn == 96) return f8 ? launch_scan_t<96, 4, true>(a, grid, smem, st) : launch_scan_t<96, 4, false>(a, grid, smem, st);
+    if (tn == 224)
+        return f8 ? launch_scan_t<224, 2, true>(a, grid, smem, st) : launch_scan_t<224, 2, false>(a, grid, smem, st);
+    return f8 ? launch_scan_t<192, 2, true>(a, grid, smem, st) : launch_scan_t<192, 2, false>(a, grid, smem, st);
 }
 
 }  // namespace knn

@@ -117,6 +117,19 @@ __device__ __forceinline__ void mma_tf32_ts(uint32_t d_tmem, uint32_t a_tmem, ui
         : "memory");
 }
 
+// D[tmem] (+)= A[smem desc] * B[smem desc]^T, kind::tf32, cta_group::1 (both operands K-major in
+// shared memory)
+__device__ __forceinline__ void mma_tf32_ss(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                            uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
 // D[tmem] (+)= A[tmem] * B[smem desc]^T, kind::f16 (BF16 operands, FP32 accumulate), cta_group::1
 __device__ __forceinline__ void mma_bf16_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc, uint32_t idesc,
                                             uint32_t accumulate)
@@ -210,6 +223,26 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v)
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
                  : "r"(taddr)
                  : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float* v)
+{
+    uint32_t* r = reinterpret_cast<uint32_t*>(v);
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(taddr)
+                 : "memory");
+}
+
+// 32 lanes x W consecutive 32-bit columns (W = 32, 16, 8 or 4), no wait
+template <int W>
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, float (&v)[W])
+{
+    static_assert(W == 32 || W == 16 || W == 8 || W == 4, "tcgen05.ld width");
+    if constexpr (W == 32) tmem_ld32(taddr, v);
+    else if constexpr (W == 16) tmem_ld16(taddr, v);
+    else if constexpr (W == 8) tmem_ld8(taddr, v);
+    else tmem_ld4(taddr, v);
 }
 
 // After tcgen05.wait::ld: mark every register of v as written here, so that no

@@ -244,3 +244,32 @@ def test_long_shortlist_needs_the_scan(engine):
     with pytest.raises(engine.KnnsError) as e:
         run(engine, X, Qs, 100, precision=engine.PREC_BF16, shortlist=2)
     assert e.value.code == engine.ERR_UNSUPPORTED
+
+
+# ---------------------------------------------------------------- accumulator variants of the scan
+@pytest.mark.parametrize("D,form", [(128, "exact"), (256, "exact"), (72, "exact"), (128, "fp8"), (256, "bf16")])
+def test_scan_accumulator_variants_agree(engine, oracle, D, form):
+    # two accumulators of 224 (192) columns or four of 96: same keys, same candidates, same answers
+    # (integer data: bit-exact against the oracle; E4M3-exact data for the FP8 form)
+    rng = np.random.default_rng(D + len(form))
+    if form == "fp8":
+        # integers in [-7, 7] with one +-7 per row: E4M3 codes and scales are exact
+        X = rng.integers(-7, 8, (60000, D)).astype(np.float32)
+        X[:, 0] = 7.0
+        Qs = rng.integers(-7, 8, (300, D)).astype(np.float32)
+        Qs[:, 0] = -7.0
+        kw = dict(precision=engine.PREC_FP8, shortlist=2)
+    else:
+        X, Qs = ints(60000, 300, D, 3 * D)
+        kw = {} if form == "exact" else dict(precision=engine.PREC_BF16, shortlist=2)
+    k = 32
+    out = {}
+    for accs in (2, 4):
+        d, i, st = run(engine, X, Qs, k, scan=engine.SCAN_ON, scan_accs=accs, **kw)
+        assert st["scan"] == 1
+        out[accs] = (d, i)
+    np.testing.assert_array_equal(out[2][1], out[4][1])
+    np.testing.assert_array_equal(out[2][0], out[4][0])
+    od, oi = oracle.knn_gemm(X, Qs, k, kp=st["kp"], rerank=True)
+    np.testing.assert_array_equal(out[4][1], oi)
+    assert engine.last_fixups() <= 3
