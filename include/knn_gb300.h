@@ -34,7 +34,7 @@ extern "C" {
 /* kernel families */
 #define KNNS_ALGO_AUTO 0 /* tensor cores when the shape allows, else CUDA cores */
 #define KNNS_ALGO_TC 1   /* tcgen05 tensor cores: BF16 keys for data exact in BF16, else 3xTF32; D <= 128
-                            with shortlists <= 128 on any corpus, any D (to 4096) and shortlists up to 512
+                            with shortlists <= 128 on any corpus, any D (to 2048) and shortlists up to 512
                             on corpora of at least 16384 rows (the 3xTF32 threshold scan) */
 #define KNNS_ALGO_SIMT 2 /* CUDA-core FP32 fused distance + shortlist (any D, shortlist <= 512) */
 

@@ -176,8 +176,9 @@ static int encode_rows_bf16(CUtensorMap* m, const void* base, int64_t rows, int6
 constexpr int64_t kScanMinRowsForced = 16384;
 // accumulators of the threshold scan when the options leave it open
 constexpr int kScanAccsAuto = 2;
-// widest rows the 3xTF32 scan takes (its K loop has no limit; the TF32 copies cost 8 bytes a value)
-constexpr int kTscanMaxDp = 4096;
+// widest rows the 3xTF32 scan takes: its K loop has no limit, the selection's re-rank stages
+// candidate rows in shared memory (four rows of 2048 values per warp)
+constexpr int kTscanMaxDp = 2048;
 static inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 static inline int round32(int x) { return (x + 31) & ~31; }
 static inline int round16(int x) { return (x + 15) & ~15; }

@@ -139,7 +139,7 @@ select_kernel(const uint64_t* __restrict__ part, int splits, int64_t Q, int kp, 
 namespace {
 // rows of candidate vectors staged per re-rank batch: [rows][D + 1] floats (about 8 KB: the
 // staging area sets the warp's shared memory, hence how many queries run per SM)
-__host__ __device__ inline int cand_stage_rows(int D) { return D <= 128 ? 16 : 8; }
+__host__ __device__ inline int cand_stage_rows(int D) { return D <= 128 ? 16 : (D <= 512 ? 8 : 4); }
 
 // candidate words a warp can hold: threshold mode (seeding passes) and result mode
 constexpr int kCandThrMax = 1024;

@@ -7,18 +7,28 @@ oracle/_ref/src):
 
     python tests/golden/make_ref_fixtures.py OUT_DIR
 
-It calls the reference's drivers exactly as its own C API does
+It calls the reference's heap driver exactly as its own C API does
 (knnsexecute -> plan.pt2Function, src/knnsexecute.cu:14), with numStreams = 1:
 
-* gpuknnsBitonic (src/cuknnBitonic.cu:422-618) and gpuknnsHeap
-  (src/cuknnHeap.cu:394-575) on the 65,536 x 128 uniform [0,1) corpus with
-  its 1,024 queries, k = 16, seed 0 -- the whole workload;
-* gpuknnsBitonic on the 1,000,000 x 128 integer-descriptor corpus, seed 1,
-  k = 128 (its k must be a power of two; the tests truncate to k = 100), in
-  chunks of 1,000 queries: the driver sizes its N x Q distance buffers with
-  int arithmetic (src/cuknnBitonic.cu:520-536), which 1,000 x 1,000,000 keeps
-  far from 2^31.  All ten chunks are run and timed; the answers of the first
-  chunk (queries 0..999) are stored.
+* gpuknnsHeap (src/cuknnHeap.cu:394-575) on the 65,536 x 128 uniform [0,1)
+  corpus with its 1,024 queries, k = 16, seed 0 -- the whole workload;
+* gpuknnsHeap on the 1,000,000 x 128 integer-descriptor corpus, seed 1,
+  k = 128 (its heap holds 2^floor(log2 k) entries, so k must be a power of
+  two; the tests truncate to k = 100), in chunks of 250 queries: the driver
+  sizes its N x Q distance buffer with int arithmetic
+  (src/cuknnHeap.cu:476-496), and with more than 256 queries (BLOCKSIZE) its
+  norm-add kernel pdot_v2 (include/utils.h:463-483, launched at :917-926) has
+  no bound on the corpus row, which for 1,000,000 rows (not a multiple of its
+  62 rows per block) runs past the distance buffer; at 250 queries it takes the
+  bounded pdot (:442-461).  All forty chunks are run and timed; the answers of
+  the first four (queries 0..999) are stored.
+
+The reference's other driver, gpuknnsBitonic, is not called: its selection
+kernels execute __syncthreads() inside `if (threadIdx.x < obj)`
+(bitonic_shared, src/cuknnBitonic.cu:99-107; bitonic_shared2, :168-175), a
+barrier that half of the block skips from the second merge round on.  That is
+undefined on GPUs with independent thread scheduling, and on a GB300 the call
+ran until its time limit.
 
 Inputs are regenerated from the seeded generators of cuknns.synth and their
 SHA-256 is stored beside the answers, so a test can check it holds the same
@@ -52,7 +62,8 @@ for p in (os.path.join(ROOT, "knn-toolbox_gb300"), os.path.join(ROOT, "oracle"))
 
 import numpy as np  # noqa: E402
 
-C2_CHUNK = 1000
+C2_CHUNK = 250
+C2_KEEP = 1000
 
 
 def sha(a: np.ndarray) -> str:
@@ -116,37 +127,43 @@ def main(out_dir: str) -> int:
         t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
         keep.append(t)
         return t.numpy()
-    bitonic, heap = driver(lib, "gpuknnsBitonic"), driver(lib, "gpuknnsHeap")
+    heap = driver(lib, "gpuknnsHeap")
     os.makedirs(out_dir, exist_ok=True)
     log = {}
+
+    def say(msg):
+        print(msg, flush=True)
 
     # ---- 65,536 x 128 uniform, 1,024 queries, k = 16
     corpus, queries = S.uniform(65_536, 128, seed=0, nq=1_024)
     corpus, queries = pinned(corpus), pinned(queries)
-    run(bitonic, corpus, pinned(queries[:64]), 16)  # warms cuBLAS
-    bd, bi, bs, bw = run(bitonic, corpus, queries, 16)
+    say("uniform64k: warm-up call (64 queries)")
+    run(heap, corpus, pinned(queries[:64]), 16, heap=True)  # warms cuBLAS
+    say("uniform64k: 1,024 queries")
     hd, hi, hs, hw = run(heap, corpus, queries, 16, heap=True)
-    np.savez_compressed(os.path.join(out_dir, "ref_uniform64k.npz"),
-                        bitonic_dist=bd, bitonic_idx=bi, heap_dist=hd, heap_idx=hi,
+    np.savez_compressed(os.path.join(out_dir, "ref_uniform64k.npz"), heap_dist=hd, heap_idx=hi,
                         corpus_sha256=sha(corpus), queries_sha256=sha(queries),
                         N=65_536, D=128, Q=1_024, k=16, seed=0)
-    log["uniform64k"] = {"bitonic_s": bs, "bitonic_wall_s": bw, "heap_s": hs, "heap_wall_s": hw}
+    log["uniform64k"] = {"heap_s": hs, "heap_wall_s": hw}
+    say(json.dumps(log["uniform64k"]))
 
     # ---- 1,000,000 x 128 integer descriptors, 10,000 queries in chunks of 1,000, k = 128
     corpus, queries = S.int_descriptor(1_000_000, 128, seed=1, nq=10_000)
     corpus = pinned(corpus)
-    secs, walls = [], []
-    first = None
+    secs, walls, kept = [], [], []
     for c0 in range(0, queries.shape[0], C2_CHUNK):
-        d, i, s, w = run(bitonic, corpus, pinned(queries[c0:c0 + C2_CHUNK]), 128)
-        secs.append(s)
+        d, i, s_, w = run(heap, corpus, pinned(queries[c0:c0 + C2_CHUNK]), 128, heap=True)
+        say(f"int1m: queries {c0}..{c0 + C2_CHUNK - 1}: {s_:.3f} s reported, {w:.3f} s wall")
+        secs.append(s_)
         walls.append(w)
-        if first is None:
-            first = (d, i)
-    np.savez_compressed(os.path.join(out_dir, "ref_int1m_q1000.npz"),
-                        bitonic_dist=first[0], bitonic_idx=first[1],
-                        corpus_sha256=sha(corpus), queries_sha256=sha(queries[:C2_CHUNK]),
-                        N=1_000_000, D=128, Q=C2_CHUNK, k=128, seed=1)
+        if c0 < C2_KEEP:
+            kept.append((d, i))
+            if c0 + C2_CHUNK == C2_KEEP:
+                np.savez_compressed(os.path.join(out_dir, "ref_int1m_q1000.npz"),
+                                    heap_dist=np.concatenate([x[0] for x in kept]),
+                                    heap_idx=np.concatenate([x[1] for x in kept]),
+                                    corpus_sha256=sha(corpus), queries_sha256=sha(queries[:C2_KEEP]),
+                                    N=1_000_000, D=128, Q=C2_KEEP, k=128, seed=1)
     log["int1m"] = {"chunk_queries": C2_CHUNK, "chunks": len(secs), "reported_s": secs, "wall_s": walls,
                     "queries_per_s_reported": queries.shape[0] / sum(secs),
                     "queries_per_s_wall": queries.shape[0] / sum(walls)}

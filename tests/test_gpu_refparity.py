@@ -1,12 +1,12 @@
 """Parity with the reference's own CUDA library.
 
 tests/golden/ref_uniform64k.npz and tests/golden/ref_int1m_q1000.npz hold the
-answers of the reference's drivers gpuknnsBitonic (src/cuknnBitonic.cu:422-618)
-and gpuknnsHeap (src/cuknnHeap.cu:394-575), built from the reference's sources
-and run on a GB300 by tests/golden/make_ref_fixtures.py (numStreams = 1):
+answers of the reference's heap driver gpuknnsHeap (src/cuknnHeap.cu:394-575),
+built from the reference's sources and run on a GB300 by
+tests/golden/make_ref_fixtures.py (numStreams = 1; that script says why the
+bitonic driver is not run):
 
-* 65,536 x 128 uniform [0,1) corpus, its 1,024 queries, k = 16, seed 0
-  (bitonic and heap drivers);
+* 65,536 x 128 uniform [0,1) corpus, its 1,024 queries, k = 16, seed 0;
 * 1,000,000 x 128 integer-descriptor corpus, seed 1, the first 1,000 of its
   10,000 queries, k = 128 (the drivers need a power of two; the comparison
   sorts the reference's list by (distance, index) and keeps 100, the
@@ -125,13 +125,13 @@ def test_reference_answers_are_exact_on_integer_data(oracle):
     g = _fixture("ref_int1m_q1000.npz")
     X, Qs = _inputs_int(int(g["Q"]))
     sub = np.arange(0, int(g["Q"]), 20)
-    ref = _reference_topk(g["bitonic_dist"][sub], g["bitonic_idx"][sub], 100)
+    ref = _reference_topk(g["heap_dist"][sub], g["heap_idx"][sub], 100)
     ex_d, ex_i = oracle.knn_f64(X, Qs[sub], 100)
     n, worst = _compare(oracle, X, Qs[sub], ex_i, ref, lambda *a: 0.0)
     assert worst == 0.0
     # and its distances are the exact integers (key + ||q||^2 computed exactly)
-    d64 = oracle.pair_dist_f64(X, Qs[sub], g["bitonic_idx"][sub].astype(np.int32))
-    np.testing.assert_array_equal(g["bitonic_dist"][sub].astype(np.float64), d64)
+    d64 = oracle.pair_dist_f64(X, Qs[sub], g["heap_idx"][sub].astype(np.int32))
+    np.testing.assert_array_equal(g["heap_dist"][sub].astype(np.float64), d64)
 
 
 # ---------------------------------------------------------------- the engine against the reference (GPU)
@@ -144,7 +144,7 @@ def test_engine_matches_reference_uniform_65536x128_k16(engine, oracle):
     d, i = engine.search(torch.from_numpy(X).cuda(), torch.from_numpy(Qs).cuda(), k)
     d, i = d.cpu().numpy(), i.cpu().numpy()
     oracle.check_parity(X, Qs, k, d, i, gap_rel=GAP, dist_rel=DIST_REL)
-    for drv in ("bitonic", "heap"):
+    for drv in ("heap",):
         ref = f[f"{drv}_idx"]
         assert ref.shape == (1024, k)
         eps_g = _key_err_bound(X, Qs, i)
@@ -169,7 +169,7 @@ def test_engine_matches_reference_int_1m_x128_k100(engine, oracle):
     k = 100
     d, i = engine.search(torch.from_numpy(X).cuda(), torch.from_numpy(Qs).cuda(), k)
     d, i = d.cpu().numpy(), i.cpu().numpy()
-    ref = _reference_topk(g["bitonic_dist"], g["bitonic_idx"], k)
+    ref = _reference_topk(g["heap_dist"], g["heap_idx"], k)
     n, worst = _compare(oracle, X, Qs, i, ref, lambda q, a_idx, b_idx, a, b: GAP * max(a, b))
     # differences only between exactly tied candidates
     assert worst == 0.0
