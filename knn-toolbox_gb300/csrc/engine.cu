@@ -826,42 +826,78 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         ws += E.qbf.cap + E.cand.cap + E.cnt.cap + E.tq.cap + E.cnv.cap + E.fail.cap;
     }
     ws += E.part.cap + E.thr2.cap;
-    // corpus still in host memory: with the threshold scan it is copied in blocks of whole
-    // main-scan splits (each prepared and scanned as soon as it lands), the seeding sample
-    // (every sp.stride0-th row, the rows the seeding levels read) ahead of them; without the
-    // scan the search simply starts once the whole copy has landed
-    const bool streamed = host_corpus != nullptr && scan;
-    const int64_t smp_n = streamed ? cdiv(N, sp.stride0) : 0;
+    // Blocked mode (threshold scan on a corpus not prepared in advance, not under capture): the
+    // seeding sample (every sp.stride0-th row, the rows the seeding levels read) is prepared first
+    // and the seeding passes run while the corpus is prepared block by block (blocks of whole
+    // main-scan splits) on the engine's preparation stream; each block is scanned, on one of two
+    // worker streams, once it is prepared and the thresholds are seeded.  A corpus still in host
+    // memory is copied in the same blocks on the copy stream, each block prepared as it lands.
+    // Without the scan a host corpus is copied whole before the search starts.
+    const bool blocked = scan && !pc && !capture && !o.single_stream;
+    const bool streamed = blocked && host_corpus != nullptr;
+    const int64_t smp_n = blocked ? cdiv(N, sp.stride0) : 0;
     const int64_t smp_pad = cdiv(smp_n, kScanTileN) * kScanTileN + kScanTileN;
-    if (streamed) {
-        rc = E.smp.ensure((size_t)smp_n * D * sizeof(float));
+    // where the sample rows are read: the device corpus in place; page-locked host memory in place
+    // (it is mapped into the device's address space); otherwise a device copy gathered by a 2-D copy
+    const float* smp_src = nullptr;
+    int64_t smp_ld = 0;
+    bool smp_copy = false;
+    if (blocked && !streamed) {
+        smp_src = corpus;
+        smp_ld = sp.stride0 * ldc;
+    } else if (streamed) {
+        cudaPointerAttributes pa;
+        if (cudaPointerGetAttributes(&pa, host_corpus) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
+            pa.devicePointer != nullptr) {
+            smp_src = (const float*)pa.devicePointer;
+            smp_ld = sp.stride0 * D;
+        } else {
+            (void)cudaGetLastError();
+            smp_copy = true;
+            smp_ld = D;
+        }
+    }
+    if (blocked) {
+        rc = smp_copy ? E.smp.ensure((size_t)smp_n * D * sizeof(float)) : KNNS_OK;
         if (!rc) rc = E.smp_cn.ensure((size_t)smp_pad * sizeof(float));
         if (!rc) rc = E.smp_bf.ensure((size_t)smp_n * c.dpb * 2);
         if (!rc && f8) rc = E.smp_f8.ensure((size_t)smp_n * c.dpf * 2);
         if (!rc && f8) rc = E.smp_cs.ensure((size_t)smp_pad * sizeof(float));
         if (rc) return rc;
+        if (smp_copy) smp_src = (const float*)E.smp.p;
     }
-    constexpr int kHostBlocks = 8;
-    const int blk_splits = streamed ? (int)cdiv(sp.S, std::min(sp.S, kHostBlocks)) : 0;  // main-scan splits per block
-    const int nblk = streamed ? (int)cdiv(sp.S, blk_splits) : 0;
+    constexpr int kBlocks = 8;
+    const int blk_splits = blocked ? (int)cdiv(sp.S, std::min(sp.S, kBlocks)) : 0;  // main-scan splits per block
+    const int nblk = blocked ? (int)cdiv(sp.S, blk_splits) : 0;
+    auto blk_rows = [&](int b, int64_t* r0, int64_t* r1) {
+        *r0 = (int64_t)b * blk_splits * sp.len;
+        *r1 = std::min(N, *r0 + blk_splits * sp.len);
+    };
 
     if (!capture) KNN_CUDA(cudaStreamWaitEvent(s, E.last_done, 0));
     // ordering events: [0] start, [1] sample landed, [2 + b] block b landed, [2 + nblk + b]
-    // block b prepared, [2 + 2 nblk + b] block b scanned
+    // block b prepared, [2 + 2 nblk + b] block b scanned, [2 + 3 nblk] flag words cleared,
+    // [3 + 3 nblk] thresholds seeded
     auto oev = [&](int i) -> cudaEvent_t { return E.order_event(i); };
+    if (host_corpus != nullptr || blocked) {
+        if (!oev(4 + 3 * nblk) || !E.copy_stream() || (blocked && (!E.prep_stream() || !E.worker_stream(0) ||
+                                                                   !E.worker_stream(Engine::kScanWorkers - 1))))
+            return set_error(KNNS_ERR_CUDA, "stream or event creation failed");
+    }
     if (host_corpus != nullptr) {
         cudaStream_t cs_ = E.copy_stream();
-        if (!cs_ || !oev(2 + 3 * std::max(nblk, 1))) return set_error(KNNS_ERR_CUDA, "stream or event creation failed");
         // the copies overwrite the device corpus only once the previous search is done with it
         KNN_CUDA(cudaEventRecord(oev(0), s));
         KNN_CUDA(cudaStreamWaitEvent(cs_, oev(0), 0));
         if (streamed) {
-            KNN_CUDA(cudaMemcpy2DAsync(E.smp.p, (size_t)D * sizeof(float), host_corpus,
-                                       (size_t)sp.stride0 * D * sizeof(float), (size_t)D * sizeof(float),
-                                       (size_t)smp_n, cudaMemcpyHostToDevice, cs_));
+            if (smp_copy)
+                KNN_CUDA(cudaMemcpy2DAsync(E.smp.p, (size_t)D * sizeof(float), host_corpus,
+                                           (size_t)sp.stride0 * D * sizeof(float), (size_t)D * sizeof(float),
+                                           (size_t)smp_n, cudaMemcpyHostToDevice, cs_));
             KNN_CUDA(cudaEventRecord(oev(1), cs_));
             for (int b = 0; b < nblk; ++b) {
-                const int64_t r0 = (int64_t)b * blk_splits * sp.len, r1 = std::min(N, r0 + blk_splits * sp.len);
+                int64_t r0, r1;
+                blk_rows(b, &r0, &r1);
                 KNN_CUDA(cudaMemcpyAsync(const_cast<float*>(corpus) + r0 * D, host_corpus + r0 * D,
                                          (size_t)(r1 - r0) * D * sizeof(float), cudaMemcpyHostToDevice, cs_));
                 KNN_CUDA(cudaEventRecord(oev(2 + b), cs_));
@@ -901,10 +937,29 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     }
     // 3xTF32 keys on request: the data count as not BF16-exact (the preparation only ORs into the word)
     if (o.tf32_only && !bf16_only) KNN_CUDA(cudaMemsetAsync(words + 1, 0x01, 1, s));
+    if (blocked) {
+        // the corpus blocks, prepared on the preparation stream as they land (their flag words
+        // only OR into the words just cleared)
+        cudaStream_t ps = E.prep_stream();
+        KNN_CUDA(cudaEventRecord(oev(2 + 3 * nblk), s));
+        KNN_CUDA(cudaStreamWaitEvent(ps, oev(2 + 3 * nblk), 0));
+        const int64_t ld = streamed ? D : ldc;
+        for (int b = 0; b < nblk; ++b) {
+            int64_t r0, r1;
+            blk_rows(b, &r0, &r1);
+            if (streamed) KNN_CUDA(cudaStreamWaitEvent(ps, oev(2 + b), 0));
+            KNN_CUDA(launch_prep_rows(corpus + r0 * ld, r1 - r0, ld, D, c.dpb, (char*)E.bf.p + (size_t)r0 * c.dpb * 2,
+                                      cn + r0, b == nblk - 1 ? n_pad - r0 : r1 - r0, not_exact, ps, int_stats,
+                                      f8 ? (char*)E.f8.p + (size_t)r0 * c.dpf * 2 : nullptr, 2 * c.dpf,
+                                      f8 ? (float*)E.cs.p + r0 : nullptr));
+            ++launches;
+            KNN_CUDA(cudaEventRecord(oev(2 + nblk + b), ps));
+        }
+    }
     if (c.algo == KNNS_ALGO_TC) {
-        // one pass per input: BF16 copy, exactness test, integrality, norms (a streamed corpus:
-        // block by block as the blocks land, below)
-        if (!pc && !streamed) {
+        // one pass per input: BF16 copy, exactness test, integrality, norms (blocked mode: the
+        // corpus block by block, above)
+        if (!pc && !blocked) {
             KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, c.dpb, E.bf.p, cn, n_pad, not_exact, s, int_stats,
                                       f8 ? E.f8.p : nullptr, 2 * c.dpf, f8 ? (float*)E.cs.p : nullptr));
             ++launches;
@@ -916,7 +971,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
             KNN_CUDA(launch_prep_rows(queries, Q, ldq, D, c.dpb, scan ? E.qbf.p : nullptr, qn, Q, not_exact, s,
                                       int_stats));
         ++launches;
-        if (!bf16_only && !pc && !streamed) {
+        if (!bf16_only && !pc && !blocked) {
             // the TF32 split runs only for data that is not BF16-exact
             KNN_CUDA(launch_split(corpus, N, ldc, D, c.dp, (float*)E.hi.p, (float*)E.lo.p, flags, any_lo, not_exact,
                                   s));
@@ -991,7 +1046,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     const uint32_t* old_gate = scan ? not_exact : nullptr;
 
     // The shortlist path (TF32 keys in the exact form; gated on the device by the data's
-    // BF16-exactness when the scan is on).  With a streamed corpus it runs once every block
+    // BF16-exactness when the scan is on).  In blocked mode it runs once every block
     // has landed and been prepared.
     auto old_path = [&]() -> int {
         if (!run_old) return KNNS_OK;
@@ -1042,7 +1097,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         }
         return KNNS_OK;
     };
-    if (!streamed && (rc = old_path())) return rc;
+    if (!blocked && (rc = old_path())) return rc;
 
     if (!scan) {
         for (int i = 2; i <= 5; ++i)
@@ -1096,16 +1151,16 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         cs.D = D;
         // seeding, coarse to fine: level l keeps the keys below the previous level's
         // threshold (the coarsest keeps every key) and yields the key of rank j_l
-        // (a streamed corpus: the levels read the sample copied ahead of the corpus, whose
-        // row r is corpus row sp.stride0 * r -- the same rows, prepared by the same pass)
+        // (blocked mode: the levels read the sample prepared ahead of the corpus, whose row r is
+        // corpus row sp.stride0 * r -- the same rows, prepared by the same pass)
         const void* key_src = f8 ? f8_p : bf_p;
         const float* lv_cn = cn;
         const float* lv_cs = cs_p;
         int64_t lv_div = 1;
-        if (streamed) {
-            KNN_CUDA(cudaStreamWaitEvent(s, oev(1), 0));
-            KNN_CUDA(launch_prep_rows((const float*)E.smp.p, smp_n, D, D, c.dpb, E.smp_bf.p, (float*)E.smp_cn.p,
-                                      smp_pad, not_exact, s, int_stats, f8 ? E.smp_f8.p : nullptr, 2 * c.dpf,
+        if (blocked) {
+            if (smp_copy) KNN_CUDA(cudaStreamWaitEvent(s, oev(1), 0));
+            KNN_CUDA(launch_prep_rows(smp_src, smp_n, smp_ld, D, c.dpb, E.smp_bf.p, (float*)E.smp_cn.p, smp_pad,
+                                      not_exact, s, int_stats, f8 ? E.smp_f8.p : nullptr, 2 * c.dpf,
                                       f8 ? (float*)E.smp_cs.p : nullptr));
             ++launches;
             key_src = f8 ? E.smp_f8.p : E.smp_bf.p;
@@ -1138,24 +1193,16 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         }
         if ((rc = mark(2))) return rc;
         // main pass
-        if (!streamed) {
+        if (!blocked) {
             if ((rc = scan_pass(f8 ? f8_p : bf_p, N, 1, cn, cs_p, T, sp.S, sp.len, sp.cap))) return rc;
         } else {
-            // block by block: prepared on the search stream once landed, scanned on a worker
-            // stream (blocks scanned on the two workers overlap each other's tails)
+            // block by block on the worker streams (blocks scanned on the two workers overlap each
+            // other's tails), each once prepared and once the thresholds are seeded
+            KNN_CUDA(cudaEventRecord(oev(3 + 3 * nblk), s));
             for (int b = 0; b < nblk; ++b) {
-                const int64_t r0 = (int64_t)b * blk_splits * sp.len, r1 = std::min(N, r0 + blk_splits * sp.len);
-                const bool last = b == nblk - 1;
-                KNN_CUDA(cudaStreamWaitEvent(s, oev(2 + b), 0));
-                KNN_CUDA(launch_prep_rows(corpus + r0 * D, r1 - r0, D, D, c.dpb, (char*)E.bf.p + (size_t)r0 * c.dpb * 2,
-                                          cn + r0, last ? n_pad - r0 : r1 - r0, not_exact, s, int_stats,
-                                          f8 ? (char*)E.f8.p + (size_t)r0 * c.dpf * 2 : nullptr, 2 * c.dpf,
-                                          f8 ? (float*)E.cs.p + r0 : nullptr));
-                ++launches;
-                KNN_CUDA(cudaEventRecord(oev(2 + nblk + b), s));
                 cudaStream_t w = E.worker_stream(b % Engine::kScanWorkers);
-                if (!w) return set_error(KNNS_ERR_CUDA, "stream creation failed");
                 KNN_CUDA(cudaStreamWaitEvent(w, oev(2 + nblk + b), 0));
+                KNN_CUDA(cudaStreamWaitEvent(w, oev(3 + 3 * nblk), 0));
                 const int sb = std::min(blk_splits, sp.S - b * blk_splits);
                 if ((rc = scan_pass(f8 ? f8_p : bf_p, N, 1, cn, cs_p, T, sb, sp.len, sp.cap, b * blk_splits, w)))
                     return rc;
@@ -1464,6 +1511,14 @@ cudaStream_t Engine::copy_stream()
         if (cudaStreamCreateWithFlags(&copy_, cudaStreamNonBlocking) != cudaSuccess) copy_ = nullptr;
     }
     return copy_;
+}
+
+cudaStream_t Engine::prep_stream()
+{
+    if (!prep_) {
+        if (cudaStreamCreateWithFlags(&prep_, cudaStreamNonBlocking) != cudaSuccess) prep_ = nullptr;
+    }
+    return prep_;
 }
 
 cudaStream_t Engine::worker_stream(int i)

@@ -70,15 +70,17 @@ struct Engine {
     cudaStream_t host_stream();
     cudaEvent_t t0();
     cudaEvent_t t1();
-    // host-buffer searches: the stream that copies the corpus in, the streams that scan the
-    // blocks already landed, and a pool of ordering events (null on failure)
+    // blocked searches: the stream that copies a host corpus in, the stream that prepares its
+    // blocks, the streams that scan the blocks prepared, and a pool of ordering events (null on
+    // failure)
     static constexpr int kScanWorkers = 2;
     cudaStream_t copy_stream();
+    cudaStream_t prep_stream();
     cudaStream_t worker_stream(int i);
     cudaEvent_t order_event(int i);
 
   private:
-    cudaStream_t stream_ = nullptr, copy_ = nullptr, workers_[kScanWorkers] = {};
+    cudaStream_t stream_ = nullptr, copy_ = nullptr, prep_ = nullptr, workers_[kScanWorkers] = {};
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
     std::vector<cudaEvent_t> order_;
 };

@@ -55,7 +55,7 @@ class Options(ctypes.Structure):
                 ("kp", ctypes.c_int), ("timing", ctypes.c_int), ("pilot", ctypes.c_int),
                 ("precision", ctypes.c_int), ("shortlist", ctypes.c_int), ("scan", ctypes.c_int),
                 ("scan_boxes", ctypes.c_int), ("block_rows", ctypes.c_int), ("tf32_only", ctypes.c_int),
-                ("scan_accs", ctypes.c_int), ("reserved", ctypes.c_int * 1)]
+                ("scan_accs", ctypes.c_int), ("single_stream", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -151,7 +151,8 @@ def _check(rc):
 
 
 def options(algo=ALGO_AUTO, splits=0, rerank=True, kp=0, timing=False, pilot=True, precision=PREC_EXACT,
-            shortlist=0, scan=SCAN_AUTO, scan_boxes=0, block_rows=0, tf32_only=False, scan_accs=0) -> Options:
+            shortlist=0, scan=SCAN_AUTO, scan_boxes=0, block_rows=0, tf32_only=False, scan_accs=0,
+            single_stream=False) -> Options:
     o = Options()
     lib().knns_default_options(ctypes.byref(o))
     o.algo, o.splits, o.rerank, o.kp = int(algo), int(splits), int(bool(rerank)), int(kp)
@@ -162,6 +163,7 @@ def options(algo=ALGO_AUTO, splits=0, rerank=True, kp=0, timing=False, pilot=Tru
     o.block_rows = int(block_rows)
     o.tf32_only = int(bool(tf32_only))
     o.scan_accs = int(scan_accs)
+    o.single_stream = int(bool(single_stream))
     return o
 
 
@@ -202,7 +204,7 @@ def last_stats() -> dict:
 
 def search(corpus, queries, k, *, dist=None, idx=None, algo=ALGO_AUTO, splits=0, rerank=True, kp=0,
            stream=None, check=True, timing=False, pilot=True, precision=PREC_EXACT, shortlist=0, scan=SCAN_AUTO,
-           scan_boxes=0, tf32_only=False, scan_accs=0):
+           scan_boxes=0, tf32_only=False, scan_accs=0, single_stream=False):
     """kNN on CUDA tensors (float32, rows contiguous).  Returns (dist[Q,k] f32, idx[Q,k] i32)."""
     import torch
     assert corpus.is_cuda and queries.is_cuda, "search() takes device tensors"
@@ -217,7 +219,7 @@ def search(corpus, queries, k, *, dist=None, idx=None, algo=ALGO_AUTO, splits=0,
         idx = torch.empty((Q, k), dtype=torch.int32, device=corpus.device)
     s = torch.cuda.current_stream(corpus.device) if stream is None else stream
     o = options(algo, splits, rerank, kp, timing, pilot, precision, shortlist, scan, scan_boxes,
-                tf32_only=tf32_only, scan_accs=scan_accs)
+                tf32_only=tf32_only, scan_accs=scan_accs, single_stream=single_stream)
     rc = lib().knns_search_device(corpus.data_ptr(), N, corpus.stride(0), queries.data_ptr(), Q,
                                   queries.stride(0), D, k, dist.data_ptr(), idx.data_ptr(), ctypes.byref(o),
                                   ctypes.c_void_p(s.cuda_stream))
