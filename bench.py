@@ -359,7 +359,8 @@ def run_gb300(args, w):
     stream = torch.cuda.current_stream(dev)
 
     prec = {"exact": cuknns.PREC_EXACT, "bf16": cuknns.PREC_BF16, "fp8": cuknns.PREC_FP8}[args.precision]
-    scan_mode = {"auto": cuknns.SCAN_AUTO, "on": cuknns.SCAN_ON, "off": cuknns.SCAN_OFF}[args.scan]
+    scan_mode = {"auto": cuknns.SCAN_AUTO, "on": cuknns.SCAN_ON, "off": cuknns.SCAN_OFF,
+                 "tf32": cuknns.SCAN_TF32}[args.scan]
 
     def autotune(p):
         """Shortlist factor c of a precision form: recall@k against the exact form on 256 queries."""
@@ -688,7 +689,7 @@ def main():
                          "shortlist + exact re-rank")
     ap.add_argument("--shortlist", type=int, default=0,
                     help="bf16 / fp8: shortlist factor c (0 = chosen by the autotuner)")
-    ap.add_argument("--scan", default="auto", choices=["auto", "on", "off"],
+    ap.add_argument("--scan", default="auto", choices=["auto", "on", "off", "tf32"],
                     help="threshold-scan path for BF16 keys (auto: corpora of 131,072 rows and more)")
     ap.add_argument("--scan-boxes", type=int, default=0, help="threshold scan: K boxes per ring slot (0 = auto)")
     ap.add_argument("--scan-accs", type=int, default=0, choices=[0, 2, 4],

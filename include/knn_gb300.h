@@ -54,6 +54,8 @@ extern "C" {
 #define KNNS_SCAN_AUTO 0 /* used for BF16 keys when N >= 131072 */
 #define KNNS_SCAN_ON 1   /* used for BF16 keys when N >= 16384 */
 #define KNNS_SCAN_OFF 2  /* never used */
+#define KNNS_SCAN_TF32 3 /* exact form: the 3xTF32 threshold scan for every shape when N >= 16384 (by default
+                            it serves rows wider than 128 and k above 128); same results */
 
 typedef struct knns_options {
     int algo;        /* KNNS_ALGO_* */

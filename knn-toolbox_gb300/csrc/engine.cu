@@ -261,7 +261,7 @@ int resolve_config(const Engine& E, int64_t N, int64_t Q, int D, int k, const kn
     // 3xTF32 threshold scan on corpora large enough to seed its thresholds
     const bool wide = dp > kMaxDpTC || round16(k) > kMaxKpTC;
     const bool tscan_ok = E.cc >= 100 && o.scan != KNNS_SCAN_OFF && N >= kScanMinRowsForced && dp <= kTscanMaxDp &&
-                          c->kp <= kMaxKpScan && wide;
+                          c->kp <= kMaxKpScan && (wide || o.scan == KNNS_SCAN_TF32);
     if ((algo == KNNS_ALGO_AUTO || algo == KNNS_ALGO_TC) && tscan_ok) {
         c->algo = KNNS_ALGO_TC;
         c->tscan = true;
@@ -671,7 +671,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     if (N > 0x7fffffffLL) return set_error(KNNS_ERR_UNSUPPORTED, "corpus larger than 2^31-1 rows");
     if (ldc < D || ldq < D) return set_error(KNNS_ERR_INVALID, "row pitch smaller than D");
     if (!corpus || (!queries && Q > 0)) return set_error(KNNS_ERR_INVALID, "null input pointer");
-    if (o.scan < KNNS_SCAN_AUTO || o.scan > KNNS_SCAN_OFF) return set_error(KNNS_ERR_INVALID, "unknown scan mode %d", o.scan);
+    if (o.scan < KNNS_SCAN_AUTO || o.scan > KNNS_SCAN_TF32) return set_error(KNNS_ERR_INVALID, "unknown scan mode %d", o.scan);
     Config c;
     int rc = resolve_config(E, N, Q, D, k, o, &c);
     if (rc) return rc;

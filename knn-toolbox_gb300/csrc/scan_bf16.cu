@@ -423,6 +423,9 @@ cudaError_t launch_scan(const ScanArgs& a, int splits, cudaStream_t st)
         return cudaErrorInvalidValue;
     const size_t smem = scan_smem_bytes(a.dpb, a.bps, a.ring, f8, a.accs);
     if (smem > kScanSmemLimit) return cudaErrorInvalidValue;
+    // the two issuers alternate tiles: a slot's previous use must be the waiting issuer's own
+    // (a tile's slots at most half the ring), else a wait could run two phases ahead of its barrier
+    if (2 * (nbox / a.bps) > a.ring) return cudaErrorInvalidValue;
     if (a.Q <= 0) return cudaSuccess;
     const int64_t qt = (a.Q + kTileQ - 1) / kTileQ;
     dim3 grid((unsigned)qt, (unsigned)splits);

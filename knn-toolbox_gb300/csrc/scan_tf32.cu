@@ -25,7 +25,8 @@
 //   warp 0      producer: per tile and K chunk the query and corpus boxes (2-D TMA,
 //               32 fp32 x 128 rows, 128-byte swizzle), low parts only where present;
 //               per tile the corpus norms (1-D bulk copy);
-//   warps 1, 18 MMA issuers of the even / odd tiles, into accumulator t mod 4;
+//   warps 1, 18 MMA issuers, into accumulator t mod 4: of the even / odd tiles when a
+//               tile takes at most half the ring, else warp 1 alone (see below);
 //   warps 2..17 epilogue: thread = query (TMEM lane); warp 2 + 4p + j reads
 //               columns [32p, 32p + 32) of lane quarter j, releases the
 //               accumulator, forms the keys, appends those below the threshold.
@@ -184,10 +185,17 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_kernel(const __grid_constan
         }
     } else if (warp == 1 || warp == 2 + kEpi) {
         // ------------------------------------------------------------ MMA issuers
+        // Two issuers alternate tiles only when a tile's chunks fill at most half the ring: an
+        // issuer's wait on a slot must never run two phases ahead of the slot's barrier, which
+        // is guaranteed when the slot's previous use (R chunks back) is one of its own chunks
+        // (or none).  With longer tiles a second issuer could wait on a slot whose previous
+        // use, in the other issuer's tile, has not landed yet -- its parity would then read
+        // as complete -- so warp 1 issues every tile in order and warp 18 only drains.
+        const int nissue = 2 * nch <= R ? kIss : 1;
         if (lane == 0) {
             const int iss = warp == 1 ? 0 : 1;
             bool ok = true;
-            for (int t = iss; t < ntiles && ok; t += kIss) {
+            for (int t = iss; t < ntiles && ok && iss < nissue; t += nissue) {
                 const int b = t % kAcc;
                 const uint32_t use = (uint32_t)(t / kAcc);
                 if (!t_wait(a, s, &s.acce[b], (use & 1u) ^ 1u, kDevTimeoutMma)) { ok = false; break; }

@@ -29,7 +29,7 @@ LIB_PATH = os.path.join(PKG, "_build", "libknngb300.so")
 
 ALGO_AUTO, ALGO_TC, ALGO_SIMT = 0, 1, 2
 PREC_EXACT, PREC_BF16, PREC_FP8 = 0, 1, 2
-SCAN_AUTO, SCAN_ON, SCAN_OFF = 0, 1, 2
+SCAN_AUTO, SCAN_ON, SCAN_OFF, SCAN_TF32 = 0, 1, 2, 3
 OK, ERR_INVALID, ERR_CUDA, ERR_UNSUPPORTED, ERR_DEVICE_TIMEOUT, ERR_NOMEM = range(6)
 
 # Every symbol include/knn_gb300.h and include/cuknns.h declare.
