@@ -214,6 +214,20 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def path_of(st, bf16_keys):
+    """(path, dominant kernel) of a search from its statistics: bf16_keys when its keys are BF16 /
+    E4M3 (a precision form, or BF16-exact data in the exact form)."""
+    import cuknns
+    keys = st.get("scan_keys", 0)
+    if keys & 1 and (bf16_keys or not keys & 2):
+        return "threshold scan (BF16 / E4M3 keys)", "scan_kernel"
+    if keys & 2:
+        return "threshold scan (3xTF32 keys)", "tscan_kernel"
+    if st["algo"] == cuknns.ALGO_TC:
+        return "shortlist kernel (tcgen05)", "tc_kernel"
+    return "shortlist kernel (CUDA cores)", "simt_kernel"
+
+
 def lo_tile_fraction(x, rows=128):
     """Fraction of 128-row tiles whose TF32 low part (x - tf32(x), rounded to TF32) is nonzero.
 
@@ -424,14 +438,23 @@ def run_gb300(args, w):
 
     # ---- headline: the requested form, inputs resident in HBM
     with ClockSampler(local) as clk:
-        el_ms, _, st = timed(search_step(prec, args.shortlist), args.steps)
+        el_ms, hl_stages, st = timed(search_step(prec, args.shortlist, single_stream=args.single_stream),
+                                     args.steps)
+    # the path that ran: the exact form decides between BF16 and 3xTF32 keys on the device (BF16
+    # keys when every corpus and query value is exact in BF16); the data tell which
+    bf16_exact = bool(((corpus_np.view(np.uint32) & 0xFFFF) == 0).all() and
+                      ((queries_np.view(np.uint32) & 0xFFFF) == 0).all())
+    path, kern = path_of(st, args.precision != "exact" or bf16_exact)
     # whole-job throughput: replicas search world x Q queries; a corpus split searches Q
     value = Q * args.steps * (1 if split_corpus else world) / (el_ms / 1e3)
     # stage times and the dominant kernel's launch time: the same search with every kernel on the
     # search stream (by default the threshold scan overlaps the corpus preparation with the seeding
     # and scans the corpus in blocks on two more streams, which no single stage event brackets)
-    ss_ms, (prep_ms, seed_ms, fused_ms, select_ms, fix_ms, nt), _ = timed(
-        search_step(prec, args.shortlist, single_stream=True), args.steps)
+    if args.single_stream:
+        ss_ms, (prep_ms, seed_ms, fused_ms, select_ms, fix_ms, nt) = el_ms, hl_stages
+    else:
+        ss_ms, (prep_ms, seed_ms, fused_ms, select_ms, fix_ms, nt), _ = timed(
+            search_step(prec, args.shortlist, single_stream=True), args.steps)
     single_stream_qps = Q * args.steps * (1 if split_corpus else world) / (ss_ms / 1e3)
 
     # ---- accuracy against the FP64 oracle on a query sample (outside every timed region)
@@ -461,8 +484,7 @@ def run_gb300(args, w):
     # ---- the other forms on the same workload (plain form only): BF16 shortlist, 3xTF32 keys
     forms = None
     if prec == cuknns.PREC_EXACT and not args.no_forms and not split_corpus:
-        forms = {"exact": {"queries_per_s": value, "accuracy": accuracy,
-                           "path": "threshold scan (BF16 keys, data BF16-exact)" if st["scan"] else "shortlist kernel"}}
+        forms = {"exact": {"queries_per_s": value, "accuracy": accuracy, "path": path}}
         cf, tuned_bf = autotune(cuknns.PREC_BF16)
         f_ms, f_stages, f_st = timed(search_step(cuknns.PREC_BF16, cf), args.steps)
         forms["bf16_shortlist"] = {"queries_per_s": Q * args.steps * world / (f_ms / 1e3),
@@ -471,12 +493,15 @@ def run_gb300(args, w):
         t_steps = max(3, min(args.steps, 20))
         t_ms, t_stages, t_st = timed(search_step(cuknns.PREC_EXACT, 0, tf32_only=True, single_stream=True), t_steps)
         f_c, f_q = lo_tile_fraction(corpus_np), lo_tile_fraction(queries_np)
-        t_fused = (t_stages[1] + t_stages[2]) / max(1, t_stages[5])
+        t_path, t_kern = path_of(t_st, False)
+        t_scan = t_kern == "tscan_kernel"
+        # the TF32 scan's main pass is its own stage; the shortlist kernel's stage includes its pilot
+        t_fused = (t_stages[2] if t_scan else t_stages[1] + t_stages[2]) / max(1, t_stages[5])
         products = 1.0 + f_c + f_q
-        t_flops = products * 2.0 * N * Q * D * (1.0 + (1.0 / 16.0 if t_st["pilot"] else 0.0))
+        t_flops = products * 2.0 * N * Q * D * (1.0 + (1.0 / 16.0 if t_st["pilot"] and not t_scan else 0.0))
         tf32_peak = tf32_peak_live()
         forms["tf32_plain"] = {"queries_per_s": Q * t_steps * world / (t_ms / 1e3), "ms_per_step": t_ms / t_steps,
-                               "steps": t_steps, "kernel": "tc_kernel (3xTF32)",
+                               "steps": t_steps, "kernel": f"{t_kern} (3xTF32)", "path": t_path,
                                "products_per_useful_product": products,
                                "note": "3xTF32 keys; a correction product is skipped where the TF32 low part of the "
                                        "corpus tile or query tile is zero (exact zeros), as on integer data",
@@ -497,12 +522,10 @@ def run_gb300(args, w):
 
     # ---- roofline of the dominant kernel (the main fused distance pass)
     peaks, peak_kind = measured_peaks()
-    bf16_exact = bool(((corpus_np.view(np.uint32) & 0xFFFF) == 0).all() and
-                      ((queries_np.view(np.uint32) & 0xFFFF) == 0).all())
-    on_scan = bool(st["scan"]) and (args.precision != "exact" or bf16_exact)
-    kern = "scan_kernel" if on_scan else ("tc_kernel" if st["algo"] == cuknns.ALGO_TC else "simt_kernel")
-    # shortlist kernels: the fused stage includes their pilot pass
-    fused_avg_ms = (fused_ms if on_scan else seed_ms + fused_ms) / max(1, nt)
+    on_scan = kern == "scan_kernel"
+    # shortlist kernels: the fused stage includes their pilot pass; the scans' seeding passes are
+    # their own stage
+    fused_avg_ms = (fused_ms if kern in ("scan_kernel", "tscan_kernel") else seed_ms + fused_ms) / max(1, nt)
     if on_scan:
         # the main pass alone is timed (seeding passes are their own stage); one product per pair
         flops = 2.0 * N * Q * D
@@ -523,8 +546,9 @@ def run_gb300(args, w):
                 "unit": "TFLOP/s", "peak_source": peak_src, "mma_kind": mma, "products_per_useful_product": 1.0,
                 "flops_per_launch": flops, "padded_k": int(padded_k)}
     elif st["algo"] == cuknns.ALGO_TC:
-        # executed tensor work of the fused stage (main pass + the 1/16-sample pilot pass)
-        pilot_f = 1.0 + (1.0 / 16.0 if st["pilot"] else 0.0)
+        # executed tensor work of the fused stage (main pass + the 1/16-sample pilot pass of the
+        # shortlist kernel; the TF32 scan's main pass alone)
+        pilot_f = 1.0 + (1.0 / 16.0 if st["pilot"] and kern == "tc_kernel" else 0.0)
         if args.precision != "exact" or bf16_exact:
             kind, products, peak = ("bf16 shortlist" if args.precision != "exact" else "bf16 (data BF16-exact)",
                                     1.0, peaks["bf16_tflops"])
@@ -542,7 +566,7 @@ def run_gb300(args, w):
         flops = products * 2.0 * N * Q * D * pilot_f
         roof = {"bound": "tensor", "achieved": flops / (fused_avg_ms / 1e3) / 1e12, "peak": peak,
                 "unit": "TFLOP/s", "peak_source": peak_src, "mma_kind": kind,
-                "products_per_useful_product": products, "pilot_pass_included": bool(st["pilot"])}
+                "products_per_useful_product": products, "pilot_pass_included": pilot_f > 1.0}
     else:
         flops = 2.0 * N * Q * D
         peak = 152 * 128 * 2 * 2.07e9 / 1e12
@@ -575,7 +599,7 @@ def run_gb300(args, w):
                        else "working set within L2 (65,536 x 128 corpus)",
                        "algo": {1: "tcgen05", 2: "CUDA-core FP32"}[st["algo"]], "precision": args.precision,
                        "pilot": st["pilot"], "splits": st["scan_splits"] if on_scan else st["splits"],
-                       "shortlist": st["kp"], "path": "threshold scan" if on_scan else "shortlist kernel",
+                       "shortlist": st["kp"], "path": path,
                        "scan_cap": st["scan_cap"], "scan_ring": st["scan_ring"], "stages": st["stages"]},
             "stage_ms": {"prep": prep_ms / max(1, nt), "seed": seed_ms / max(1, nt), "fused": fused_ms / max(1, nt),
                          "select": select_ms / max(1, nt), "fixup": fix_ms / max(1, nt),
@@ -690,8 +714,12 @@ def main():
     ap.add_argument("--shortlist", type=int, default=0,
                     help="bf16 / fp8: shortlist factor c (0 = chosen by the autotuner)")
     ap.add_argument("--scan", default="auto", choices=["auto", "on", "off", "tf32"],
-                    help="threshold-scan path for BF16 keys (auto: corpora of 131,072 rows and more)")
+                    help="threshold scan (auto: BF16 keys for BF16-exact data and 3xTF32 keys otherwise from "
+                         "131,072 rows, 3xTF32 keys from 16,384; on: the pair from 16,384; tf32: 3xTF32 alone)")
     ap.add_argument("--scan-boxes", type=int, default=0, help="threshold scan: K boxes per ring slot (0 = auto)")
+    ap.add_argument("--single-stream", action="store_true",
+                    help="the headline search with every kernel on one stream (a fixed launch order for "
+                         "profiler captures)")
     ap.add_argument("--scan-accs", type=int, default=0, choices=[0, 2, 4],
                     help="threshold scan: tensor-memory accumulators (0 = auto)")
     ap.add_argument("--rate", type=float, default=4000.0, help="serving: offered requests per second")

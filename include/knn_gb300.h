@@ -48,14 +48,17 @@ extern "C" {
                              Where the scan does not run (N below its threshold, KNNS_SCAN_OFF) and
                              for the rare queries the scan hands to its fix-up, BF16 keys are used */
 
-/* threshold scan: for large corpora the BF16 tensor-core pass keeps no shortlist
-   on chip; per-query thresholds seeded from two corpus samples let it collect
-   only the keys that can still enter the top-kp (results are the same) */
-#define KNNS_SCAN_AUTO 0 /* used for BF16 keys when N >= 131072 */
-#define KNNS_SCAN_ON 1   /* used for BF16 keys when N >= 16384 */
+/* threshold scan: the tensor-core pass keeps no shortlist on chip; per-query thresholds
+   seeded from nested corpus samples let it collect only the keys that can still enter the
+   top-kp (results are the same).  It runs on BF16 / E4M3 keys, or in the exact form on 3xTF32
+   keys for data that are not exact in BF16 (the choice is made on the device). */
+#define KNNS_SCAN_AUTO 0 /* N >= 131072: BF16 keys for BF16-exact data (always in the BF16 / FP8
+                            forms), 3xTF32 keys otherwise; exact form with 16384 <= N < 131072
+                            (and re-rank on): the 3xTF32 scan for any data */
+#define KNNS_SCAN_ON 1   /* as AUTO, with the BF16 / 3xTF32 pair from N >= 16384 */
 #define KNNS_SCAN_OFF 2  /* never used */
-#define KNNS_SCAN_TF32 3 /* exact form: the 3xTF32 threshold scan for every shape when N >= 16384 (by default
-                            it serves rows wider than 128 and k above 128); same results */
+#define KNNS_SCAN_TF32 3 /* exact form: the 3xTF32 threshold scan alone for any data when N >= 16384
+                            (by default it also serves rows wider than 128 and k above 128); same results */
 
 typedef struct knns_options {
     int algo;        /* KNNS_ALGO_* */
@@ -97,6 +100,8 @@ typedef struct knns_stats {
     int scan_splits; /* corpus splits of the main threshold scan */
     int scan_cap;    /* candidate slots per (query, split half) of the main threshold scan */
     int scan_ring;   /* ring slots x boxes per slot, as 100 * slots + boxes */
+    int scan_keys;   /* threshold scans launched: 1 BF16 / E4M3 keys, 2 3xTF32 keys, 3 both (the exact
+                        form then runs the one that matches the data: BF16 keys for BF16-exact data) */
 } knns_stats;
 
 /* Fill *opt with the defaults (automatic algo, splits and shortlist, re-rank on, pilot on). */

@@ -174,6 +174,9 @@ static int encode_rows_bf16(CUtensorMap* m, const void* base, int64_t rows, int6
 // ---------------------------------------------------------------- planning
 // smallest corpus the threshold scan runs on when asked to (KNNS_SCAN_ON, long shortlists)
 constexpr int64_t kScanMinRowsForced = 16384;
+// Corpus size from which the BF16 / E4M3 threshold scan runs by default; below it the exact
+// form runs the 3xTF32 threshold scan (from kScanMinRowsForced rows) for data of any kind.
+constexpr int64_t kScanMinRowsAuto = 131072;
 // accumulators of the threshold scan when the options leave it open
 constexpr int kScanAccsAuto = 2;
 // widest rows the 3xTF32 scan takes: its K loop has no limit, the selection's re-rank stages
@@ -257,11 +260,13 @@ int resolve_config(const Engine& E, int64_t N, int64_t Q, int D, int k, const kn
     int algo = o.algo;
     const int dp = (int)round32(D);
     const bool tc_ok = E.cc >= 100 && dp <= kMaxDpTC;
-    // Rows wider than 128 or k above 128 (shapes of the shortlist kernel's limits) go to the
-    // 3xTF32 threshold scan on corpora large enough to seed its thresholds
+    // The 3xTF32 threshold scan alone (no BF16 path beside it) on corpora large enough to seed
+    // its thresholds: rows wider than 128 or k above 128 (the shortlist kernel's limits),
+    // corpora below the BF16 scan's default size, or on request
     const bool wide = dp > kMaxDpTC || round16(k) > kMaxKpTC;
+    const bool small = o.scan == KNNS_SCAN_AUTO && N < kScanMinRowsAuto && c->rerank;
     const bool tscan_ok = E.cc >= 100 && o.scan != KNNS_SCAN_OFF && N >= kScanMinRowsForced && dp <= kTscanMaxDp &&
-                          c->kp <= kMaxKpScan && (wide || o.scan == KNNS_SCAN_TF32);
+                          c->kp <= kMaxKpScan && (wide || small || o.scan == KNNS_SCAN_TF32);
     if ((algo == KNNS_ALGO_AUTO || algo == KNNS_ALGO_TC) && tscan_ok) {
         c->algo = KNNS_ALGO_TC;
         c->tscan = true;
@@ -310,10 +315,10 @@ int resolve_config(const Engine& E, int64_t N, int64_t Q, int D, int k, const kn
 // Seeding: the main scan needs, per query, a threshold T with at least kp keys
 // below it (then every top-kp candidate is collected) and few more.  Nested
 // corpus samples give it, coarse to fine: level l keeps every stride_l-th row
-// (stride s for the finest level -- seed_stride below --, 16x more per coarser level, the
+// (stride s for the finest level -- seed_stride below --, kSeedRatio x more per coarser level, the
 // coarsest small enough to keep every key).  Each level collects the keys below
 // the previous level's threshold and picks the key of rank j_l as its own.  With
-// m = j_next / 16 (the expected rank, in this level's sample, of the key of
+// m = j_next / kSeedRatio (the expected rank, in this level's sample, of the key of
 // rank j_next in the next one; m = kp / s for the finest level)
 // j = 2m + 4 sqrt(m) + 1 leaves a chance of roughly 1e-5 that fewer than j_next
 // keys fall below the threshold at the next level.  Queries for which that
@@ -328,6 +333,9 @@ constexpr int kMaxSeedLevels = 6;
 // shortlists take a finer stride, so that a query's main-pass candidates
 // (mean + six standard deviations) still fit the selection's buffer.
 constexpr int64_t kSeedStride = 32;
+// Stride ratio of neighbouring levels: 32 leaves two levels for a million rows (every 32nd row,
+// and every 1024th, whose keys are all kept), where 16 needs three.
+constexpr int64_t kSeedRatio = 32;
 
 static int64_t seed_stride(int kp)
 {
@@ -408,11 +416,11 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
         pc = scan_part_cols(dpb, P->accs);  // segment columns per tile
     }
     const int64_t qt = cdiv(Q, kTileQ);  // query tiles
-    // levels, finest first: strides s, 16 s, ... until the sample fits the selector whole
+    // levels, finest first: strides s, kSeedRatio s, ... until the sample fits the selector whole
     P->stride0 = seed_stride(kp);
     int64_t st[kMaxSeedLevels];
     int L = 0;
-    for (int64_t stride = P->stride0;; stride *= 16) {
+    for (int64_t stride = P->stride0;; stride *= kSeedRatio) {
         if (L == kMaxSeedLevels) return set_error(KNNS_ERR_UNSUPPORTED, "threshold scan: corpus too large to seed");
         st[L++] = stride;
         if (cdiv(N, stride) <= kCandMax / 2) break;
@@ -493,9 +501,188 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
 }
 
 // ---------------------------------------------------------------- 3xTF32 threshold scan
-// The exact form for rows wider than 128 or k above 128: corpus and query norms and TF32
-// hi / lo copies, threshold seeding over nested corpus samples, the main scan, the selection
-// with the exact re-rank, and the CUDA-core fix-up of the queries the scan could not answer.
+// The stages of the 3xTF32 threshold scan over prepared corpus operands (norms, TF32 hi / lo
+// copies and their tile flags) and query norms: the queries' TF32 split, threshold seeding over
+// nested corpus samples, the main scan, the selection with the exact re-rank, and the CUDA-core
+// fix-up of the queries the scan could not answer.  With run_if set, every kernel that writes
+// thresholds, candidates or results returns at once unless *run_if != 0 (the exact form's
+// device-side choice between BF16 and TF32 keys); its failed-query list is its own (fail), so
+// the other path's fix-up never sees it.
+struct TscanStages {
+    Engine& E;
+    const Config& c;
+    const ScanPlan& sp;
+    const float* corpus;
+    int64_t N, ldc;
+    const float* queries;
+    int64_t Q, ldq;
+    int D, k;
+    const float* cn;
+    const float* hi;
+    const float* lo;
+    const uint32_t* cflags;
+    const float* qn;
+    float* dist;
+    int32_t* idx;
+    float* idx_f;
+    const uint32_t* run_if;
+    uint32_t* q_any_lo;  // a word the queries' split ORs its low-part flag into
+    DevBuf& fail;
+    cudaStream_t s;
+    int launches = 0;
+    TscanArgs a;
+    const float* T = nullptr;
+
+    // buffers of the queries and of the plan (the corpus side is the caller's)
+    int ensure()
+    {
+        const int dp = c.dp;
+        int rc = E.qhi.ensure((size_t)Q * dp * sizeof(float));
+        if (!rc) rc = E.qlo.ensure((size_t)Q * dp * sizeof(float));
+        if (!rc) rc = E.qlof.ensure(((size_t)cdiv(Q, 128) + 4) * sizeof(uint32_t));
+        if (!rc) rc = E.tq.ensure((size_t)2 * Q * sizeof(float));
+        if (!rc) rc = E.cand.ensure(sp.cand_words * sizeof(uint64_t));
+        if (!rc) rc = E.cnt.ensure(sp.cnt_words * sizeof(uint32_t));
+        if (!rc) rc = E.cnv.ensure(sp.norm_words * sizeof(float));
+        if (!rc) rc = fail.ensure((size_t)(Q + 1) * sizeof(uint32_t));
+        if (!rc) rc = E.part.ensure(sp.part_words * sizeof(uint64_t));
+        if (!rc) rc = E.thr2.ensure(Q * sizeof(uint32_t));
+        return rc;
+    }
+    size_t workspace() const
+    {
+        return E.qhi.cap + E.qlo.cap + E.qlof.cap + E.tq.cap + E.cand.cap + E.cnt.cap + E.cnv.cap + fail.cap +
+               E.part.cap + E.thr2.cap;
+    }
+    // the queries' TF32 hi / lo copies and the tensor maps of the scan's query operand
+    int split_queries()
+    {
+        KNN_CUDA(launch_split(queries, Q, ldq, D, c.dp, (float*)E.qhi.p, (float*)E.qlo.p, (uint32_t*)E.qlof.p,
+                              q_any_lo, run_if, s));
+        ++launches;
+        memset(&a, 0, sizeof(a));
+        int rc = encode_rows(&a.tm_qhi, (const float*)E.qhi.p, Q, c.dp, c.dp);
+        if (!rc) rc = encode_rows(&a.tm_qlo, (const float*)E.qlo.p, Q, c.dp, c.dp);
+        if (rc) return rc;
+        a.qlo_flags = (const uint32_t*)E.qlof.p;
+        a.cand = (uint64_t*)E.cand.p;
+        a.cnt = (uint32_t*)E.cnt.p;
+        a.err = (int*)E.err.p;
+        a.Q = Q;
+        a.dp = c.dp;
+        a.ring = sp.ring;
+        a.run_if = run_if;
+        return KNNS_OK;
+    }
+    // one scan over rows 0, stride, 2*stride, ... of the corpus (nview of them)
+    int pass(int64_t nview, int64_t stride, const float* cn_view, const float* thr, int splits, int64_t split_len,
+             int cap, const uint32_t* flags)
+    {
+        int r = encode_rows(&a.tm_chi, hi, nview, c.dp, stride * c.dp);
+        if (!r) r = encode_rows(&a.tm_clo, lo, nview, c.dp, stride * c.dp);
+        if (r) return r;
+        a.cn = cn_view;
+        a.thr = thr;
+        a.N = nview;
+        a.split_len = split_len;
+        a.cap = cap;
+        a.clo_flags = flags;
+        KNN_CUDA(launch_tscan(a, splits, s));
+        ++launches;
+        return KNNS_OK;
+    }
+    CandSelect cand_select() const
+    {
+        CandSelect cs;
+        cs.cand = (const uint64_t*)E.cand.p;
+        cs.cnt = (const uint32_t*)E.cnt.p;
+        cs.Q = Q;
+        cs.D = D;
+        cs.skip_if_zero = run_if;
+        return cs;
+    }
+    // seeding, coarse to fine: level l keeps the keys below the previous level's threshold (the
+    // coarsest keeps every key) and yields the key of rank j_l
+    int seed()
+    {
+        float* Tbuf[2] = {(float*)E.tq.p, (float*)E.tq.p + Q};
+        float* cnv = (float*)E.cnv.p;
+        CandSelect cs = cand_select();
+        T = nullptr;
+        for (int l = 0; l < sp.levels; ++l) {
+            const ScanLevel& v = sp.lv[l];
+            KNN_CUDA(launch_gather_norms(cn, v.n, v.stride, cnv, v.n_pad, s));
+            int rc = pass(v.n, v.stride, cnv, T, v.S, v.len, v.cap, nullptr);
+            if (rc) return rc;
+            cs.nseg = kScanParts * v.S;
+            cs.cap = v.cap;
+            cs.thr_out = Tbuf[l & 1];
+            cs.thr_rank = v.j;
+            cs.thr_fallback = T;
+            KNN_CUDA(launch_select_cand(cs, s));
+            launches += 2;
+            T = Tbuf[l & 1];
+            cnv += v.n_pad;
+        }
+        return KNNS_OK;
+    }
+    int main_pass() { return pass(N, 1, cn, T, sp.S, sp.len, sp.cap, cflags); }
+    int select()
+    {
+        uint32_t* fail_cnt = (uint32_t*)fail.p;
+        KNN_CUDA(cudaMemsetAsync(fail_cnt, 0, sizeof(uint32_t), s));
+        CandSelect cs = cand_select();
+        cs.nseg = kScanParts * sp.S;
+        cs.cap = sp.cap;
+        cs.kp = c.kp;
+        cs.k = k;
+        cs.need = (int)std::min<int64_t>(c.kp, N);
+        cs.buf_words = sp.sel_words;
+        cs.rerank = c.rerank;
+        cs.corpus = corpus;
+        cs.ldc = ldc;
+        cs.queries = queries;
+        cs.ldq = ldq;
+        cs.qn = qn;
+        cs.out_dist = dist;
+        cs.out_idx = idx;
+        cs.out_idx_f = idx_f;
+        cs.fail_idx = (int32_t*)fail.p + 1;
+        cs.fail_cnt = fail_cnt;
+        KNN_CUDA(launch_select_cand(cs, s));
+        ++launches;
+        return KNNS_OK;
+    }
+    // fix-up: the queries the scan could not answer, on the CUDA-core kernel (exact FP32 keys),
+    // compacted; launches whose rows are all past the failure count return at once
+    int fix_pass(int64_t qbase, int64_t rows, int splits, int64_t split_len)
+    {
+        if (rows <= 0) return KNNS_OK;
+        uint32_t* fail_cnt = (uint32_t*)fail.p;
+        int32_t* fail_idx = (int32_t*)fail.p + 1;
+        uint32_t* thr2 = (uint32_t*)E.thr2.p;
+        KNN_CUDA(cudaMemsetAsync(thr2, 0xFF, rows * sizeof(uint32_t), s));
+        KNN_CUDA(launch_simt(corpus, N, ldc, cn, queries, rows, ldq, D, c.kp, 32, split_len, splits,
+                             (uint64_t*)E.part.p, thr2, s, nullptr, fail_idx, fail_cnt, qbase));
+        SelectExtra ex;
+        ex.qmap = fail_idx;
+        ex.qcount = fail_cnt;
+        ex.qbase = qbase;
+        KNN_CUDA(launch_select((const uint64_t*)E.part.p, splits, rows, c.kp, k, corpus, ldc, queries, ldq, D,
+                               c.rerank, c.rerank ? nullptr : qn, dist, idx, idx_f, s, ex));
+        launches += 2;
+        return KNNS_OK;
+    }
+    int fix()
+    {
+        int rc = fix_pass(0, sp.fixA_rows, sp.fixA_S, sp.fixA_len);
+        if (!rc) rc = fix_pass(sp.fixA_rows, sp.fixB_rows, sp.fixB_S, sp.fixB_len);
+        return rc;
+    }
+};
+
+// The exact form on TF32 keys alone (rows wider than 128, k above 128, corpora below the BF16
+// scan's size, or on request): corpus and query norms and TF32 copies, then the stages above.
 static int run_tscan(Engine& E, const Config& c, const float* corpus, int64_t N, int64_t ldc, const float* queries,
                      int64_t Q, int64_t ldq, int D, int k, float* dist, int32_t* idx, float* idx_f,
                      const knns_options& o, cudaStream_t s, knns_stats* st, const PreparedCorpus* pc, bool capture)
@@ -515,26 +702,16 @@ static int run_tscan(Engine& E, const Config& c, const float* corpus, int64_t N,
         if (rc) return rc;
     }
     rc = E.qn.ensure(Q * sizeof(float));
-    if (!rc) rc = E.qhi.ensure((size_t)Q * dp * sizeof(float));
-    if (!rc) rc = E.qlo.ensure((size_t)Q * dp * sizeof(float));
-    if (!rc) rc = E.qlof.ensure(((size_t)cdiv(Q, 128) + 4) * sizeof(uint32_t));
     if (!rc) rc = E.words.ensure(8 * sizeof(uint32_t));
-    if (!rc) rc = E.tq.ensure((size_t)2 * Q * sizeof(float));
-    if (!rc) rc = E.cand.ensure(sp.cand_words * sizeof(uint64_t));
-    if (!rc) rc = E.cnt.ensure(sp.cnt_words * sizeof(uint32_t));
-    if (!rc) rc = E.cnv.ensure(sp.norm_words * sizeof(float));
-    if (!rc) rc = E.fail.ensure((size_t)(Q + 1) * sizeof(uint32_t));
-    if (!rc) rc = E.part.ensure(sp.part_words * sizeof(uint64_t));
-    if (!rc) rc = E.thr2.ensure(Q * sizeof(uint32_t));
     if (rc) return rc;
-    const size_t ws = (pc ? 0 : E.cn.cap + E.hi.cap + E.lo.cap + E.loflags.cap) + E.qn.cap + E.qhi.cap + E.qlo.cap +
-                      E.tq.cap + E.cand.cap + E.cnt.cap + E.cnv.cap + E.fail.cap + E.part.cap + E.thr2.cap;
-    float* cn = (float*)(pc ? pc->cn.p : E.cn.p);
-    const float* hi = (const float*)(pc ? pc->hi.p : E.hi.p);
-    const float* lo = (const float*)(pc ? pc->lo.p : E.lo.p);
-    uint32_t* cflags = (uint32_t*)(pc ? pc->tiles.p : E.loflags.p);
-    float* qn = (float*)E.qn.p;
     uint32_t* words = (uint32_t*)E.words.p;
+    float* cn = (float*)(pc ? pc->cn.p : E.cn.p);
+    uint32_t* cflags = (uint32_t*)(pc ? pc->tiles.p : E.loflags.p);
+    TscanStages ts{E, c, sp, corpus, N, ldc, queries, Q, ldq, D, k, cn,
+                   (const float*)(pc ? pc->hi.p : E.hi.p), (const float*)(pc ? pc->lo.p : E.lo.p), cflags,
+                   (const float*)E.qn.p, dist, idx, idx_f, nullptr, words + 1, E.fail, s};
+    if ((rc = ts.ensure())) return rc;
+    const size_t ws = (pc ? 0 : E.cn.cap + E.hi.cap + E.lo.cap + E.loflags.cap) + E.qn.cap + ts.workspace();
 
     if (!capture) KNN_CUDA(cudaStreamWaitEvent(s, E.last_done, 0));
     cudaEvent_t tv[Engine::kTimingEvents] = {};
@@ -544,119 +721,27 @@ static int run_tscan(Engine& E, const Config& c, const float* corpus, int64_t N,
         return KNNS_OK;
     };
     if ((rc = mark(0))) return rc;
-    int launches = 0;
     KNN_CUDA(cudaMemsetAsync(words, 0, 4 * sizeof(uint32_t), s));
     if (!pc) {
         KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, 0, nullptr, cn, n_pad, nullptr, s));
         KNN_CUDA(launch_split(corpus, N, ldc, D, dp, (float*)E.hi.p, (float*)E.lo.p, cflags, words, nullptr, s));
-        launches += 2;
+        ts.launches += 2;
     }
-    KNN_CUDA(launch_prep_rows(queries, Q, ldq, D, 0, nullptr, qn, Q, nullptr, s));
-    KNN_CUDA(launch_split(queries, Q, ldq, D, dp, (float*)E.qhi.p, (float*)E.qlo.p, (uint32_t*)E.qlof.p, words + 1,
-                          nullptr, s));
-    launches += 2;
+    KNN_CUDA(launch_prep_rows(queries, Q, ldq, D, 0, nullptr, (float*)E.qn.p, Q, nullptr, s));
+    ++ts.launches;
+    if ((rc = ts.split_queries())) return rc;
     if ((rc = mark(1))) return rc;
-
-    TscanArgs a;
-    memset(&a, 0, sizeof(a));
-    if ((rc = encode_rows(&a.tm_qhi, (const float*)E.qhi.p, Q, dp, dp))) return rc;
-    if ((rc = encode_rows(&a.tm_qlo, (const float*)E.qlo.p, Q, dp, dp))) return rc;
-    a.qlo_flags = (const uint32_t*)E.qlof.p;
-    a.cand = (uint64_t*)E.cand.p;
-    a.cnt = (uint32_t*)E.cnt.p;
-    a.err = (int*)E.err.p;
-    a.Q = Q;
-    a.dp = dp;
-    a.ring = sp.ring;
-    // one scan over rows 0, stride, 2*stride, ... of the corpus (nview of them)
-    auto tscan_pass = [&](int64_t nview, int64_t stride, const float* cn_view, const float* thr, int splits,
-                          int64_t split_len, int cap, const uint32_t* flags) -> int {
-        int r = encode_rows(&a.tm_chi, hi, nview, dp, stride * dp);
-        if (!r) r = encode_rows(&a.tm_clo, lo, nview, dp, stride * dp);
-        if (r) return r;
-        a.cn = cn_view;
-        a.thr = thr;
-        a.N = nview;
-        a.split_len = split_len;
-        a.cap = cap;
-        a.clo_flags = flags;
-        KNN_CUDA(launch_tscan(a, splits, s));
-        ++launches;
-        return KNNS_OK;
-    };
-    float* Tbuf[2] = {(float*)E.tq.p, (float*)E.tq.p + Q};
-    uint32_t* fail_cnt = (uint32_t*)E.fail.p;
-    int32_t* fail_idx = (int32_t*)E.fail.p + 1;
-    CandSelect cs;
-    cs.cand = (const uint64_t*)E.cand.p;
-    cs.cnt = (const uint32_t*)E.cnt.p;
-    cs.Q = Q;
-    cs.D = D;
-    float* cnv = (float*)E.cnv.p;
-    const float* T = nullptr;
-    for (int l = 0; l < sp.levels; ++l) {
-        const ScanLevel& v = sp.lv[l];
-        KNN_CUDA(launch_gather_norms(cn, v.n, v.stride, cnv, v.n_pad, s));
-        if ((rc = tscan_pass(v.n, v.stride, cnv, T, v.S, v.len, v.cap, nullptr))) return rc;
-        cs.nseg = kScanParts * v.S;
-        cs.cap = v.cap;
-        cs.thr_out = Tbuf[l & 1];
-        cs.thr_rank = v.j;
-        cs.thr_fallback = T;
-        KNN_CUDA(launch_select_cand(cs, s));
-        launches += 2;
-        T = Tbuf[l & 1];
-        cnv += v.n_pad;
-    }
+    if ((rc = ts.seed())) return rc;
     if ((rc = mark(2))) return rc;
-    if ((rc = tscan_pass(N, 1, cn, T, sp.S, sp.len, sp.cap, cflags))) return rc;
+    if ((rc = ts.main_pass())) return rc;
     if ((rc = mark(3))) return rc;
-    KNN_CUDA(cudaMemsetAsync(fail_cnt, 0, sizeof(uint32_t), s));
-    cs.nseg = kScanParts * sp.S;
-    cs.cap = sp.cap;
-    cs.thr_out = nullptr;
-    cs.thr_fallback = nullptr;
-    cs.kp = c.kp;
-    cs.k = k;
-    cs.need = (int)std::min<int64_t>(c.kp, N);
-    cs.buf_words = sp.sel_words;
-    cs.rerank = c.rerank;
-    cs.corpus = corpus;
-    cs.ldc = ldc;
-    cs.queries = queries;
-    cs.ldq = ldq;
-    cs.qn = qn;
-    cs.out_dist = dist;
-    cs.out_idx = idx;
-    cs.out_idx_f = idx_f;
-    cs.fail_idx = fail_idx;
-    cs.fail_cnt = fail_cnt;
-    KNN_CUDA(launch_select_cand(cs, s));
-    ++launches;
+    if ((rc = ts.select())) return rc;
     if ((rc = mark(4))) return rc;
-    // fix-up: the queries the scan could not answer, on the CUDA-core kernel (exact FP32 keys),
-    // compacted; launches whose rows are all past the failure count return at once
-    auto fix_pass = [&](int64_t qbase, int64_t rows, int splits, int64_t split_len) -> int {
-        if (rows <= 0) return KNNS_OK;
-        uint32_t* thr2 = (uint32_t*)E.thr2.p;
-        KNN_CUDA(cudaMemsetAsync(thr2, 0xFF, rows * sizeof(uint32_t), s));
-        KNN_CUDA(launch_simt(corpus, N, ldc, cn, queries, rows, ldq, D, c.kp, 32, split_len, splits,
-                             (uint64_t*)E.part.p, thr2, s, nullptr, fail_idx, fail_cnt, qbase));
-        SelectExtra ex;
-        ex.qmap = fail_idx;
-        ex.qcount = fail_cnt;
-        ex.qbase = qbase;
-        KNN_CUDA(launch_select((const uint64_t*)E.part.p, splits, rows, c.kp, k, corpus, ldc, queries, ldq, D,
-                               c.rerank, c.rerank ? nullptr : qn, dist, idx, idx_f, s, ex));
-        launches += 2;
-        return KNNS_OK;
-    };
-    if ((rc = fix_pass(0, sp.fixA_rows, sp.fixA_S, sp.fixA_len))) return rc;
-    if ((rc = fix_pass(sp.fixA_rows, sp.fixB_rows, sp.fixB_S, sp.fixB_len))) return rc;
+    if ((rc = ts.fix())) return rc;
     if ((rc = mark(5))) return rc;
     if (!capture) KNN_CUDA(cudaEventRecord(E.last_done, s));
     if (st)
-        *st = knns_stats{c.algo, sp.S, c.kp, 0, launches, 1, (int64_t)ws, 1, sp.S, sp.cap, 100 * sp.ring};
+        *st = knns_stats{c.algo, sp.S, c.kp, 0, ts.launches, 1, (int64_t)ws, 1, sp.S, sp.cap, 100 * sp.ring, 2};
     return KNNS_OK;
 }
 
@@ -676,7 +761,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     int rc = resolve_config(E, N, Q, D, k, o, &c);
     if (rc) return rc;
     if (Q == 0) {
-        if (st) *st = knns_stats{c.algo, c.splits, c.kp, c.stages, 0, 0, 0, 0, 0, 0, 0};
+        if (st) *st = knns_stats{c.algo, c.splits, c.kp, c.stages, 0, 0, 0, 0, 0, 0, 0, 0};
         return KNNS_OK;
     }
     // the precision forms: BF16 / E4M3 keys only, always re-ranked
@@ -702,12 +787,13 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     }
 
     // The threshold scan serves BF16 keys on large corpora: always in the BF16
-    // precision form, and in the exact form when the data turn out BF16-exact
-    // (decided on the device; the TF32 path then stands down and vice versa).
-    ScanPlan sp;
+    // precision form, and in the exact form when the data turn out BF16-exact; otherwise the
+    // exact form runs the 3xTF32 threshold scan (decided on the device: the kernels of the path
+    // that does not match the data return at once).
+    ScanPlan sp, sp_tf;
     bool scan = false;
     if (c.algo == KNNS_ALGO_TC && o.scan != KNNS_SCAN_OFF && E.cc >= 100 && c.dpb <= 256 && c.rerank) {
-        const int64_t min_n = (o.scan == KNNS_SCAN_ON || c.kp > kMaxKpTC) ? kScanMinRowsForced : 131072;
+        const int64_t min_n = (o.scan == KNNS_SCAN_ON || c.kp > kMaxKpTC) ? kScanMinRowsForced : kScanMinRowsAuto;
         if (N >= min_n) {
             rc = plan_scan(E, N, Q, c.fp8 ? c.dpf : c.dpb, c.kp, o, &sp, c.fp8);
             if (rc) return rc;
@@ -716,7 +802,11 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     }
     // E4M3 keys exist only on the scan: without it the form falls back to BF16 keys
     const bool f8 = scan && c.fp8;
-    const bool run_old = !(scan && bf16_only);  // the shortlist path is needed (possibly gated)
+    // beside the BF16 scan, the exact form's TF32 keys run on the 3xTF32 scan; without the scan,
+    // on the shortlist kernel
+    const bool tf_scan = scan && !bf16_only;
+    const bool run_old = !scan;
+    if (tf_scan && (rc = plan_scan(E, N, Q, c.dpb, c.kp, o, &sp_tf, false, true))) return rc;
     if (pc != nullptr) {
         // (the CUDA-core kernel uses the index's norms only)
         if (pc->corpus != corpus || pc->N != N || pc->ldc != ldc || pc->D != D ||
@@ -826,6 +916,17 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         ws += E.qbf.cap + E.cand.cap + E.cnt.cap + E.tq.cap + E.cnv.cap + E.fail.cap;
     }
     ws += E.part.cap + E.thr2.cap;
+    // the 3xTF32 scan beside the BF16 one (its buffers are shared with it but for its queries'
+    // TF32 copies and its failed-query list: only one of the two paths runs)
+    const float* cn_ts = (const float*)(pc ? pc->cn.p : E.cn.p);
+    TscanStages ts{E, c, sp_tf, corpus, N, ldc, queries, Q, ldq, D, k, cn_ts,
+                   (const float*)(pc ? pc->hi.p : E.hi.p), (const float*)(pc ? pc->lo.p : E.lo.p),
+                   (const uint32_t*)(pc ? pc->tiles.p : E.loflags.p), (const float*)E.qn.p, dist, idx, idx_f,
+                   (const uint32_t*)E.words.p + 1, (uint32_t*)E.words.p + 5, E.tfail, s};
+    if (tf_scan) {
+        if ((rc = ts.ensure())) return rc;
+        ws += E.qhi.cap + E.qlo.cap + E.qlof.cap + E.tfail.cap;
+    }
     // Blocked mode (threshold scan on a corpus not prepared in advance, not under capture): the
     // seeding sample (every sp.stride0-th row, the rows the seeding levels read) is prepared first
     // and the seeding passes run while the corpus is prepared block by block (blocks of whole
@@ -931,9 +1032,9 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     uint32_t* flags = c.algo == KNNS_ALGO_TC ? (uint32_t*)(pc ? pc->tiles.p : E.loflags.p) : nullptr;
     if (pc) {
         KNN_CUDA(cudaMemcpyAsync(words, pc->words.p, 4 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
-        KNN_CUDA(cudaMemsetAsync(words + 4, 0, sizeof(uint32_t), s));
+        KNN_CUDA(cudaMemsetAsync(words + 4, 0, 2 * sizeof(uint32_t), s));
     } else {
-        KNN_CUDA(cudaMemsetAsync(words, 0, 5 * sizeof(uint32_t), s));
+        KNN_CUDA(cudaMemsetAsync(words, 0, 6 * sizeof(uint32_t), s));
     }
     // 3xTF32 keys on request: the data count as not BF16-exact (the preparation only ORs into the word)
     if (o.tf32_only && !bf16_only) KNN_CUDA(cudaMemsetAsync(words + 1, 0x01, 1, s));
@@ -977,6 +1078,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
                                   s));
             ++launches;
         }
+        if (tf_scan && !blocked && (rc = ts.split_queries())) return rc;
     } else {
         if (!pc) {
             KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, 0, nullptr, cn, n_pad, nullptr, s));
@@ -992,7 +1094,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     if ((rc = mark(1))) return rc;
 
     // One shortlist pass over a corpus view: rows 0, stride, 2*stride, ... (nview
-    // of them).  With the threshold scan on, the BF16 variant is left to the scan.
+    // of them); runs only without the threshold scan.
     auto fused_pass = [&](int64_t nview, int64_t stride, const float* cn_view, int kp, int stages, int splits,
                           int64_t split_len, uint32_t* thr, const uint32_t* redo, bool tile_flags) -> int {
         if (c.algo == KNNS_ALGO_TC) {
@@ -1031,10 +1133,8 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
                 KNN_CUDA(launch_tc(a, splits, false, s));
                 ++launches;
             }
-            if (!scan) {
-                KNN_CUDA(launch_tc(a, splits, true, s));
-                ++launches;
-            }
+            KNN_CUDA(launch_tc(a, splits, true, s));
+            ++launches;
         } else {
             KNN_CUDA(launch_simt(corpus, nview, ldc * stride, cn_view, queries, Q, ldq, D, kp, c.qtile, split_len,
                                  splits, part, thr, s, redo));
@@ -1042,12 +1142,8 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         }
         return KNNS_OK;
     };
-    // in the exact form with the scan on, the shortlist path's selections run only for TF32 data
-    const uint32_t* old_gate = scan ? not_exact : nullptr;
-
-    // The shortlist path (TF32 keys in the exact form; gated on the device by the data's
-    // BF16-exactness when the scan is on).  In blocked mode it runs once every block
-    // has landed and been prepared.
+    // The shortlist path (corpora below the threshold scan's size, or the scan off): TF32 and
+    // BF16 variants, the one that does not match the data returning at once.
     auto old_path = [&]() -> int {
         if (!run_old) return KNNS_OK;
         if (pilot) {
@@ -1060,7 +1156,6 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
             ex.thr_out = thr_g;
             ex.thr_rank = rank;
             ex.qtile = c.qtile;
-            ex.skip_if_zero = old_gate;
             KNN_CUDA(launch_select(part, splits1, Q, kp1, std::min(kp1, (int)ns), corpus, ldc, queries, ldq, D, 0,
                                    nullptr, nullptr, nullptr, nullptr, s, ex));
             launches += 2;
@@ -1071,7 +1166,6 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         if (rc) return rc;
         SelectExtra ex;
         ex.qtile = c.qtile;
-        ex.skip_if_zero = old_gate;
         uint32_t* redo = (uint32_t*)E.redo.p;
         if (pilot) {
             KNN_CUDA(cudaMemsetAsync(redo, 0, qt * sizeof(uint32_t), s));
@@ -1090,14 +1184,13 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
             SelectExtra ex2;
             ex2.qtile = c.qtile;
             ex2.redo_in = redo;
-            ex2.skip_if_zero = old_gate;
             KNN_CUDA(launch_select(part, c.splits, Q, c.kp, k, corpus, ldc, queries, ldq, D, c.rerank,
                                    c.rerank ? nullptr : (const float*)E.qn.p, dist, idx, idx_f, s, ex2));
             ++launches;
         }
         return KNNS_OK;
     };
-    if (!blocked && (rc = old_path())) return rc;
+    if (run_old && (rc = old_path())) return rc;
 
     if (!scan) {
         for (int i = 2; i <= 5; ++i)
@@ -1191,10 +1284,14 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
             cnv += v.n_pad;
             if (csv) csv += v.n_pad;
         }
+        // (the TF32 scan's seeding reuses the sample norms and threshold buffers: the BF16
+        // levels, run or skipped, are done with them)
+        if (tf_scan && !blocked && (rc = ts.seed())) return rc;
         if ((rc = mark(2))) return rc;
         // main pass
         if (!blocked) {
             if ((rc = scan_pass(f8 ? f8_p : bf_p, N, 1, cn, cs_p, T, sp.S, sp.len, sp.cap))) return rc;
+            if (tf_scan && (rc = ts.main_pass())) return rc;
         } else {
             // block by block on the worker streams (blocks scanned on the two workers overlap each
             // other's tails), each once prepared and once the thresholds are seeded
@@ -1209,14 +1306,16 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
                 KNN_CUDA(cudaEventRecord(oev(2 + 2 * nblk + b), w));
             }
             for (int b = 0; b < nblk; ++b) KNN_CUDA(cudaStreamWaitEvent(s, oev(2 + 2 * nblk + b), 0));
-            // what needs the whole corpus: the TF32 copies and the shortlist path (gated on the
-            // data's BF16-exactness in the exact form)
-            if (!bf16_only) {
+            // what needs the whole corpus: the TF32 copies and the TF32 scan (gated on the data's
+            // BF16-exactness in the exact form)
+            if (tf_scan) {
                 KNN_CUDA(launch_split(corpus, N, ldc, D, c.dp, (float*)E.hi.p, (float*)E.lo.p, flags, any_lo,
                                       not_exact, s));
                 ++launches;
+                if ((rc = ts.split_queries())) return rc;
+                if ((rc = ts.seed())) return rc;
+                if ((rc = ts.main_pass())) return rc;
             }
-            if ((rc = old_path())) return rc;
         }
         if ((rc = mark(3))) return rc;
         KNN_CUDA(cudaMemsetAsync(fail_cnt, 0, sizeof(uint32_t), s));
@@ -1244,6 +1343,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         cs.fail_cnt = fail_cnt;
         KNN_CUDA(launch_select_cand(cs, s));
         ++launches;
+        if (tf_scan && (rc = ts.select())) return rc;
         if ((rc = mark(4))) return rc;
         // fix-up: failed queries, compacted, through the shortlist kernel without a threshold
         // (launches whose rows are all past the failure count return at once)
@@ -1300,12 +1400,15 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         };
         if ((rc = fix_pass(0, sp.fixA_rows, sp.fixA_S, sp.fixA_len))) return rc;
         if ((rc = fix_pass(sp.fixA_rows, sp.fixB_rows, sp.fixB_S, sp.fixB_len))) return rc;
+        if (tf_scan && (rc = ts.fix())) return rc;
         if ((rc = mark(5))) return rc;
     }
+    launches += ts.launches;
     if (!capture) KNN_CUDA(cudaEventRecord(E.last_done, s));
     if (st)
         *st = knns_stats{c.algo, c.splits, c.kp, c.stages, launches, (pilot || scan) ? 1 : 0, (int64_t)ws,
-                         scan ? 1 : 0, scan ? sp.S : 0, scan ? sp.cap : 0, scan ? 100 * sp.ring + sp.bps : 0};
+                         scan ? 1 : 0, scan ? sp.S : 0, scan ? sp.cap : 0, scan ? 100 * sp.ring + sp.bps : 0,
+                         (scan ? 1 : 0) | (tf_scan ? 2 : 0)};
     return KNNS_OK;
 }
 

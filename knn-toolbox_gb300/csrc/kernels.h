@@ -169,6 +169,7 @@ struct TscanArgs {
     int dp;                       // D rounded up to 32
     int split0;                   // first split of this launch
     int ring;                     // ring slots (tscan_ring())
+    const uint32_t* run_if;       // optional: the kernel returns at once when *run_if == 0
 };
 size_t tscan_smem_bytes(int ring);
 int tscan_ring();
@@ -221,7 +222,8 @@ struct CandSelect {
     int nseg = 0;
     int cap = 0;
     int64_t Q = 0;
-    const uint32_t* skip_if = nullptr;  // the kernel does nothing when *skip_if != 0
+    const uint32_t* skip_if = nullptr;       // the kernel does nothing when *skip_if != 0
+    const uint32_t* skip_if_zero = nullptr;  // the kernel does nothing when *skip_if_zero == 0
     float* thr_out = nullptr;
     int thr_rank = 0;
     const float* thr_fallback = nullptr;

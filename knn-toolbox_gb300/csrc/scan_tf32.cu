@@ -86,6 +86,8 @@ __device__ __forceinline__ bool t_wait(const TscanArgs& a, const TSmem& s, uint6
 __global__ void __launch_bounds__(kThreads, 1) tscan_kernel(const __grid_constant__ TscanArgs a)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
+    // device-side path choice: the kernel runs only when *run_if != 0
+    if (a.run_if != nullptr && *a.run_if == 0u) return;
     if ((ptx::smem_u32(sm) & 1023u) != 0u) {
         if (threadIdx.x == 0) atomicCAS(a.err, 0, kDevMisaligned);
         return;

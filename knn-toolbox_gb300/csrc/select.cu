@@ -251,6 +251,7 @@ __global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandS
 {
     extern __shared__ __align__(16) unsigned char smem[];
     if (c.skip_if != nullptr && *c.skip_if != 0u) return;
+    if (c.skip_if_zero != nullptr && *c.skip_if_zero == 0u) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const size_t wb = cand_warp_bytes(c.D, kThr, c.rerank != 0, c.buf_words, c.kp);
     const int buf_max = c.buf_words;

@@ -62,7 +62,7 @@ class Stats(ctypes.Structure):
     _fields_ = [("algo", ctypes.c_int), ("splits", ctypes.c_int), ("kp", ctypes.c_int),
                 ("stages", ctypes.c_int), ("launches", ctypes.c_int), ("pilot", ctypes.c_int),
                 ("workspace_bytes", ctypes.c_int64), ("scan", ctypes.c_int), ("scan_splits", ctypes.c_int),
-                ("scan_cap", ctypes.c_int), ("scan_ring", ctypes.c_int)]
+                ("scan_cap", ctypes.c_int), ("scan_ring", ctypes.c_int), ("scan_keys", ctypes.c_int)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -195,7 +195,7 @@ def last_stats() -> dict:
     _check(lib().knns_last_stats(ctypes.byref(s)))
     return {"algo": s.algo, "splits": s.splits, "kp": s.kp, "stages": s.stages, "launches": s.launches,
             "pilot": s.pilot, "workspace_bytes": s.workspace_bytes, "scan": s.scan, "scan_splits": s.scan_splits,
-            "scan_cap": s.scan_cap, "scan_ring": s.scan_ring}
+            "scan_cap": s.scan_cap, "scan_ring": s.scan_ring, "scan_keys": s.scan_keys}
 
 
 # --------------------------------------------------------------------------

@@ -264,8 +264,10 @@ def test_pilot_does_not_change_results(engine, oracle, algo, kind):
     else:
         X, Qs = S.int_descriptor(70000, 64, seed=4, nq=200)
     k = 24
-    d0, i0, st0 = run(engine, X, Qs, k, algo=algo, pilot=False)
-    d1, i1, st1 = run(engine, X, Qs, k, algo=algo, pilot=True)
+    # the pilot belongs to the shortlist kernels (without the threshold scan)
+    off = dict(algo=algo, scan=engine.SCAN_OFF)
+    d0, i0, st0 = run(engine, X, Qs, k, pilot=False, **off)
+    d1, i1, st1 = run(engine, X, Qs, k, pilot=True, **off)
     assert st0["pilot"] == 0 and st1["pilot"] == 1
     np.testing.assert_array_equal(i0, i1)
     np.testing.assert_array_equal(d0, d1)
@@ -284,12 +286,17 @@ def test_pilot_fixup_on_unrepresentative_sample(engine, oracle, algo):
     X = (10.0 + rng.random((N, D), dtype=np.float32)).astype(np.float32)
     near = np.arange(0, N, 16)
     X[near] = Qs[rng.integers(0, Q, near.size)] + 0.01 * rng.random((near.size, D), dtype=np.float32)
-    d, i, st = run(engine, X, Qs, k, algo=algo)
+    d, i, st = run(engine, X, Qs, k, algo=algo, scan=engine.SCAN_OFF)
     assert st["pilot"] == 1
     od, oi = oracle.knn_gemm(X, Qs, k, kp=st["kp"], rerank=True)
     oracle.check_parity(X, Qs, k, d, i, ref_idx=oi, gap_rel=GAP, dist_rel=DIST_REL, dist_abs=1e-6)
-    d0, i0, _ = run(engine, X, Qs, k, algo=algo, pilot=False)
+    d0, i0, _ = run(engine, X, Qs, k, algo=algo, pilot=False, scan=engine.SCAN_OFF)
     np.testing.assert_array_equal(i, i0)
+    # the TF32 threshold scan (the default at this size) on the same unrepresentative sample
+    if algo == engine.ALGO_TC:
+        d2, i2, st2 = run(engine, X, Qs, k)
+        assert st2["scan"] == 1
+        np.testing.assert_array_equal(i2, i0)
 
 
 # ---------------------------------------------------------------- precision form: BF16 shortlist + exact re-rank
@@ -319,16 +326,19 @@ def test_bf16_shortlist_on_bf16_exact_data_is_exact(engine, oracle):
 
 
 # ---------------------------------------------------------------- 3xTF32 keys on request
-@pytest.mark.parametrize("N", [20000, 150000])
-def test_tf32_only_gives_the_same_answers(engine, oracle, N):
-    # integer data are exact in BF16: by default the BF16 kernels (the threshold scan at
-    # N >= 131072) rank them; tf32_only sends them through the 3xTF32 kernel instead,
-    # whose keys are exact on this data as well -- same answers, bit for bit
+@pytest.mark.parametrize("N,scan", [(20000, 2), (150000, 0), (150000, 1)])
+def test_tf32_only_gives_the_same_answers(engine, oracle, N, scan):
+    # integer data are exact in BF16: by default the BF16 kernels (the shortlist kernel's BF16
+    # variant without the scan, the BF16 threshold scan at N >= 131072) rank them; tf32_only
+    # sends them through the 3xTF32 kernels instead (the shortlist kernel's TF32 variant, the
+    # TF32 threshold scan run beside the BF16 one), whose keys are exact on this data as
+    # well -- same answers, bit for bit
     import cuknns.synth as S
     X, Qs = S.int_descriptor(N, 128, seed=12, nq=257)
     k = 100
-    d0, i0, st0 = run(engine, X, Qs, k)
-    d1, i1, st1 = run(engine, X, Qs, k, tf32_only=True)
+    d0, i0, st0 = run(engine, X, Qs, k, scan=scan)
+    d1, i1, st1 = run(engine, X, Qs, k, tf32_only=True, scan=scan)
+    assert st0["scan"] == st1["scan"] == (scan != 2)
     np.testing.assert_array_equal(i0, i1)
     np.testing.assert_array_equal(d0, d1)
     od, oi = oracle.knn_gemm(X, Qs, k, kp=st1["kp"], rerank=True)

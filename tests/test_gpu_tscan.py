@@ -105,3 +105,47 @@ def test_dropin_and_index_on_wide_rows(engine, oracle):
     np.testing.assert_array_equal(i.cpu().numpy(), idxf.astype(np.int32))
     np.testing.assert_array_equal(d.cpu().numpy(), vals)
     ix.close()
+
+
+@pytest.mark.parametrize("N,D,k", [(150_000, 128, 100), (140_003, 96, 10)])
+def test_fp32_data_beside_the_bf16_scan(engine, oracle, N, D, k):
+    # Large corpora of FP32 data in the exact form: the BF16 threshold scan and the 3xTF32 one
+    # are both launched and the data's BF16-exactness, found on the device, lets only the TF32
+    # scan run.  Its answers are those of the TF32 scan alone (same plan, bit for bit), in the
+    # blocked and the single-stream schedules, and of the shortlist kernel up to ties.
+    rng = np.random.default_rng(N + D)
+    X = rng.random((N, D), dtype=np.float32)
+    Qs = rng.random((300, D), dtype=np.float32)
+    d, i, st = run(engine, X, Qs, k)
+    assert st["scan"] == 1 and st["scan_keys"] == 3
+    d1, i1, _ = run(engine, X, Qs, k, single_stream=True)
+    np.testing.assert_array_equal(i1, i)
+    np.testing.assert_array_equal(d1, d)
+    d2, i2, st2 = run(engine, X, Qs, k, scan=engine.SCAN_TF32)
+    assert st2["scan_keys"] == 2
+    np.testing.assert_array_equal(i2, i)
+    np.testing.assert_array_equal(d2, d)
+    d3, i3, _ = run(engine, X, Qs, k, scan=engine.SCAN_OFF)
+    assert (i3 == i).mean() > 0.999
+    sub = np.arange(0, 300, 3)
+    od, oi = oracle.knn_gemm(X, Qs[sub], k, kp=st["kp"], rerank=True)
+    oracle.check_parity(X, Qs[sub], k, d[sub], i[sub], ref_idx=oi, gap_rel=GAP, dist_rel=DIST_REL)
+
+
+def test_small_corpus_fp32_and_integer_data_on_the_tf32_scan(engine, oracle):
+    # Below the BF16 scan's default size (16,384 <= N < 131,072) the exact form runs the TF32
+    # scan for data of every kind: parity on FP32 data, bit-exact on integer data.
+    import cuknns.synth as S
+    X, Qs = S.uniform(65536, 128, seed=0, nq=1024)
+    d, i, st = run(engine, X, Qs, 16)
+    assert st["scan_keys"] == 2
+    od, oi = oracle.knn_gemm(X, Qs[:256], 16, kp=st["kp"], rerank=True)
+    oracle.check_parity(X, Qs[:256], 16, d[:256], i[:256], ref_idx=oi, gap_rel=GAP, dist_rel=DIST_REL)
+    rng = np.random.default_rng(5)
+    Xi = rng.integers(0, 200, (70000, 64)).astype(np.float32)
+    Qi = rng.integers(0, 200, (129, 64)).astype(np.float32)
+    d, i, st = run(engine, Xi, Qi, 24)
+    assert st["scan_keys"] == 2
+    od, oi = oracle.knn_gemm(Xi, Qi, 24, kp=st["kp"], rerank=True)
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_array_equal(d, od)
