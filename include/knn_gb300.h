@@ -82,10 +82,11 @@ typedef struct knns_options {
                         the kernels slower -- a measurement switch for comparing the two key types */
     int scan_accs;   /* threshold scan: tensor-memory accumulators, 2 (tiles of 224 corpus rows; 192
                         above 128 BF16 columns) or 4 (tiles of 96); 0 = automatic */
-    int single_stream; /* 1: every kernel of the search on the caller's stream, one after another;
-                        0 (default): the threshold scan prepares the corpus in blocks on a second stream
-                        while the seeding passes run, and scans each block as soon as it is ready, on
-                        two more streams (a host corpus is also copied in those blocks).  Same results */
+    int single_stream; /* host-buffer searches on the threshold scan: 1: copy the corpus, then search it
+                        on one stream; 0 (default): copy the corpus in blocks on a second stream,
+                        prepare each block as it lands on a third while the seeding passes run, and
+                        scan each block as soon as it is ready, on two more.  Same results.  Searches
+                        of a resident corpus always run on the caller's stream alone */
 } knns_options;
 
 typedef struct knns_stats {

@@ -333,9 +333,11 @@ constexpr int kMaxSeedLevels = 6;
 // shortlists take a finer stride, so that a query's main-pass candidates
 // (mean + six standard deviations) still fit the selection's buffer.
 constexpr int64_t kSeedStride = 32;
-// Stride ratio of neighbouring levels: 32 leaves two levels for a million rows (every 32nd row,
-// and every 1024th, whose keys are all kept), where 16 needs three.
-constexpr int64_t kSeedRatio = 32;
+// Stride ratio of neighbouring levels.  32 would leave two levels for a million rows where 16
+// needs three, but its coarser thresholds cost more than the level they save: seeding 0.46
+// against 0.37 ms on the 1M x 128 integer workload, and on the 4M x 96 mixture (BF16 keys) a
+// main pass of 7.7 against 6.8 ms with 0.85 against 0.03 ms of fix-up.
+constexpr int64_t kSeedRatio = 16;
 
 static int64_t seed_stride(int kp)
 {
@@ -927,26 +929,25 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         if ((rc = ts.ensure())) return rc;
         ws += E.qhi.cap + E.qlo.cap + E.qlof.cap + E.tfail.cap;
     }
-    // Blocked mode (threshold scan on a corpus not prepared in advance, not under capture): the
+    // Blocked mode (threshold scan on a corpus still in host memory, not under capture): the
     // seeding sample (every sp.stride0-th row, the rows the seeding levels read) is prepared first
-    // and the seeding passes run while the corpus is prepared block by block (blocks of whole
-    // main-scan splits) on the engine's preparation stream; each block is scanned, on one of two
-    // worker streams, once it is prepared and the thresholds are seeded.  A corpus still in host
-    // memory is copied in the same blocks on the copy stream, each block prepared as it lands.
-    // Without the scan a host corpus is copied whole before the search starts.
-    const bool blocked = scan && !pc && !capture && !o.single_stream;
-    const bool streamed = blocked && host_corpus != nullptr;
+    // and the seeding passes run while the corpus is copied in blocks (of whole main-scan splits)
+    // on the copy stream and prepared block by block, as each lands, on the engine's preparation
+    // stream; each block is scanned, on one of two worker streams, once it is prepared and the
+    // thresholds are seeded.  A resident corpus is searched on the search's stream alone: there
+    // the blocks' partial waves and the preparation beside the scans cost more than the overlap
+    // gives (4M x 96 mixture, BF16 keys: 10.8 against 8.3 ms).  Without the scan a host corpus
+    // is copied whole before the search starts.
+    const bool blocked = scan && !pc && !capture && !o.single_stream && host_corpus != nullptr;
+    const bool streamed = blocked;
     const int64_t smp_n = blocked ? cdiv(N, sp.stride0) : 0;
     const int64_t smp_pad = cdiv(smp_n, kScanTileN) * kScanTileN + kScanTileN;
-    // where the sample rows are read: the device corpus in place; page-locked host memory in place
-    // (it is mapped into the device's address space); otherwise a device copy gathered by a 2-D copy
+    // where the sample rows are read: page-locked host memory in place (it is mapped into the
+    // device's address space); otherwise a device copy gathered by a 2-D copy
     const float* smp_src = nullptr;
     int64_t smp_ld = 0;
     bool smp_copy = false;
-    if (blocked && !streamed) {
-        smp_src = corpus;
-        smp_ld = sp.stride0 * ldc;
-    } else if (streamed) {
+    if (streamed) {
         cudaPointerAttributes pa;
         if (cudaPointerGetAttributes(&pa, host_corpus) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
             pa.devicePointer != nullptr) {

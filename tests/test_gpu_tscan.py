@@ -111,14 +111,16 @@ def test_dropin_and_index_on_wide_rows(engine, oracle):
 def test_fp32_data_beside_the_bf16_scan(engine, oracle, N, D, k):
     # Large corpora of FP32 data in the exact form: the BF16 threshold scan and the 3xTF32 one
     # are both launched and the data's BF16-exactness, found on the device, lets only the TF32
-    # scan run.  Its answers are those of the TF32 scan alone (same plan, bit for bit), in the
-    # blocked and the single-stream schedules, and of the shortlist kernel up to ties.
+    # scan run.  Its answers are those of the TF32 scan alone (same plan, bit for bit), of a
+    # host-buffer search (the corpus copied, prepared and scanned in blocks), and of the shortlist
+    # kernel up to ties.
     rng = np.random.default_rng(N + D)
     X = rng.random((N, D), dtype=np.float32)
     Qs = rng.random((300, D), dtype=np.float32)
     d, i, st = run(engine, X, Qs, k)
     assert st["scan"] == 1 and st["scan_keys"] == 3
-    d1, i1, _ = run(engine, X, Qs, k, single_stream=True)
+    d1, i1 = engine.search_host(X, Qs, k)
+    assert engine.last_stats()["scan_keys"] == 3
     np.testing.assert_array_equal(i1, i)
     np.testing.assert_array_equal(d1, d)
     d2, i2, st2 = run(engine, X, Qs, k, scan=engine.SCAN_TF32)
