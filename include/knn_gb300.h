@@ -304,10 +304,11 @@ int knns_debug_tc_dot_tile(const float *corpus, int64_t N, const float *queries,
  * sum of squares in column order), bf16[n][round64(D)] (BF16 copy, zero
  * padded), f8[n][round128(D)] (E4M3 codes) with scales[n] (per-row absmax /
  * 448), words[3] ([0] not BF16-exact, [1] some value not an integer, [2] max
- * |x| as float bits).  D <= 384.  Synchronous.
+ * |x| as float bits), norm_parts[n][16] (optional: the norm as BF16 parts n1 + n2 + n3,
+ * then zeros, the BF16 scan's norm operand).  D <= 384.  Synchronous.
  */
 int knns_debug_prep(const float *x, int64_t n, int64_t ld, int D, float *norms, void *bf16, void *f8,
-                    float *scales, uint32_t *words);
+                    float *scales, uint32_t *words, void *norm_parts);
 
 #ifdef __cplusplus
 }

@@ -171,6 +171,24 @@ static int encode_rows_bf16(CUtensorMap* m, const void* base, int64_t rows, int6
     return KNNS_OK;
 }
 
+// Norm parts [rows][kNormParts] BF16 (rows `pitch` elements apart), box {kNormParts, box_rows},
+// 32B swizzle (one 32-byte row per corpus row, the BF16 scan's last K step)
+static int encode_np(CUtensorMap* m, const void* base, int64_t rows, int64_t pitch, int box_rows)
+{
+    EncodeTiledFn fn;
+    int rc = get_encode_fn(&fn);
+    if (rc) return rc;
+    cuuint64_t dims[2] = {(cuuint64_t)kNormParts, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)pitch * 2};
+    cuuint32_t box[2] = {(cuuint32_t)kNormParts, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(KNNS_ERR_CUDA, "cuTensorMapEncodeTiled (norm parts) failed (%d)", (int)r);
+    return KNNS_OK;
+}
+
 // ---------------------------------------------------------------- planning
 // smallest corpus the threshold scan runs on when asked to (KNNS_SCAN_ON, long shortlists)
 constexpr int64_t kScanMinRowsForced = 16384;
@@ -890,6 +908,12 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
             if (rc) return rc;
             ws += E.f8.cap + E.cs.cap;
         }
+        if (scan && !f8) {
+            // BF16 keys: the norms as BF16 parts, added inside the scan's MMA
+            rc = E.np.ensure((size_t)N * kNormParts * 2);
+            if (rc) return rc;
+            ws += E.np.cap;
+        }
     }
     if (f8) {
         rc = E.qs.ensure(Q * sizeof(float));
@@ -903,6 +927,9 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     const float* lo_p = (const float*)(pc ? pc->lo.p : E.lo.p);
     const void* f8_p = pc ? pc->f8.p : E.f8.p;
     const float* cs_p = (const float*)(pc ? pc->cs.p : E.cs.p);
+    // BF16 keys on the scan: the corpus norm parts (the scan's last K step)
+    const bool np_keys = scan && !f8;
+    const void* np_p = pc ? pc->np.p : E.np.p;
     // the scan's operand row width in 16-bit units
     const int sdp = f8 ? c.dpf : c.dpb;
     if (scan) {
@@ -965,6 +992,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         if (!rc) rc = E.smp_bf.ensure((size_t)smp_n * c.dpb * 2);
         if (!rc && f8) rc = E.smp_f8.ensure((size_t)smp_n * c.dpf * 2);
         if (!rc && f8) rc = E.smp_cs.ensure((size_t)smp_pad * sizeof(float));
+        if (!rc && np_keys) rc = E.smp_np.ensure((size_t)smp_n * kNormParts * 2);
         if (rc) return rc;
         if (smp_copy) smp_src = (const float*)E.smp.p;
     }
@@ -1053,7 +1081,8 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
             KNN_CUDA(launch_prep_rows(corpus + r0 * ld, r1 - r0, ld, D, c.dpb, (char*)E.bf.p + (size_t)r0 * c.dpb * 2,
                                       cn + r0, b == nblk - 1 ? n_pad - r0 : r1 - r0, not_exact, ps, int_stats,
                                       f8 ? (char*)E.f8.p + (size_t)r0 * c.dpf * 2 : nullptr, 2 * c.dpf,
-                                      f8 ? (float*)E.cs.p + r0 : nullptr));
+                                      f8 ? (float*)E.cs.p + r0 : nullptr,
+                                      np_keys ? (char*)E.np.p + (size_t)r0 * kNormParts * 2 : nullptr));
             ++launches;
             KNN_CUDA(cudaEventRecord(oev(2 + nblk + b), ps));
         }
@@ -1063,7 +1092,8 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         // corpus block by block, above)
         if (!pc && !blocked) {
             KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, c.dpb, E.bf.p, cn, n_pad, not_exact, s, int_stats,
-                                      f8 ? E.f8.p : nullptr, 2 * c.dpf, f8 ? (float*)E.cs.p : nullptr));
+                                      f8 ? E.f8.p : nullptr, 2 * c.dpf, f8 ? (float*)E.cs.p : nullptr,
+                                      np_keys ? E.np.p : nullptr));
             ++launches;
         }
         if (f8)
@@ -1220,11 +1250,12 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         a.qs = f8 ? (const float*)E.qs.p : nullptr;
         // one scan over rows 0, stride, 2*stride, ... (nview of them) of the operand copy at src;
         // grid rows are the splits split0 .. split0 + splits - 1, launched on stream ls
-        auto scan_pass = [&](const void* src, int64_t nview, int64_t stride, const float* cn_view,
+        auto scan_pass = [&](const void* src, const void* np_src, int64_t nview, int64_t stride, const float* cn_view,
                              const float* cs_view, const float* thr, int splits, int64_t split_len, int cap,
                              int split0 = 0, cudaStream_t ls = nullptr) -> int {
             // the map moves bytes: E4M3 rows are described as rows of 16-bit units
             int r = encode_rows_bf16(&a.tm_c, src, nview, sdp, stride * sdp, scan_box_rows(sdp, sp.accs));
+            if (!r && np_keys) r = encode_np(&a.tm_np, np_src, nview, stride * kNormParts, scan_box_rows(sdp, sp.accs));
             if (r) return r;
             a.cn = cn_view;
             a.cs = cs_view;
@@ -1250,16 +1281,18 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         const void* key_src = f8 ? f8_p : bf_p;
         const float* lv_cn = cn;
         const float* lv_cs = cs_p;
+        const void* lv_np = np_p;
         int64_t lv_div = 1;
         if (blocked) {
             if (smp_copy) KNN_CUDA(cudaStreamWaitEvent(s, oev(1), 0));
             KNN_CUDA(launch_prep_rows(smp_src, smp_n, smp_ld, D, c.dpb, E.smp_bf.p, (float*)E.smp_cn.p, smp_pad,
                                       not_exact, s, int_stats, f8 ? E.smp_f8.p : nullptr, 2 * c.dpf,
-                                      f8 ? (float*)E.smp_cs.p : nullptr));
+                                      f8 ? (float*)E.smp_cs.p : nullptr, np_keys ? E.smp_np.p : nullptr));
             ++launches;
             key_src = f8 ? E.smp_f8.p : E.smp_bf.p;
             lv_cn = (const float*)E.smp_cn.p;
             lv_cs = (const float*)E.smp_cs.p;
+            lv_np = E.smp_np.p;
             lv_div = sp.stride0;
         }
         float* cnv = (float*)E.cnv.p;
@@ -1267,20 +1300,21 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         const float* T = nullptr;
         for (int l = 0; l < sp.levels; ++l) {
             const ScanLevel& v = sp.lv[l];
-            KNN_CUDA(launch_gather_norms(lv_cn, v.n, v.stride / lv_div, cnv, v.n_pad, s));
             if (f8) {
-                // scales of the sample rows, 0 for padding (whose +inf norms keep their keys at +inf)
+                // norms and scales of the sample rows: 0 scales for padding, whose +inf norms keep
+                // their keys at +inf (BF16 keys take the norm parts in place)
+                KNN_CUDA(launch_gather_norms(lv_cn, v.n, v.stride / lv_div, cnv, v.n_pad, s));
                 KNN_CUDA(launch_gather_norms(lv_cs, v.n, v.stride / lv_div, csv, v.n_pad, s, 0.f));
-                ++launches;
+                launches += 2;
             }
-            if ((rc = scan_pass(key_src, v.n, v.stride / lv_div, cnv, csv, T, v.S, v.len, v.cap))) return rc;
+            if ((rc = scan_pass(key_src, lv_np, v.n, v.stride / lv_div, cnv, csv, T, v.S, v.len, v.cap))) return rc;
             cs.nseg = kScanParts * v.S;
             cs.cap = v.cap;
             cs.thr_out = Tbuf[l & 1];
             cs.thr_rank = v.j;
             cs.thr_fallback = T;  // a level that fails keeps the previous threshold
             KNN_CUDA(launch_select_cand(cs, s));
-            launches += 3;
+            ++launches;
             T = Tbuf[l & 1];
             cnv += v.n_pad;
             if (csv) csv += v.n_pad;
@@ -1291,7 +1325,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         if ((rc = mark(2))) return rc;
         // main pass
         if (!blocked) {
-            if ((rc = scan_pass(f8 ? f8_p : bf_p, N, 1, cn, cs_p, T, sp.S, sp.len, sp.cap))) return rc;
+            if ((rc = scan_pass(f8 ? f8_p : bf_p, np_p, N, 1, cn, cs_p, T, sp.S, sp.len, sp.cap))) return rc;
             if (tf_scan && (rc = ts.main_pass())) return rc;
         } else {
             // block by block on the worker streams (blocks scanned on the two workers overlap each
@@ -1302,7 +1336,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
                 KNN_CUDA(cudaStreamWaitEvent(w, oev(2 + nblk + b), 0));
                 KNN_CUDA(cudaStreamWaitEvent(w, oev(3 + 3 * nblk), 0));
                 const int sb = std::min(blk_splits, sp.S - b * blk_splits);
-                if ((rc = scan_pass(f8 ? f8_p : bf_p, N, 1, cn, cs_p, T, sb, sp.len, sp.cap, b * blk_splits, w)))
+                if ((rc = scan_pass(f8 ? f8_p : bf_p, np_p, N, 1, cn, cs_p, T, sb, sp.len, sp.cap, b * blk_splits, w)))
                     return rc;
                 KNN_CUDA(cudaEventRecord(oev(2 + 2 * nblk + b), w));
             }
@@ -1423,6 +1457,7 @@ void PreparedCorpus::release()
     words.release();
     f8.release();
     cs.release();
+    np.release();
 }
 
 int prepare_corpus(Engine& E, PreparedCorpus* pc, const float* corpus, int64_t N, int64_t ldc, int D, bool tf32,
@@ -1443,11 +1478,12 @@ int prepare_corpus(Engine& E, PreparedCorpus* pc, const float* corpus, int64_t N
     const int dpf = ((D + 127) & ~127) / 2;
     if (!rc && fp8) rc = pc->f8.ensure((size_t)N * dpf * 2);
     if (!rc && fp8) rc = pc->cs.ensure(n_pad * sizeof(float));
+    if (!rc) rc = pc->np.ensure((size_t)N * kNormParts * 2);
     if (rc) return rc;
     uint32_t* w = (uint32_t*)pc->words.p;
     KNN_CUDA(cudaMemsetAsync(w, 0, 8 * sizeof(uint32_t), s));
     KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, dpb, pc->bf.p, (float*)pc->cn.p, n_pad, w + 1, s, w + 2,
-                              fp8 ? pc->f8.p : nullptr, 2 * dpf, fp8 ? (float*)pc->cs.p : nullptr));
+                              fp8 ? pc->f8.p : nullptr, 2 * dpf, fp8 ? (float*)pc->cs.p : nullptr, pc->np.p));
     if (tf32)
         KNN_CUDA(launch_split(corpus, N, ldc, D, dp, (float*)pc->hi.p, (float*)pc->lo.p, (uint32_t*)pc->tiles.p, w,
                               nullptr, s));
@@ -1941,7 +1977,7 @@ void knns_index_destroy(knns_index* ix)
 }
 
 int knns_debug_prep(const float* x, int64_t n, int64_t ld, int D, float* norms, void* bf16, void* f8, float* scales,
-                    uint32_t* words)
+                    uint32_t* words, void* norm_parts)
 {
     clear_error();
     if (!x || !norms || !bf16 || !f8 || !scales || !words || n <= 0 || D <= 0 || D > kPrepMaxD || ld < D)
@@ -1953,7 +1989,7 @@ int knns_debug_prep(const float* x, int64_t n, int64_t ld, int D, float* norms, 
     cudaStream_t s = E->host_stream();
     KNN_CUDA(cudaMemsetAsync(words, 0, 3 * sizeof(uint32_t), s));
     KNN_CUDA(launch_prep_rows(x, n, ld, D, (D + 63) & ~63, bf16, norms, n, words, s, words + 1, f8, (D + 127) & ~127,
-                              scales));
+                              scales, norm_parts));
     KNN_CUDA(cudaStreamSynchronize(s));
     return KNNS_OK;
 }

@@ -47,9 +47,12 @@ constexpr int kPrepMaxD = 384;
 // integer, [1] = max |x| as float bits.
 // f8 / scales (optional): E4M3 copy [n][f8_bytes] (f8_bytes a multiple of 128, zero padded) with
 // per-row absmax scales (row = scale * codes; scales[n..n_pad) = 0); needs D <= kPrepMaxD.
+// np (optional): norm parts [n][kNormParts] BF16, (n1, n2, n3, 0, ...) with n1 + n2 + n3 equal
+// to the row's FP32 norm; needs D <= kPrepMaxD.
+constexpr int kNormParts = 16;
 cudaError_t launch_prep_rows(const float* x, int64_t n, int64_t ld, int D, int dpb, void* out, float* norms,
                              int64_t n_pad, uint32_t* not_exact, cudaStream_t s, uint32_t* int_stats = nullptr,
-                             void* f8 = nullptr, int f8_bytes = 0, float* scales = nullptr);
+                             void* f8 = nullptr, int f8_bytes = 0, float* scales = nullptr, void* np = nullptr);
 
 // CUDA-core FP32 fused distance + shortlist.  qpb in {32, 128}.
 size_t simt_smem_bytes(int qpb, int kp);
@@ -115,8 +118,10 @@ constexpr size_t kScanSmemLimit = 232448;
 // so both key types share one tile geometry per 128-byte K box.
 struct ScanArgs {
     CUtensorMap tm_c;          // corpus [N][dpb] 16-bit units (view), box {64, scan_box_rows(dpb)}, 128B swizzle
+    CUtensorMap tm_np;         // BF16 keys: norm parts of the view [N][kNormParts] BF16, box {16, tile rows},
+                               // 32B swizzle (E4M3 keys: unused)
     const void* qbf;           // queries [Q][dpb] 16-bit units (BF16, or E4M3 bytes)
-    const float* cn;           // [>= N + scan_tile_rows(dpb)] corpus norms of the view, +inf padding
+    const float* cn;           // fp8: [>= N + scan_tile_rows(dpb)] corpus norms of the view, +inf padding
     const float* cs;           // fp8: corpus row scales of the view (same padding, 0 there)
     const float* qs;           // fp8: query row scales [Q]
     const float* thr;          // [Q] thresholds (null: +inf, every key collected)

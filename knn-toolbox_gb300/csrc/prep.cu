@@ -138,6 +138,7 @@ struct PrepArgs {
     uint32_t* int_stats;
     uint8_t* f8;
     float* scales;
+    __nv_bfloat16* np;  // optional: norm parts, kNormParts BF16 per row
 };
 
 // s + t = a + b exactly (Knuth's TwoSum; no contraction: explicit roundings)
@@ -238,6 +239,34 @@ __device__ __forceinline__ float pick_row(const float (&v)[kU], int g)
     return x;
 }
 
+// The norm f as three BF16 parts, then zeros: one 32-byte row of the operand that adds ||c||^2
+// inside the BF16 scan's MMA.  n1 + n2 + n3 == f exactly for f = 0 and f >= 2^-100 (each
+// remainder is exact by Sterbenz's lemma, a multiple of f's FP32 ulp, and the last one holds at
+// most 8 significant bits, all within BF16's normal range); smaller norms are kept to within
+// 2^-133, BF16's subnormal spacing.  Norms that are not finite in BF16 (past 3.39e38) keep n1
+// alone (+inf).
+__device__ __forceinline__ void store_norm_parts(__nv_bfloat16* dst, float f)
+{
+    const __nv_bfloat16 n1 = __float2bfloat16_rn(f);
+    __nv_bfloat16 n2 = __float2bfloat16_rn(0.f), n3 = n2;
+    if (isfinite(__bfloat162float(n1))) {
+        const float r1 = __fsub_rn(f, __bfloat162float(n1));
+        n2 = __float2bfloat16_rn(r1);
+        n3 = __float2bfloat16_rn(__fsub_rn(r1, __bfloat162float(n2)));
+    }
+    uint4 w0;
+    w0.x = (uint32_t)__bfloat16_as_ushort(n1) | ((uint32_t)__bfloat16_as_ushort(n2) << 16);
+    w0.y = (uint32_t)__bfloat16_as_ushort(n3);
+    w0.z = 0u;
+    w0.w = 0u;
+    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+    uint4* d = reinterpret_cast<uint4*>(dst);
+    d[0] = w0;
+    d[1] = z;
+    d[2] = z;
+    d[3] = z;
+}
+
 template <int kChunks, int kU>
 __global__ void __launch_bounds__(256) prep_rows_kernel(const PrepArgs p)
 {
@@ -331,7 +360,7 @@ __global__ void __launch_bounds__(256) prep_rows_kernel(const PrepArgs p)
                 if (lane == 0) p.scales[r] = mx / 448.f;
             }
         }
-        if (p.norms != nullptr) {
+        if (p.norms != nullptr || p.np != nullptr) {
             // the kU rows' norms together: lane l settles row g = l / (32 / kU) of the batch
             constexpr int kGroup = 32 / kU;
             const int g = lane / kGroup;
@@ -395,7 +424,8 @@ __global__ void __launch_bounds__(256) prep_rows_kernel(const PrepArgs p)
                     }
                     f = __double2float_rn(acc);
                 }
-                p.norms[r] = f;
+                if (p.norms) p.norms[r] = f;
+                if (p.np) store_norm_parts(p.np + r * kNormParts, f);
             }
         }
     }
@@ -415,7 +445,7 @@ __global__ void __launch_bounds__(256) prep_rows_kernel(const PrepArgs p)
 
 cudaError_t launch_prep_rows(const float* x, int64_t n, int64_t ld, int D, int dpb, void* out, float* norms,
                              int64_t n_pad, uint32_t* not_exact, cudaStream_t s, uint32_t* int_stats, void* f8,
-                             int f8_bytes, float* scales)
+                             int f8_bytes, float* scales, void* np)
 {
     const int64_t rows = std::max(n, (norms || scales) ? n_pad : n);
     if (rows <= 0) return cudaSuccess;
@@ -425,6 +455,7 @@ cudaError_t launch_prep_rows(const float* x, int64_t n, int64_t ld, int D, int d
     const int span = (D + 127) / 128 * 128;
     if (out != nullptr && (dpb % 64 != 0 || dpb < D || (D <= kPrepMaxD && dpb > span))) return cudaErrorInvalidValue;
     if (f8 != nullptr && f8_bytes > span) return cudaErrorInvalidValue;
+    if (np != nullptr && D > kPrepMaxD) return cudaErrorInvalidValue;
     if (D > kPrepMaxD) {
         // wide rows: separate passes
         cudaError_t e = cudaSuccess;
@@ -448,6 +479,7 @@ cudaError_t launch_prep_rows(const float* x, int64_t n, int64_t ld, int D, int d
     a.int_stats = int_stats;
     a.f8 = static_cast<uint8_t*>(f8);
     a.scales = scales;
+    a.np = static_cast<__nv_bfloat16*>(np);
     auto blocks = [&](int ku) {
         const int64_t b = (rows + 8 * ku - 1) / (8 * ku);
         return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, 16384));

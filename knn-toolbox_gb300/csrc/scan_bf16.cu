@@ -9,8 +9,11 @@
 // corpus by the engine) and every key strictly below T is appended to the
 // query's candidate segment in global memory.  The final top-kp is chosen
 // from the segments by select_cand_kernel.  Keys are the reference's ranking
-// key ||c||^2 - 2 q.c (demo/knn.m:5), q.c from BF16 operands with FP32
-// accumulation (exact products), the norm added with one FP32 fma.
+// key ||c||^2 - 2 q.c (demo/knn.m:5), formed whole by the tensor core: A = -2 q
+// (exact in BF16) against the corpus rows, then an all-ones A block against the
+// rows' norms split into three BF16 parts (n1 + n2 + n3 = ||c||^2 exactly), one
+// more K step of 16; products are exact and accumulate in FP32, so on integer
+// data every key is exact.  The epilogue only compares.
 // The E4M3 variant (kF8) takes both operands as FP8 E4M3 codes with per-row
 // absmax scales (x = s_x * codes): kind::f8f6f4 MMAs accumulate the code
 // products in FP32 and the epilogue forms ||c||^2 + (-2 s_q) * (s_c * acc),
@@ -21,12 +24,15 @@
 // for up to 128 BF16 columns, 192 for up to 256.  Tensor memory holds two
 // TN-column FP32 accumulators and the A operand (this CTA's queries) in the
 // remaining dpb/2 columns, so shared memory carries only the corpus tiles
-// (a ring of whole tiles where three fit) and their norms.  Every CTA loads
+// (a ring of whole tiles where three fit) with their norm parts (32 bytes per
+// row, 32-byte swizzle) and the 4 KB ones block (E4M3 keys: a ring of norms
+// and scales instead).  Every CTA loads
 // its own corpus tiles (CTAs of neighbouring query tiles read the same tiles
 // from L2 at about the same time).
 // Warp roles (608 threads):
 //   warp 0      producer: per tile the corpus K-boxes (2-D TMA, 64 bf16 x TN
-//               rows, 128-byte swizzle) and the corpus norms (1-D bulk copy);
+//               rows, 128-byte swizzle) and the norm parts with the tile's last
+//               slot (E4M3 keys: norms and scales by 1-D bulk copies);
 //   warp 1      TMEM owner (512 columns) and MMA issuer of the even tiles
 //               (tcgen05.mma kind::f16 / kind::f8f6f4, A from TMEM, B from
 //               shared memory) into accumulator 0;
@@ -40,9 +46,10 @@
 //               tail (16 + 8 columns for TN = 224, 16 for 192): all three
 //               tcgen05.ld in flight at once, one wait, the accumulator released
 //               (its round trip to the issuers is what the pipeline waits on),
-//               then per chunk packed fma in place, the minima of its 8-column
-//               groups, one vote; only groups holding a key below some lane's
-//               threshold are appended.
+//               then per chunk the minima of its 8-column groups (E4M3 keys:
+//               formed first by packed multiply and fma), one vote; only groups
+//               holding a key below some lane's threshold are appended.  The
+//               view's last tile masks its columns past the view (+inf).
 // Every mbarrier wait is bounded; on timeout the kernel records an error code
 // in the device error word and winds down without hanging the GPU.
 #include <algorithm>
@@ -68,10 +75,16 @@ constexpr uint32_t kTmemCols = 512;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 
 __host__ __device__ constexpr uint32_t box_bytes(int tn) { return (uint32_t)tn * 128u; }  // 64 bf16 x tn rows
-// norm ring: kNormSlots tiles of norms, then (E4M3 keys) as many tiles of corpus scales
-__host__ __device__ constexpr uint32_t norm_bytes(int tn, bool f8 = false)
+// E4M3 keys: norm ring of kNormSlots tiles of norms, then as many tiles of corpus scales
+__host__ __device__ constexpr uint32_t norm_bytes(int tn) { return (uint32_t)kNormSlots * tn * 8u; }
+// BF16 keys: per ring slot the tile's norm parts (32 bytes per corpus row), and one block of
+// 128 x 16 BF16 ones, the A operand that adds them to the keys
+__host__ __device__ constexpr uint32_t np_bytes(int tn) { return (uint32_t)tn * 32u; }
+constexpr uint32_t kOnesBytes = 128u * 32u;
+// shared memory beside the ring
+__host__ __device__ constexpr uint32_t side_bytes(int tn, bool f8, int ring)
 {
-    return (uint32_t)kNormSlots * tn * 4u * (f8 ? 2u : 1u);
+    return f8 ? norm_bytes(tn) : (uint32_t)ring * np_bytes(tn) + kOnesBytes;
 }
 
 struct ScanSmem {
@@ -120,6 +133,10 @@ __global__ void __launch_bounds__(kScanThreads, 1)
     constexpr uint32_t kBoxB = box_bytes(TN);
     constexpr uint32_t kIdesc = kF8 ? ptx::idesc_e4m3(kTileQ, TN) : ptx::idesc_bf16(kTileQ, TN);
     constexpr uint32_t kACol = (uint32_t)kNacc * TN;  // A operand columns [kACol, kACol + dpb/2)
+    // BF16 keys come out of the MMA whole: A = -2 q in TMEM against the corpus rows, then the
+    // ones block against the rows' norm parts, key = ||c||^2 - 2 q.c (E4M3 keys: the epilogue
+    // scales the accumulator and adds the norms)
+    constexpr bool kNM = !kF8;
 
     extern __shared__ __align__(1024) unsigned char sm[];
     // device-side path choice: the kernel runs only when *skip_if == 0
@@ -137,9 +154,12 @@ __global__ void __launch_bounds__(kScanThreads, 1)
 
     ScanSmem s;
     s.ring = sm;
-    s.norms = reinterpret_cast<float*>(s.ring + (size_t)R * slot_bytes);
+    unsigned char* side = s.ring + (size_t)R * slot_bytes;
+    s.norms = reinterpret_cast<float*>(side);   // E4M3 keys: the norm ring
     float* scales = s.norms + kNormSlots * TN;  // E4M3 keys: corpus scales, same slots as the norms
-    uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(s.norms) + norm_bytes(TN, kF8));
+    unsigned char* np_ring = side;              // BF16 keys: norm parts of ring slot i at i * np_bytes
+    unsigned char* ones = side + (size_t)R * np_bytes(TN);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(side + side_bytes(TN, kF8, R));
     s.full = bars;
     s.empty = bars + kScanMaxRing;
     s.accf = bars + 2 * kScanMaxRing;
@@ -177,6 +197,13 @@ __global__ void __launch_bounds__(kScanThreads, 1)
         *s.abort = 0;
         ptx::fence_mbar_init();
         ptx::tma_prefetch_desc(&a.tm_c);
+        if (kNM) ptx::tma_prefetch_desc(&a.tm_np);
+    }
+    if constexpr (kNM) {
+        // the ones block (any layout: every element is 1), visible to the tensor core
+        uint32_t* o = reinterpret_cast<uint32_t*>(ones);
+        for (int i = tid; i < (int)(kOnesBytes / 4); i += blockDim.x) o[i] = 0x3F803F80u;
+        ptx::fence_proxy_async_smem();
     }
     if (warp == 1) {
         ptx::tmem_alloc(s.tmem_holder, kTmemCols);
@@ -199,21 +226,27 @@ __global__ void __launch_bounds__(kScanThreads, 1)
                     const uint32_t ph = (uint32_t)(it / R) & 1u;
                     if (!scan_wait(a, s, &s.empty[st], ph ^ 1u, kDevTimeoutProducer)) { ok = false; break; }
                     unsigned char* dst = s.ring + (size_t)st * slot_bytes;
-                    ptx::mbar_arrive_expect_tx(&s.full[st], slot_bytes);
+                    // BF16 keys: the tile's norm parts travel with its last slot
+                    const bool np_here = kNM && c == slots_per_tile - 1;
+                    ptx::mbar_arrive_expect_tx(&s.full[st], slot_bytes + (np_here ? np_bytes(TN) : 0u));
                     for (int bx = 0; bx < bps; ++bx)
                         ptx::tma_load_2d(dst + (size_t)bx * kBoxB, &a.tm_c, &s.full[st], (c * bps + bx) * 64, (int)n0);
+                    if (np_here) ptx::tma_load_2d(np_ring + (size_t)st * np_bytes(TN), &a.tm_np, &s.full[st], 0, (int)n0);
                 }
                 if (!ok) break;
-                // norms (needed by the epilogue only, after the MMAs); the array is padded
-                // with +inf at least one tile past the view
-                const int ns = t % kNormSlots;
-                if (!scan_wait(a, s, &s.nempty[ns], ((uint32_t)(t / kNormSlots) & 1u) ^ 1u, kDevTimeoutProducer)) {
-                    ok = false;
-                    break;
+                if constexpr (kF8) {
+                    // norms and scales (needed by the epilogue only, after the MMAs); the arrays
+                    // are padded (+inf norms) at least one tile past the view
+                    const int ns = t % kNormSlots;
+                    if (!scan_wait(a, s, &s.nempty[ns], ((uint32_t)(t / kNormSlots) & 1u) ^ 1u,
+                                   kDevTimeoutProducer)) {
+                        ok = false;
+                        break;
+                    }
+                    ptx::mbar_arrive_expect_tx(&s.nfull[ns], TN * 8u);
+                    ptx::bulk_load(s.norms + ns * TN, a.cn + n0, TN * 4u, &s.nfull[ns]);
+                    ptx::bulk_load(scales + ns * TN, a.cs + n0, TN * 4u, &s.nfull[ns]);
                 }
-                ptx::mbar_arrive_expect_tx(&s.nfull[ns], TN * 4u * (kF8 ? 2u : 1u));
-                ptx::bulk_load(s.norms + ns * TN, a.cn + n0, TN * 4u, &s.nfull[ns]);
-                if (kF8) ptx::bulk_load(scales + ns * TN, a.cs + n0, TN * 4u, &s.nfull[ns]);
             }
             // let copies already issued land before the CTA winds down
             if (!ok) {
@@ -257,6 +290,11 @@ __global__ void __launch_bounds__(kScanThreads, 1)
                                                  (box | kk) != 0);
                         }
                     }
+                    // BF16 keys: + ones x norm parts, the norms added inside the tensor core
+                    if (kNM && c == slots_per_tile - 1)
+                        ptx::mma_bf16_ss(d_tmem, ptx::desc_sw32_kmajor(ptx::smem_u32(ones)),
+                                         ptx::desc_sw32_kmajor(ptx::smem_u32(np_ring + (size_t)st * np_bytes(TN))),
+                                         kIdesc, 1u);
                     // after the tile's last MMAs the accumulator-ready commit goes first: the
                     // epilogue is on the critical path, the producer has the ring's slack
                     if (c == slots_per_tile - 1) ptx::mma_commit(&s.accf[b]);
@@ -279,12 +317,20 @@ __global__ void __launch_bounds__(kScanThreads, 1)
         const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
         if (part == 0) {
             // A operand: this lane's query into TMEM (BF16 pairs or E4M3 quads per 32-bit column,
-            // lower K index in the low bits)
+            // lower K index in the low bits); BF16 keys take -2 q (exact: a power of two)
             const uint32_t* qrow = reinterpret_cast<const uint32_t*>(a.qbf) + (valid ? q : 0) * (a.dpb / 2);
             for (int bx = 0; bx < nbox; ++bx) {
                 float w[32];
 #pragma unroll
-                for (int u = 0; u < 32; ++u) w[u] = valid ? __uint_as_float(__ldg(qrow + bx * 32 + u)) : 0.f;
+                for (int u = 0; u < 32; ++u) {
+                    uint32_t x = valid ? __ldg(qrow + bx * 32 + u) : 0u;
+                    if (kNM) {
+                        __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162*>(&x);
+                        h = __hmul2(h, __float2bfloat162_rn(-2.f));
+                        x = *reinterpret_cast<const uint32_t*>(&h);
+                    }
+                    w[u] = __uint_as_float(x);
+                }
                 __syncwarp();
                 ptx::tmem_st32(tmem + lane_base + kACol + (uint32_t)(bx * 32), w);
             }
@@ -305,8 +351,8 @@ __global__ void __launch_bounds__(kScanThreads, 1)
             const uint32_t use = (uint32_t)(t / kNacc);
             const int ns = t % kNormSlots;
             // warp-uniform outcome: tcgen05.ld below is warp-collective
-            const bool ok = scan_wait(a, s, &s.accf[b], use & 1u, kDevTimeoutEpilogue) &&
-                            scan_wait(a, s, &s.nfull[ns], (uint32_t)(t / kNormSlots) & 1u, kDevTimeoutEpilogue);
+            bool ok = scan_wait(a, s, &s.accf[b], use & 1u, kDevTimeoutEpilogue);
+            if (kF8) ok = ok && scan_wait(a, s, &s.nfull[ns], (uint32_t)(t / kNormSlots) & 1u, kDevTimeoutEpilogue);
             if (!__all_sync(0xffffffffu, ok)) break;
             ptx::tc_fence_after();
             // this part's columns (see the chunk layout above)
@@ -329,18 +375,33 @@ __global__ void __launch_bounds__(kScanThreads, 1)
             ptx::tc_fence_before();
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&s.acce[b]);
-            const uint32_t ga = chunk_keys<W1, kF8>(va, nrm + c1, scl + c1, m, T, va);
+            uint32_t ga, gb, gc = 0u;
+            if constexpr (kNM) {
+                // the accumulator holds the keys; the view's last tile masks its rows past the view
+                const int64_t rem = a.N - (n_begin + (int64_t)t * TN);
+                if (rem < TN) {
+                    chunk_mask<W1>(va, c1, (int)rem);
+                    chunk_mask<W2>(vb, c2, (int)rem);
+                    if constexpr (W3 > 0) chunk_mask<W3>(vc, c3, (int)rem);
+                }
+                ga = chunk_test<W1>(va, T);
+                gb = chunk_test<W2>(vb, T);
+                if constexpr (W3 > 0) gc = chunk_test<W3>(vc, T);
+            } else {
+                ga = chunk_keys<W1, kF8>(va, nrm + c1, scl + c1, m, T, va);
+                gb = chunk_keys<W2, kF8>(vb, nrm + c2, scl + c2, m, T, vb);
+                if constexpr (W3 > 0) gc = chunk_keys<W3, kF8>(vc, nrm + c3, scl + c3, m, T, vc);
+            }
             if (__any_sync(0xffffffffu, ga != 0u)) chunk_append<W1>(va, ga, T, nb + (uint32_t)c1, out, cap, cnt);
-            const uint32_t gb = chunk_keys<W2, kF8>(vb, nrm + c2, scl + c2, m, T, vb);
-            uint32_t gc = 0u;
-            if constexpr (W3 > 0) gc = chunk_keys<W3, kF8>(vc, nrm + c3, scl + c3, m, T, vc);
             if (__any_sync(0xffffffffu, (gb | gc) != 0u)) {
                 chunk_append<W2>(vb, gb, T, nb + (uint32_t)c2, out, cap, cnt);
                 if constexpr (W3 > 0) chunk_append<W3>(vc, gc, T, nb + (uint32_t)c3, out, cap, cnt);
             }
-            // norm slot ns fully read
-            __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(&s.nempty[ns]);
+            if constexpr (kF8) {
+                // norm slot ns fully read
+                __syncwarp();
+                if (lane == 0) ptx::mbar_arrive(&s.nempty[ns]);
+            }
         }
         if (valid) a.cnt[seg * (size_t)a.Q + (size_t)q] = cnt;
     }
@@ -371,7 +432,7 @@ int scan_part_cols(int dpb, int accs) { return scan_tile_rows(dpb, accs) / kScan
 size_t scan_smem_bytes(int dpb, int bps, int ring, bool fp8, int accs)
 {
     const int tn = scan_tile_rows(dpb, accs);
-    return (size_t)ring * bps * box_bytes(tn) + norm_bytes(tn, fp8) + kCtrlBytes;
+    return (size_t)ring * bps * box_bytes(tn) + side_bytes(tn, fp8, ring) + kCtrlBytes;
 }
 
 int scan_plan(int dpb, int want_bps, int* bps, int* ring, bool fp8, int accs)
@@ -379,9 +440,12 @@ int scan_plan(int dpb, int want_bps, int* bps, int* ring, bool fp8, int accs)
     const int nbox = dpb / 64;
     if (dpb % 64 != 0 || nbox < 1 || nbox > 4 || (accs != 2 && accs != 4)) return -1;
     const int tn = scan_tile_rows(dpb, accs);
-    const size_t fixed = norm_bytes(tn, fp8) + kCtrlBytes;
+    // E4M3 keys: the norm ring beside the slots; BF16 keys: norm parts in every slot, the ones block
+    const size_t fixed = (fp8 ? norm_bytes(tn) : kOnesBytes) + kCtrlBytes;
+    const size_t per_slot_side = fp8 ? 0 : np_bytes(tn);
     auto slots = [&](int b) {
-        return (int)std::min<size_t>(kScanMaxRing, (kScanSmemLimit - fixed) / ((size_t)b * box_bytes(tn)));
+        return (int)std::min<size_t>(kScanMaxRing,
+                                     (kScanSmemLimit - fixed) / ((size_t)b * box_bytes(tn) + per_slot_side));
     };
     int b = 0;
     if (want_bps > 0) {

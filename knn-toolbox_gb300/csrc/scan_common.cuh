@@ -52,6 +52,30 @@ __device__ __forceinline__ uint32_t chunk_keys(const float (&v)[W], const float*
     return gm;
 }
 
+// Mask of the 8-column groups of a W-column chunk of keys that hold a key below T.
+template <int W>
+__device__ __forceinline__ uint32_t chunk_test(const float (&key)[W], float T)
+{
+    constexpr int G = W < 8 ? W : 8;
+    uint32_t gm = 0;
+#pragma unroll
+    for (int g = 0; g < W / G; ++g) {
+        const float* kg = key + G * g;
+        const float mn = G == 8 ? min8(kg) : fminf(ptx::fmin3(kg[0], kg[1], kg[2]), kg[G - 1]);
+        gm |= (mn < T ? 1u : 0u) << g;
+    }
+    return gm;
+}
+
+// Keys of the columns at or past `rem` (rows past the corpus view in its last tile) set to +inf.
+template <int W>
+__device__ __forceinline__ void chunk_mask(float (&key)[W], int c0, int rem)
+{
+#pragma unroll
+    for (int j = 0; j < W; ++j)
+        if (c0 + j >= rem) key[j] = __int_as_float(0x7f800000);
+}
+
 // Append the keys below T of the flagged groups, in increasing corpus index.
 // Words hold the raw key bits above the index; the selection maps them to
 // ordered keys.

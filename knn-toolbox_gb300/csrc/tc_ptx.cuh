@@ -130,6 +130,18 @@ __device__ __forceinline__ void mma_tf32_ss(uint32_t d_tmem, uint64_t a_desc, ui
         : "memory");
 }
 
+// D[tmem] (+)= A[smem desc] * B[smem desc]^T, kind::f16 (BF16 operands, FP32 accumulate), cta_group::1
+__device__ __forceinline__ void mma_bf16_ss(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                            uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
 // D[tmem] (+)= A[tmem] * B[smem desc]^T, kind::f16 (BF16 operands, FP32 accumulate), cta_group::1
 __device__ __forceinline__ void mma_bf16_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc, uint32_t idesc,
                                             uint32_t accumulate)
@@ -279,6 +291,25 @@ __device__ __forceinline__ uint64_t desc_sw128_kmajor(uint32_t smem_addr)
     d |= (uint64_t)1 << 46;                           // descriptor version (tcgen05)
     d |= (uint64_t)2 << 61;                           // swizzle mode: 128B
     return d;
+}
+
+// Shared-memory matrix descriptor, K-major operand with 32-byte swizzle (rows of 16 BF16, as the
+// TMA's 32-byte swizzle writes them): 8-row x 32-byte swizzle atoms stacked at 256-byte stride.
+__device__ __forceinline__ uint64_t desc_sw32_kmajor(uint32_t smem_addr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((smem_addr & 0x3FFFFu) >> 4);     // start address
+    d |= (uint64_t)(16u >> 4) << 16;                  // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(256u >> 4) << 32;                 // stride byte offset: next 8-row group
+    d |= (uint64_t)1 << 46;                           // descriptor version (tcgen05)
+    d |= (uint64_t)6 << 61;                           // swizzle mode: 32B
+    return d;
+}
+
+// Shared-memory writes of this thread made visible to the async proxy (tensor core, TMA).
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
 // Instruction descriptor: kind::f16 with BF16 A/B, D f32, K-major, M x N.

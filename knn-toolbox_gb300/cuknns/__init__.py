@@ -108,7 +108,7 @@ def lib():
     L.knns_last_fixups.argtypes = [ctypes.POINTER(ctypes.c_int64)]
     L.knns_debug_tc_dot_tile.argtypes = [vp, i64, vp, i64, ci, vp]
     L.knns_debug_stall_next_search.argtypes = [i64]
-    L.knns_debug_prep.argtypes = [vp, i64, i64, ci, vp, vp, vp, vp, vp]
+    L.knns_debug_prep.argtypes = [vp, i64, i64, ci, vp, vp, vp, vp, vp, vp]
     L.knns_timing_collect.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
     L.knns_timing_collect5.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
     L.knns_search_device_noalloc.argtypes = [vp, i64, i64, vp, i64, i64, ci, ci, vp, vp, vp]
@@ -267,8 +267,9 @@ def search_host(corpus, queries, k, *, algo=ALGO_AUTO, splits=0, rerank=True, kp
     return dist, idx
 
 
-def debug_prep(x):
-    """Preparation pass over a device matrix: (norms, bf16 copy, E4M3 codes, scales, words), all torch tensors."""
+def debug_prep(x, norm_parts=False):
+    """Preparation pass over a device matrix: (norms, bf16 copy, E4M3 codes, scales, words), all torch tensors;
+    with norm_parts, also the [n][16] BF16 norm parts."""
     import torch
     n, D = x.shape
     dev = x.device
@@ -277,8 +278,11 @@ def debug_prep(x):
     f8 = torch.empty((n, (D + 127) // 128 * 128), dtype=torch.uint8, device=dev)
     scales = torch.empty(n, dtype=torch.float32, device=dev)
     words = torch.zeros(3, dtype=torch.int32, device=dev)
+    np_ = torch.empty((n, 16), dtype=torch.bfloat16, device=dev) if norm_parts else None
     _check(lib().knns_debug_prep(x.data_ptr(), n, x.stride(0), D, norms.data_ptr(), bf.data_ptr(), f8.data_ptr(),
-                                 scales.data_ptr(), words.data_ptr()))
+                                 scales.data_ptr(), words.data_ptr(), np_.data_ptr() if norm_parts else None))
+    if norm_parts:
+        return norms, bf, f8, scales, words, np_
     return norms, bf, f8, scales, words
 
 

@@ -9,7 +9,10 @@ Bars, all bit-exact:
  * the BF16 copy equals round-to-nearest-even BF16, zero padded to 64 columns;
  * the E4M3 codes equal round-to-nearest-even E4M3 of x * (448 / max|x|),
    zero padded to 128 bytes, and the scale is max|x| / 448;
- * the flags (not BF16-exact, not integer, max |x|) match numpy.
+ * the flags (not BF16-exact, not integer, max |x|) match numpy;
+ * the norm parts (the BF16 scan's norm operand) are three BF16 values whose sum, in any order,
+   is the FP32 norm exactly (norms of 0 and of 2^-100 or more; smaller ones to within 2^-133,
+   BF16's subnormal spacing), then zeros.
 """
 import numpy as np
 import pytest
@@ -51,7 +54,7 @@ def test_prep_outputs_bit_exact(engine, oracle, D, pad):
     buf = np.zeros((n, D + pad), np.float32)
     buf[:, :D] = x
     xt = torch.from_numpy(buf).cuda()[:, :D]
-    norms, bf, f8, scales, words = engine.debug_prep(xt)
+    norms, bf, f8, scales, words, parts = engine.debug_prep(xt, norm_parts=True)
     with np.errstate(over="ignore"):
         want = oracle.norms(x)
     got = norms.cpu().numpy()
@@ -71,6 +74,15 @@ def test_prep_outputs_bit_exact(engine, oracle, D, pad):
     np.testing.assert_array_equal(f8c[:, :D], codes)
     assert (f8c[:, D:] == 0).all()
     np.testing.assert_array_equal(scales.cpu().numpy(), (mx / np.float32(448.0)).astype(np.float32))
+
+    p = parts.float().cpu().numpy().astype(np.float64)
+    assert (p[:, 3:] == 0).all()
+    fin = np.isfinite(want) & (want < 3.3e38)
+    big = fin & ((want == 0) | (want >= 2.0 ** -100))
+    tiny = fin & ~big
+    np.testing.assert_array_equal(p[big, 0] + p[big, 1] + p[big, 2], want[big].astype(np.float64))
+    assert (np.abs(p[tiny, 0] + p[tiny, 1] + p[tiny, 2] - want[tiny].astype(np.float64)) <= 2.0 ** -133).all()
+    assert (p[~fin, 0] >= 3.3e38).all() and (p[~fin, 1:] == 0).all()
 
     w = words.cpu().numpy().view(np.uint32)
     assert w[0] == int((xb.float().numpy() != x).any())
