@@ -259,12 +259,10 @@ __device__ __forceinline__ void store_norm_parts(__nv_bfloat16* dst, float f)
     w0.y = (uint32_t)__bfloat16_as_ushort(n3);
     w0.z = 0u;
     w0.w = 0u;
-    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+    static_assert(kNormParts * 2 == 2 * sizeof(uint4), "one row of norm parts is two 16-byte words");
     uint4* d = reinterpret_cast<uint4*>(dst);
     d[0] = w0;
-    d[1] = z;
-    d[2] = z;
-    d[3] = z;
+    d[1] = make_uint4(0u, 0u, 0u, 0u);
 }
 
 template <int kChunks, int kU>
