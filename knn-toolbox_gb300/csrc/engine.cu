@@ -189,24 +189,6 @@ static int encode_np(CUtensorMap* m, const void* base, int64_t rows, int64_t pit
     return KNNS_OK;
 }
 
-// Norm parts [rows][kNormPartsTf32] fp32 (rows `pitch` elements apart), box {8, 128 rows}, 32B
-// swizzle (one 32-byte row per corpus row, the 3xTF32 scan's norm step)
-static int encode_np32(CUtensorMap* m, const float* base, int64_t rows, int64_t pitch)
-{
-    EncodeTiledFn fn;
-    int rc = get_encode_fn(&fn);
-    if (rc) return rc;
-    cuuint64_t dims[2] = {(cuuint64_t)kNormPartsTf32, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)pitch * sizeof(float)};
-    cuuint32_t box[2] = {(cuuint32_t)kNormPartsTf32, (cuuint32_t)kTileN};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return set_error(KNNS_ERR_CUDA, "cuTensorMapEncodeTiled (TF32 norm parts) failed (%d)", (int)r);
-    return KNNS_OK;
-}
-
 // ---------------------------------------------------------------- planning
 // smallest corpus the threshold scan runs on when asked to (KNNS_SCAN_ON, long shortlists)
 constexpr int64_t kScanMinRowsForced = 16384;
@@ -559,7 +541,6 @@ struct TscanStages {
     const float* hi;
     const float* lo;
     const uint32_t* cflags;
-    const float* np32;  // corpus norm parts [N][kNormPartsTf32]
     const float* qn;
     float* dist;
     int32_t* idx;
@@ -582,6 +563,7 @@ struct TscanStages {
         if (!rc) rc = E.tq.ensure((size_t)2 * Q * sizeof(float));
         if (!rc) rc = E.cand.ensure(sp.cand_words * sizeof(uint64_t));
         if (!rc) rc = E.cnt.ensure(sp.cnt_words * sizeof(uint32_t));
+        if (!rc) rc = E.cnv.ensure(sp.norm_words * sizeof(float));
         if (!rc) rc = fail.ensure((size_t)(Q + 1) * sizeof(uint32_t));
         if (!rc) rc = E.part.ensure(sp.part_words * sizeof(uint64_t));
         if (!rc) rc = E.thr2.ensure(Q * sizeof(uint32_t));
@@ -589,15 +571,14 @@ struct TscanStages {
     }
     size_t workspace() const
     {
-        return E.qhi.cap + E.qlo.cap + E.qlof.cap + E.tq.cap + E.cand.cap + E.cnt.cap + fail.cap +
+        return E.qhi.cap + E.qlo.cap + E.qlof.cap + E.tq.cap + E.cand.cap + E.cnt.cap + E.cnv.cap + fail.cap +
                E.part.cap + E.thr2.cap;
     }
-    // the TF32 hi / lo copies of -2 q (the scale is exact) and the tensor maps of the scan's
-    // query operand
+    // the queries' TF32 hi / lo copies and the tensor maps of the scan's query operand
     int split_queries()
     {
         KNN_CUDA(launch_split(queries, Q, ldq, D, c.dp, (float*)E.qhi.p, (float*)E.qlo.p, (uint32_t*)E.qlof.p,
-                              q_any_lo, run_if, s, -2.f));
+                              q_any_lo, run_if, s));
         ++launches;
         memset(&a, 0, sizeof(a));
         int rc = encode_rows(&a.tm_qhi, (const float*)E.qhi.p, Q, c.dp, c.dp);
@@ -614,13 +595,13 @@ struct TscanStages {
         return KNNS_OK;
     }
     // one scan over rows 0, stride, 2*stride, ... of the corpus (nview of them)
-    int pass(int64_t nview, int64_t stride, const float* thr, int splits, int64_t split_len, int cap,
-             const uint32_t* flags)
+    int pass(int64_t nview, int64_t stride, const float* cn_view, const float* thr, int splits, int64_t split_len,
+             int cap, const uint32_t* flags)
     {
         int r = encode_rows(&a.tm_chi, hi, nview, c.dp, stride * c.dp);
         if (!r) r = encode_rows(&a.tm_clo, lo, nview, c.dp, stride * c.dp);
-        if (!r) r = encode_np32(&a.tm_np, np32, nview, stride * kNormPartsTf32);
         if (r) return r;
+        a.cn = cn_view;
         a.thr = thr;
         a.N = nview;
         a.split_len = split_len;
@@ -645,11 +626,13 @@ struct TscanStages {
     int seed()
     {
         float* Tbuf[2] = {(float*)E.tq.p, (float*)E.tq.p + Q};
+        float* cnv = (float*)E.cnv.p;
         CandSelect cs = cand_select();
         T = nullptr;
         for (int l = 0; l < sp.levels; ++l) {
             const ScanLevel& v = sp.lv[l];
-            int rc = pass(v.n, v.stride, T, v.S, v.len, v.cap, nullptr);
+            KNN_CUDA(launch_gather_norms(cn, v.n, v.stride, cnv, v.n_pad, s));
+            int rc = pass(v.n, v.stride, cnv, T, v.S, v.len, v.cap, nullptr);
             if (rc) return rc;
             cs.nseg = kScanParts * v.S;
             cs.cap = v.cap;
@@ -657,12 +640,13 @@ struct TscanStages {
             cs.thr_rank = v.j;
             cs.thr_fallback = T;
             KNN_CUDA(launch_select_cand(cs, s));
-            ++launches;
+            launches += 2;
             T = Tbuf[l & 1];
+            cnv += v.n_pad;
         }
         return KNNS_OK;
     }
-    int main_pass() { return pass(N, 1, T, sp.S, sp.len, sp.cap, cflags); }
+    int main_pass() { return pass(N, 1, cn, T, sp.S, sp.len, sp.cap, cflags); }
     int select()
     {
         uint32_t* fail_cnt = (uint32_t*)fail.p;
@@ -735,7 +719,6 @@ static int run_tscan(Engine& E, const Config& c, const float* corpus, int64_t N,
         if (!rc) rc = E.hi.ensure((size_t)N * dp * sizeof(float));
         if (!rc) rc = E.lo.ensure((size_t)N * dp * sizeof(float));
         if (!rc) rc = E.loflags.ensure(((size_t)cdiv(N, 128) + 4) * sizeof(uint32_t));
-        if (!rc) rc = E.np32.ensure((size_t)N * kNormPartsTf32 * sizeof(float));
         if (rc) return rc;
     }
     rc = E.qn.ensure(Q * sizeof(float));
@@ -746,11 +729,9 @@ static int run_tscan(Engine& E, const Config& c, const float* corpus, int64_t N,
     uint32_t* cflags = (uint32_t*)(pc ? pc->tiles.p : E.loflags.p);
     TscanStages ts{E, c, sp, corpus, N, ldc, queries, Q, ldq, D, k, cn,
                    (const float*)(pc ? pc->hi.p : E.hi.p), (const float*)(pc ? pc->lo.p : E.lo.p), cflags,
-                   (const float*)(pc ? pc->np32.p : E.np32.p), (const float*)E.qn.p, dist, idx, idx_f, nullptr,
-                   words + 1, E.fail, s};
+                   (const float*)E.qn.p, dist, idx, idx_f, nullptr, words + 1, E.fail, s};
     if ((rc = ts.ensure())) return rc;
-    const size_t ws =
-        (pc ? 0 : E.cn.cap + E.hi.cap + E.lo.cap + E.loflags.cap + E.np32.cap) + E.qn.cap + ts.workspace();
+    const size_t ws = (pc ? 0 : E.cn.cap + E.hi.cap + E.lo.cap + E.loflags.cap) + E.qn.cap + ts.workspace();
 
     if (!capture) KNN_CUDA(cudaStreamWaitEvent(s, E.last_done, 0));
     cudaEvent_t tv[Engine::kTimingEvents] = {};
@@ -764,8 +745,7 @@ static int run_tscan(Engine& E, const Config& c, const float* corpus, int64_t N,
     if (!pc) {
         KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, 0, nullptr, cn, n_pad, nullptr, s));
         KNN_CUDA(launch_split(corpus, N, ldc, D, dp, (float*)E.hi.p, (float*)E.lo.p, cflags, words, nullptr, s));
-        KNN_CUDA(launch_norm_parts_tf32(cn, N, (float*)E.np32.p, nullptr, s));
-        ts.launches += 3;
+        ts.launches += 2;
     }
     KNN_CUDA(launch_prep_rows(queries, Q, ldq, D, 0, nullptr, (float*)E.qn.p, Q, nullptr, s));
     ++ts.launches;
@@ -968,16 +948,10 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     // the 3xTF32 scan beside the BF16 one (its buffers are shared with it but for its queries'
     // TF32 copies and its failed-query list: only one of the two paths runs)
     const float* cn_ts = (const float*)(pc ? pc->cn.p : E.cn.p);
-    if (tf_scan && !pc) {
-        rc = E.np32.ensure((size_t)N * kNormPartsTf32 * sizeof(float));
-        if (rc) return rc;
-        ws += E.np32.cap;
-    }
     TscanStages ts{E, c, sp_tf, corpus, N, ldc, queries, Q, ldq, D, k, cn_ts,
                    (const float*)(pc ? pc->hi.p : E.hi.p), (const float*)(pc ? pc->lo.p : E.lo.p),
-                   (const uint32_t*)(pc ? pc->tiles.p : E.loflags.p), (const float*)(pc ? pc->np32.p : E.np32.p),
-                   (const float*)E.qn.p, dist, idx, idx_f, (const uint32_t*)E.words.p + 1, (uint32_t*)E.words.p + 5,
-                   E.tfail, s};
+                   (const uint32_t*)(pc ? pc->tiles.p : E.loflags.p), (const float*)E.qn.p, dist, idx, idx_f,
+                   (const uint32_t*)E.words.p + 1, (uint32_t*)E.words.p + 5, E.tfail, s};
     if (tf_scan) {
         if ((rc = ts.ensure())) return rc;
         ws += E.qhi.cap + E.qlo.cap + E.qlof.cap + E.tfail.cap;
@@ -1134,10 +1108,6 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
             KNN_CUDA(launch_split(corpus, N, ldc, D, c.dp, (float*)E.hi.p, (float*)E.lo.p, flags, any_lo, not_exact,
                                   s));
             ++launches;
-            if (tf_scan) {
-                KNN_CUDA(launch_norm_parts_tf32(cn, N, (float*)E.np32.p, not_exact, s));
-                ++launches;
-            }
         }
         if (tf_scan && !blocked && (rc = ts.split_queries())) return rc;
     } else {
@@ -1376,8 +1346,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
             if (tf_scan) {
                 KNN_CUDA(launch_split(corpus, N, ldc, D, c.dp, (float*)E.hi.p, (float*)E.lo.p, flags, any_lo,
                                       not_exact, s));
-                KNN_CUDA(launch_norm_parts_tf32(cn, N, (float*)E.np32.p, not_exact, s));
-                launches += 2;
+                ++launches;
                 if ((rc = ts.split_queries())) return rc;
                 if ((rc = ts.seed())) return rc;
                 if ((rc = ts.main_pass())) return rc;
@@ -1489,7 +1458,6 @@ void PreparedCorpus::release()
     f8.release();
     cs.release();
     np.release();
-    np32.release();
 }
 
 int prepare_corpus(Engine& E, PreparedCorpus* pc, const float* corpus, int64_t N, int64_t ldc, int D, bool tf32,
@@ -1511,17 +1479,14 @@ int prepare_corpus(Engine& E, PreparedCorpus* pc, const float* corpus, int64_t N
     if (!rc && fp8) rc = pc->f8.ensure((size_t)N * dpf * 2);
     if (!rc && fp8) rc = pc->cs.ensure(n_pad * sizeof(float));
     if (!rc) rc = pc->np.ensure((size_t)N * kNormParts * 2);
-    if (!rc && tf32) rc = pc->np32.ensure((size_t)N * kNormPartsTf32 * sizeof(float));
     if (rc) return rc;
     uint32_t* w = (uint32_t*)pc->words.p;
     KNN_CUDA(cudaMemsetAsync(w, 0, 8 * sizeof(uint32_t), s));
     KNN_CUDA(launch_prep_rows(corpus, N, ldc, D, dpb, pc->bf.p, (float*)pc->cn.p, n_pad, w + 1, s, w + 2,
                               fp8 ? pc->f8.p : nullptr, 2 * dpf, fp8 ? (float*)pc->cs.p : nullptr, pc->np.p));
-    if (tf32) {
+    if (tf32)
         KNN_CUDA(launch_split(corpus, N, ldc, D, dp, (float*)pc->hi.p, (float*)pc->lo.p, (uint32_t*)pc->tiles.p, w,
                               nullptr, s));
-        KNN_CUDA(launch_norm_parts_tf32((const float*)pc->cn.p, N, (float*)pc->np32.p, nullptr, s));
-    }
     pc->corpus = corpus;
     pc->N = N;
     pc->ldc = ldc;

@@ -62,9 +62,8 @@ struct Engine {
     // host-buffer searches with the threshold scan: the seeding sample (every 32nd corpus row)
     // copied ahead of the corpus, and its norms, BF16 copy, E4M3 codes and scales
     DevBuf smp, smp_cn, smp_bf, smp_f8, smp_cs, smp_np;
-    // threshold scans: the corpus norms as BF16 parts (kNormParts per row) and as TF32 parts
-    // (kNormPartsTf32 per row) for the MMA
-    DevBuf np, np32;
+    // BF16 threshold scan: the corpus norms as BF16 parts (kNormParts per row) for the MMA
+    DevBuf np;
     // stage timing: kTimingEvents events per timed search (start, after prep,
     // after threshold seeding, after the main fused kernel, after the main
     // selection, end)
@@ -100,7 +99,7 @@ struct PreparedCorpus {
     int64_t N = 0, ldc = 0;
     int D = 0, dpb = 0, dp = 0, dpf = 0;
     bool tf32 = false, fp8 = false;
-    DevBuf cn, bf, hi, lo, tiles, words, f8, cs, np, np32;
+    DevBuf cn, bf, hi, lo, tiles, words, f8, cs, np;
     void release();
 };
 

@@ -31,15 +31,8 @@ cudaError_t launch_norms(const float* x, int64_t n, int64_t ld, int D, float* ou
 // TF32 hi/lo split into [n][dp] arrays; lo_flags[tile of 128 rows] = any lo != 0 (may be null);
 // *any_lo (zeroed by the caller, may be null) becomes 1 when some tile has a low part.  When
 // skip_unless is given and *skip_unless == 0 at run time, the kernel does nothing.
-// scale: a power of two applied to x first (exact), -2 for the queries of the 3xTF32 scan.
 cudaError_t launch_split(const float* x, int64_t n, int64_t ld, int D, int dp, float* hi, float* lo,
-                         uint32_t* lo_flags, uint32_t* any_lo, const uint32_t* skip_unless, cudaStream_t s,
-                         float scale = 1.f);
-// The norms cn[0..n) as TF32 parts out[n][kNormPartsTf32] (n1, n2, n3, 0, ...), n1 + n2 + n3 equal
-// to the norm; nothing when skip_unless is given and *skip_unless == 0 at run time.
-constexpr int kNormPartsTf32 = 8;
-cudaError_t launch_norm_parts_tf32(const float* cn, int64_t n, float* out, const uint32_t* skip_unless,
-                                   cudaStream_t s);
+                         uint32_t* lo_flags, uint32_t* any_lo, const uint32_t* skip_unless, cudaStream_t s);
 // BF16 copy into [n][dpb] (out may be null: check only); *not_exact |= 1 when some element
 // is not exactly representable in BF16.
 cudaError_t launch_bf16(const float* x, int64_t n, int64_t ld, int D, int dpb, void* out, uint32_t* not_exact,
@@ -167,7 +160,7 @@ cudaError_t launch_scan(const ScanArgs& a, int splits, cudaStream_t s);
 struct TscanArgs {
     CUtensorMap tm_qhi, tm_qlo;   // queries hi / lo [Q][dp] fp32, box {32, 128}, 128B swizzle
     CUtensorMap tm_chi, tm_clo;   // corpus hi / lo view [N][dp] fp32, same boxes
-    CUtensorMap tm_np;            // corpus norm parts view [N][kNormPartsTf32] fp32, box {8, 128}, 32B swizzle
+    const float* cn;              // [>= N + 128] corpus norms of the view, +inf padding
     const float* thr;             // [Q] thresholds (null: +inf, every key collected)
     const uint32_t* qlo_flags;    // [query tiles] 1 when the tile has a nonzero low part (null: all)
     const uint32_t* clo_flags;    // [128-row tiles of the view] same for the corpus (null: all)

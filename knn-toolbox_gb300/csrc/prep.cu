@@ -75,12 +75,12 @@ __global__ void bf16_tiles_kernel(const float* __restrict__ x, int64_t n, int64_
     if (threadIdx.x == 0 && bad) atomicOr(not_exact, 1u);
 }
 
-// hi = tf32(s x), lo = tf32(s x - hi) for a power-of-two scale s (exact); rows padded with
-// zeros to dp columns.  One block per 128-row tile; lo_flags[tile] = 1 when any lo in the tile
-// is nonzero (the tensor-core kernels skip the correction products otherwise).
+// hi = tf32(x), lo = tf32(x - hi); rows padded with zeros to dp columns.
+// One block per 128-row tile; lo_flags[tile] = 1 when any lo in the tile is
+// nonzero (the tensor-core kernel skips the correction products otherwise).
 __global__ void split_tiles_kernel(const float* __restrict__ x, int64_t n, int64_t ld, int D, int dp,
                                    float* __restrict__ hi, float* __restrict__ lo, uint32_t* __restrict__ lo_flags,
-                                   uint32_t* __restrict__ any_lo, const uint32_t* __restrict__ skip_unless, float scale)
+                                   uint32_t* __restrict__ any_lo, const uint32_t* __restrict__ skip_unless)
 {
     // BF16-exact inputs are searched by the BF16 kernel: nothing to prepare
     if (skip_unless && *skip_unless == 0u) return;
@@ -91,7 +91,7 @@ __global__ void split_tiles_kernel(const float* __restrict__ x, int64_t n, int64
     for (int64_t i = threadIdx.x; i < total; i += blockDim.x) {
         const int64_t r = r0 + i / dp;
         const int c = (int)(i % dp);
-        const float v = c < D ? __fmul_rn(__ldg(x + r * ld + c), scale) : 0.f;
+        const float v = c < D ? __ldg(x + r * ld + c) : 0.f;
         const float h = tf32_rne(v);
         const float l = tf32_rne(__fsub_rn(v, h));
         hi[r * dp + c] = h;
@@ -103,27 +103,6 @@ __global__ void split_tiles_kernel(const float* __restrict__ x, int64_t n, int64
         if (lo_flags) lo_flags[blockIdx.x] = any ? 1u : 0u;
         if (any && any_lo) atomicOr(any_lo, 1u);
     }
-}
-
-// The norms as three TF32 parts, 8 floats per row (n1, n2, n3, 0, ...): n1 + n2 + n3 == f
-// exactly for f = 0 and f >= 2^-100 (remainders exact by Sterbenz's lemma; 11 + 11 significant
-// bits in the first two parts leave at most 2 for the third), the 3xTF32 scan's norm operand.
-__global__ void norm_parts_tf32_kernel(const float* __restrict__ cn, int64_t n, float* __restrict__ out,
-                                       const uint32_t* __restrict__ skip_unless)
-{
-    if (skip_unless && *skip_unless == 0u) return;
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float f = cn[i];
-    float n1 = tf32_rne(f), n2 = 0.f, n3 = 0.f;
-    if (isfinite(n1)) {
-        const float r1 = __fsub_rn(f, n1);
-        n2 = tf32_rne(r1);
-        n3 = tf32_rne(__fsub_rn(r1, n2));
-    }
-    float4* d = reinterpret_cast<float4*>(out + i * kNormPartsTf32);
-    d[0] = make_float4(n1, n2, n3, 0.f);
-    d[1] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 __global__ void gather_norms_kernel(const float* __restrict__ src, int64_t n, int64_t stride, float* __restrict__ out,
@@ -531,21 +510,11 @@ cudaError_t launch_norms(const float* x, int64_t n, int64_t ld, int D, float* ou
 }
 
 cudaError_t launch_split(const float* x, int64_t n, int64_t ld, int D, int dp, float* hi, float* lo,
-                         uint32_t* lo_flags, uint32_t* any_lo, const uint32_t* skip_unless, cudaStream_t s,
-                         float scale)
+                         uint32_t* lo_flags, uint32_t* any_lo, const uint32_t* skip_unless, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
     const int64_t tiles = (n + 127) / 128;
-    split_tiles_kernel<<<(unsigned)tiles, 256, 0, s>>>(x, n, ld, D, dp, hi, lo, lo_flags, any_lo, skip_unless,
-                                                       scale);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_norm_parts_tf32(const float* cn, int64_t n, float* out, const uint32_t* skip_unless,
-                                   cudaStream_t s)
-{
-    if (n <= 0) return cudaSuccess;
-    norm_parts_tf32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(cn, n, out, skip_unless);
+    split_tiles_kernel<<<(unsigned)tiles, 256, 0, s>>>(x, n, ld, D, dp, hi, lo, lo_flags, any_lo, skip_unless);
     return cudaGetLastError();
 }
 

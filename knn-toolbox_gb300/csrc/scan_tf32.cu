@@ -11,30 +11,25 @@
 // the query's candidate segment, and select_cand_kernel takes the shortlist from
 // the segments and re-ranks it by exact distance.
 //
-// Keys: with x = hi + lo (hi = tf32(x), lo = tf32(x - hi)) and the queries taken as
-// -2 q (exact), the key is accumulated in FP32 as qhi.chi + qhi.clo + qlo.chi by
-// tcgen05.mma.kind::tf32, plus one more K step: an all-ones A block against the
-// corpus rows' norms split into three TF32 parts (n1 + n2 + n3 = ||c||^2), so the
-// epilogue only compares.  A correction product whose low part is zero for the
-// whole corpus tile (or query tile) is skipped -- it would add exact zeros.
+// Keys: with x = hi + lo (hi = tf32(x), lo = tf32(x - hi)), q.c is accumulated in
+// FP32 as qhi.chi + qhi.clo + qlo.chi by tcgen05.mma.kind::tf32; a correction
+// product whose low part is zero for the whole corpus tile (or query tile) is
+// skipped -- it would add exact zeros.
 //
 // Tile: 128 queries (MMA M, TMEM lanes) x 128 corpus rows (MMA N), K in chunks of
 // 32 FP32 columns (one 128-byte swizzle row).  Both operands come from shared
 // memory, so any D works and tensor memory holds only accumulators: four of 128
 // columns.  A ring slot carries one K chunk of the query tile and of the corpus
-// tile, high and low parts (4 x 16 KB), and for a tile's last chunk the tile's
-// norm parts (128 rows x 32 bytes, 32-byte swizzle); a 4 KB block of ones is the
-// A operand of the norm step.
+// tile, high and low parts (4 x 16 KB).
 // Warp roles (608 threads):
 //   warp 0      producer: per tile and K chunk the query and corpus boxes (2-D TMA,
 //               32 fp32 x 128 rows, 128-byte swizzle), low parts only where present;
-//               with the last chunk the tile's norm parts;
+//               per tile the corpus norms (1-D bulk copy);
 //   warps 1, 18 MMA issuers, into accumulator t mod 4: of the even / odd tiles when a
 //               tile takes at most half the ring, else warp 1 alone (see below);
 //   warps 2..17 epilogue: thread = query (TMEM lane); warp 2 + 4p + j reads
-//               columns [32p, 32p + 32) of lane quarter j (the keys), releases the
-//               accumulator, appends those below the threshold (the view's last
-//               tile masks its columns past the view).
+//               columns [32p, 32p + 32) of lane quarter j, releases the
+//               accumulator, forms the keys, appends those below the threshold.
 // Every mbarrier wait is bounded; on timeout the kernel records an error code in
 // the device error word and winds down without hanging the GPU.
 #include <algorithm>
@@ -55,10 +50,9 @@ constexpr int kEpi = 4 * kParts;             // epilogue warps
 constexpr int kIss = 2;                      // MMA issuing threads
 constexpr int kThreads = 32 * (1 + kIss + kEpi);
 constexpr int kAcc = 4;                      // TMEM accumulators of 128 columns
+constexpr int kNorm = 8;                     // tiles of corpus norms in flight
 constexpr uint32_t kBox = 128u * 128u;       // one operand box: 128 rows x 32 fp32
 constexpr uint32_t kSlot = 4u * kBox;        // query hi, query lo, corpus hi, corpus lo
-constexpr uint32_t kNpBox = 128u * 32u;      // a tile's norm parts: 128 rows x 8 fp32
-constexpr uint32_t kOnes = 128u * 32u;       // the ones block: 128 rows x 8 fp32
 constexpr int kMaxRing = 3;
 constexpr uint32_t kCtrl = 512;
 constexpr uint64_t kTimeout = 4000000000ull;
@@ -66,12 +60,13 @@ constexpr uint32_t kIdesc = ptx::idesc_tf32(kTileQ, kTN);
 
 struct TSmem {
     unsigned char* ring;
-    unsigned char* np;  // [ring slots][kNpBox]: norm parts of the tile whose last chunk the slot holds
-    unsigned char* ones;
+    float* norms;       // [kNorm][kTN]
     uint64_t* full;     // [kMaxRing]
     uint64_t* empty;    // [kMaxRing]
     uint64_t* accf;     // [kAcc]
     uint64_t* acce;     // [kAcc]
+    uint64_t* nfull;    // [kNorm]
+    uint64_t* nempty;   // [kNorm]
     uint64_t* drain;
     uint32_t* tmem_holder;
     volatile int* abort;
@@ -100,14 +95,15 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_kernel(const __grid_constan
     const int R = a.ring;
     TSmem s;
     s.ring = sm;
-    s.np = sm + (size_t)R * kSlot;
-    s.ones = s.np + (size_t)R * kNpBox;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(s.ones + kOnes);
+    s.norms = reinterpret_cast<float*>(sm + (size_t)R * kSlot);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(s.norms + kNorm * kTN);
     s.full = bars;
     s.empty = bars + kMaxRing;
     s.accf = bars + 2 * kMaxRing;
     s.acce = s.accf + kAcc;
-    s.drain = s.acce + kAcc;
+    s.nfull = s.acce + kAcc;
+    s.nempty = s.nfull + kNorm;
+    s.drain = s.nempty + kNorm;
     uint32_t* words = reinterpret_cast<uint32_t*>(s.drain + 1);
     s.tmem_holder = words;
     s.abort = reinterpret_cast<volatile int*>(words + 1);
@@ -130,6 +126,10 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_kernel(const __grid_constan
             ptx::mbar_init(&s.accf[b], 1);
             ptx::mbar_init(&s.acce[b], kEpi);
         }
+        for (int b = 0; b < kNorm; ++b) {
+            ptx::mbar_init(&s.nfull[b], 1);
+            ptx::mbar_init(&s.nempty[b], kEpi);
+        }
         ptx::mbar_init(s.drain, kIss);
         *s.abort = 0;
         ptx::fence_mbar_init();
@@ -137,13 +137,6 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_kernel(const __grid_constan
         ptx::tma_prefetch_desc(&a.tm_qlo);
         ptx::tma_prefetch_desc(&a.tm_chi);
         ptx::tma_prefetch_desc(&a.tm_clo);
-        ptx::tma_prefetch_desc(&a.tm_np);
-    }
-    {
-        // the ones block (any layout: every element is 1), visible to the tensor core
-        uint32_t* o = reinterpret_cast<uint32_t*>(s.ones);
-        for (int i = tid; i < (int)(kOnes / 4); i += blockDim.x) o[i] = 0x3F800000u;
-        ptx::fence_proxy_async_smem();
     }
     if (warp == 1) {
         ptx::tmem_alloc(s.tmem_holder, 512);
@@ -170,16 +163,21 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_kernel(const __grid_constan
                     if (!t_wait(a, s, &s.empty[st], ph ^ 1u, kDevTimeoutProducer)) { ok = false; break; }
                     unsigned char* dst = s.ring + (size_t)st * kSlot;
                     s.slot_lo[st] = (qlo ? 1u : 0u) | (clo ? 2u : 0u);  // published by the arrive below
-                    const bool np_here = c == nch - 1;  // the tile's norm parts travel with its last chunk
-                    ptx::mbar_arrive_expect_tx(&s.full[st], kBox * (2u + (qlo ? 1u : 0u) + (clo ? 1u : 0u)) +
-                                                                (np_here ? kNpBox : 0u));
+                    ptx::mbar_arrive_expect_tx(&s.full[st], kBox * (2u + (qlo ? 1u : 0u) + (clo ? 1u : 0u)));
                     ptx::tma_load_2d(dst, &a.tm_qhi, &s.full[st], c * 32, (int)q0);
                     if (qlo) ptx::tma_load_2d(dst + kBox, &a.tm_qlo, &s.full[st], c * 32, (int)q0);
                     ptx::tma_load_2d(dst + 2 * kBox, &a.tm_chi, &s.full[st], c * 32, (int)n0);
                     if (clo) ptx::tma_load_2d(dst + 3 * kBox, &a.tm_clo, &s.full[st], c * 32, (int)n0);
-                    if (np_here) ptx::tma_load_2d(s.np + (size_t)st * kNpBox, &a.tm_np, &s.full[st], 0, (int)n0);
                 }
                 if (!ok) break;
+                const int ns = t % kNorm;
+                if (!t_wait(a, s, &s.nempty[ns], ((uint32_t)(t / kNorm) & 1u) ^ 1u, kDevTimeoutProducer)) {
+                    ok = false;
+                    break;
+                }
+                // the norms are padded with +inf at least one tile past the view
+                ptx::mbar_arrive_expect_tx(&s.nfull[ns], kTN * 4u);
+                ptx::bulk_load(s.norms + ns * kTN, a.cn + n0, kTN * 4u, &s.nfull[ns]);
             }
             if (!ok) {
                 // let copies already issued land before the CTA winds down
@@ -222,13 +220,8 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_kernel(const __grid_constan
                         if (lo & 2u) ptx::mma_tf32_ss(d_tmem, qh, ptx::desc_sw128_kmajor(base + 3 * kBox + kk * 32), kIdesc, 1u);
                         if (lo & 1u) ptx::mma_tf32_ss(d_tmem, ptx::desc_sw128_kmajor(base + kBox + kk * 32), ch, kIdesc, 1u);
                     }
-                    if (c == nch - 1) {
-                        // + ones x norm parts: the keys whole; then accumulator-ready first (the
-                        // epilogue waits on it)
-                        ptx::mma_tf32_ss(d_tmem, ptx::desc_sw32_kmajor(ptx::smem_u32(s.ones)),
-                                         ptx::desc_sw32_kmajor(ptx::smem_u32(s.np + (size_t)st * kNpBox)), kIdesc, 1u);
-                        ptx::mma_commit(&s.accf[b]);
-                    }
+                    // the tile's last chunk: accumulator-ready first (the epilogue waits on it)
+                    if (c == nch - 1) ptx::mma_commit(&s.accf[b]);
                     ptx::mma_commit(&s.empty[st]);
                 }
                 if (!ok) break;
@@ -254,8 +247,10 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_kernel(const __grid_constan
         for (int t = 0; t < ntiles; ++t) {
             const int b = t % kAcc;
             const uint32_t use = (uint32_t)(t / kAcc);
+            const int ns = t % kNorm;
             // warp-uniform outcome: tcgen05.ld below is warp-collective
-            const bool ok = t_wait(a, s, &s.accf[b], use & 1u, kDevTimeoutEpilogue);
+            const bool ok = t_wait(a, s, &s.accf[b], use & 1u, kDevTimeoutEpilogue) &&
+                            t_wait(a, s, &s.nfull[ns], (uint32_t)(t / kNorm) & 1u, kDevTimeoutEpilogue);
             if (!__all_sync(0xffffffffu, ok)) break;
             ptx::tc_fence_after();
             float v[32];
@@ -265,12 +260,12 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_kernel(const __grid_constan
             ptx::tc_fence_before();
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&s.acce[b]);
-            // the accumulator holds the keys; the view's last tile masks its rows past the view
-            const int64_t rem = a.N - (n_begin + (int64_t)t * kTN);
-            if (rem < kTN) chunk_mask<32>(v, 32 * part, (int)rem);
-            const uint32_t g = chunk_test<32>(v, T);
+            const float* nrm = s.norms + ns * kTN + 32 * part;
+            const uint32_t g = chunk_keys<32, false>(v, nrm, nrm, -2.0f, T, v);
             if (__any_sync(0xffffffffu, g != 0u))
                 chunk_append<32>(v, g, T, (uint32_t)(n_begin + (int64_t)t * kTN) + (uint32_t)(32 * part), out, cap, cnt);
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&s.nempty[ns]);
         }
         if (valid) a.cnt[seg * (size_t)a.Q + (size_t)q] = cnt;
     }
@@ -285,7 +280,7 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_kernel(const __grid_constan
 }
 }  // namespace
 
-size_t tscan_smem_bytes(int ring) { return (size_t)ring * (kSlot + kNpBox) + kOnes + kCtrl; }
+size_t tscan_smem_bytes(int ring) { return (size_t)ring * kSlot + (size_t)kNorm * kTN * 4 + kCtrl; }
 
 int tscan_ring()
 {
