@@ -76,27 +76,51 @@ __global__ void bf16_tiles_kernel(const float* __restrict__ x, int64_t n, int64_
 }
 
 // hi = tf32(x), lo = tf32(x - hi); rows padded with zeros to dp columns.
-// One block per 128-row tile; lo_flags[tile] = 1 when any lo in the tile is
-// nonzero (the tensor-core kernel skips the correction products otherwise).
-__global__ void split_tiles_kernel(const float* __restrict__ x, int64_t n, int64_t ld, int D, int dp,
-                                   float* __restrict__ hi, float* __restrict__ lo, uint32_t* __restrict__ lo_flags,
-                                   uint32_t* __restrict__ any_lo, const uint32_t* __restrict__ skip_unless)
+// One block per 128-row tile, one warp per row at a time (eight rows in flight per block), each
+// lane a float4 of columns: coalesced 16-byte loads and stores.  lo_flags[tile] = 1 when any lo
+// in the tile is nonzero (the tensor-core kernels skip the correction products otherwise).
+__global__ void __launch_bounds__(256) split_tiles_kernel(const float* __restrict__ x, int64_t n, int64_t ld, int D,
+                                                          int dp, float* __restrict__ hi, float* __restrict__ lo,
+                                                          uint32_t* __restrict__ lo_flags,
+                                                          uint32_t* __restrict__ any_lo,
+                                                          const uint32_t* __restrict__ skip_unless)
 {
-    // BF16-exact inputs are searched by the BF16 kernel: nothing to prepare
+    // BF16-exact inputs are searched by the BF16 kernels: nothing to prepare
     if (skip_unless && *skip_unless == 0u) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t r0 = (int64_t)blockIdx.x * 128;
-    const int64_t rows = min((int64_t)128, n - r0);
-    const int64_t total = rows * dp;
+    // 16-byte loads when every row starts 16-byte aligned and holds whole float4s
+    const bool vec = (ld % 4 == 0) && (D % 4 == 0) && ((reinterpret_cast<uintptr_t>(x) & 15u) == 0);
     int any = 0;
-    for (int64_t i = threadIdx.x; i < total; i += blockDim.x) {
-        const int64_t r = r0 + i / dp;
-        const int c = (int)(i % dp);
-        const float v = c < D ? __ldg(x + r * ld + c) : 0.f;
-        const float h = tf32_rne(v);
-        const float l = tf32_rne(__fsub_rn(v, h));
-        hi[r * dp + c] = h;
-        lo[r * dp + c] = l;
-        any |= (l != 0.f);
+    for (int rr = warp; rr < 128; rr += 8) {
+        const int64_t r = r0 + rr;
+        if (r >= n) break;  // warp-uniform
+        const float* row = x + r * ld;
+        float4* H = reinterpret_cast<float4*>(hi + r * dp);
+        float4* L = reinterpret_cast<float4*>(lo + r * dp);
+        for (int c = 4 * lane; c < dp; c += 128) {
+            float v[4];
+            if (vec) {
+                float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (c < D) t = __ldg(reinterpret_cast<const float4*>(row + c));
+                v[0] = t.x;
+                v[1] = t.y;
+                v[2] = t.z;
+                v[3] = t.w;
+            } else {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) v[i] = c + i < D ? __ldg(row + c + i) : 0.f;
+            }
+            float h[4], l[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                h[i] = tf32_rne(v[i]);
+                l[i] = tf32_rne(__fsub_rn(v[i], h[i]));
+                any |= (l[i] != 0.f);
+            }
+            H[c >> 2] = make_float4(h[0], h[1], h[2], h[3]);
+            L[c >> 2] = make_float4(l[0], l[1], l[2], l[3]);
+        }
     }
     any = __syncthreads_or(any);
     if (threadIdx.x == 0) {
@@ -513,6 +537,7 @@ cudaError_t launch_split(const float* x, int64_t n, int64_t ld, int D, int dp, f
                          uint32_t* lo_flags, uint32_t* any_lo, const uint32_t* skip_unless, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
+    if (dp % 4 != 0 || dp < D) return cudaErrorInvalidValue;  // rows of whole float4s
     const int64_t tiles = (n + 127) / 128;
     split_tiles_kernel<<<(unsigned)tiles, 256, 0, s>>>(x, n, ld, D, dp, hi, lo, lo_flags, any_lo, skip_unless);
     return cudaGetLastError();
