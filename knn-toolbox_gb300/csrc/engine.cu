@@ -631,7 +631,7 @@ struct TscanStages {
         T = nullptr;
         for (int l = 0; l < sp.levels; ++l) {
             const ScanLevel& v = sp.lv[l];
-            KNN_CUDA(launch_gather_norms(cn, v.n, v.stride, cnv, v.n_pad, s));
+            KNN_CUDA(launch_gather_norms(cn, v.n, v.stride, cnv, v.n_pad, s, std::numeric_limits<float>::infinity(), run_if));
             int rc = pass(v.n, v.stride, cnv, T, v.S, v.len, v.cap, nullptr);
             if (rc) return rc;
             cs.nseg = kScanParts * v.S;

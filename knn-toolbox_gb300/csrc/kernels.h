@@ -265,9 +265,10 @@ cudaError_t launch_merge_topk(const float* run_d, const int32_t* run_i, int have
                               const int32_t* blk_i, int kb, int32_t offset, int64_t Q, int k, float* out_d,
                               int32_t* out_i, float* out_idx_f, cudaStream_t s);
 
-// out[i] = src[i * stride] for i < n, +inf for n <= i < n_pad (norms of a strided corpus sample).
-// out[i] = src[i * stride] for i < n, pad for n <= i < n_pad (+inf: norms of padding rows)
+// out[i] = src[i * stride] for i < n, pad for n <= i < n_pad (+inf: norms of padding rows), the
+// norms of a strided corpus sample; nothing when skip_unless is given and *skip_unless == 0.
 cudaError_t launch_gather_norms(const float* src, int64_t n, int64_t stride, float* out, int64_t n_pad,
-                                cudaStream_t s, float pad = std::numeric_limits<float>::infinity());
+                                cudaStream_t s, float pad = std::numeric_limits<float>::infinity(),
+                                const uint32_t* skip_unless = nullptr);
 
 }  // namespace knn

@@ -130,8 +130,9 @@ __global__ void __launch_bounds__(256) split_tiles_kernel(const float* __restric
 }
 
 __global__ void gather_norms_kernel(const float* __restrict__ src, int64_t n, int64_t stride, float* __restrict__ out,
-                                    int64_t n_pad, float pad)
+                                    int64_t n_pad, float pad, const uint32_t* __restrict__ skip_unless)
 {
+    if (skip_unless && *skip_unless == 0u) return;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_pad) return;
     out[i] = i < n ? src[i * stride] : pad;
@@ -516,10 +517,11 @@ cudaError_t launch_prep_rows(const float* x, int64_t n, int64_t ld, int D, int d
 }
 
 cudaError_t launch_gather_norms(const float* src, int64_t n, int64_t stride, float* out, int64_t n_pad,
-                                cudaStream_t s, float pad)
+                                cudaStream_t s, float pad, const uint32_t* skip_unless)
 {
     if (n_pad <= 0) return cudaSuccess;
-    gather_norms_kernel<<<(unsigned)((n_pad + 255) / 256), 256, 0, s>>>(src, n, stride, out, n_pad, pad);
+    gather_norms_kernel<<<(unsigned)((n_pad + 255) / 256), 256, 0, s>>>(src, n, stride, out, n_pad, pad,
+                                                                         skip_unless);
     return cudaGetLastError();
 }
 

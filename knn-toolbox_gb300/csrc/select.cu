@@ -180,6 +180,49 @@ __device__ __forceinline__ uint32_t radix4_digit(const uint64_t* w, int n, V y0,
     return ((a & 0xffffu) < rank ? 1u : 0u) + ((a >> 16) < rank ? 1u : 0u) + (b < rank ? 1u : 0u);
 }
 
+// Threshold mode with few keys: at most kThrRegs keys per lane, ranks up to kThrRankRegs.
+constexpr int kThrRegs = 8;
+constexpr int kThrRankRegs = 64;
+
+// The ordered key of rank `rank` (1-based, ties counted) among the key halves of w[0..n),
+// n <= 32 * kThrRegs, n >= rank: lane l holds w[l + 32 i], sorted in registers (Batcher's
+// odd-even merge network for 8); each round the warp minimum of the lanes' heads is found, every
+// lane whose head equals it drops its head, and the count of dropped keys decides the rank.
+__device__ __forceinline__ uint32_t rank_in_registers(const uint64_t* w, int n, uint32_t rank)
+{
+    const int lane = threadIdx.x & 31;
+    uint32_t k[kThrRegs];
+#pragma unroll
+    for (int i = 0; i < kThrRegs; ++i) k[i] = lane + 32 * i < n ? (uint32_t)(w[lane + 32 * i] >> 32) : 0xFFFFFFFFu;
+    auto ce = [&](int a, int b) {
+        const uint32_t lo = min(k[a], k[b]), hi = max(k[a], k[b]);
+        k[a] = lo;
+        k[b] = hi;
+    };
+    ce(0, 1); ce(2, 3); ce(4, 5); ce(6, 7);
+    ce(0, 2); ce(1, 3); ce(4, 6); ce(5, 7);
+    ce(1, 2); ce(5, 6);
+    ce(0, 4); ce(1, 5); ce(2, 6); ce(3, 7);
+    ce(2, 4); ce(3, 5);
+    ce(1, 2); ce(3, 4); ce(5, 6);
+    uint32_t removed = 0, x = 0xFFFFFFFFu;
+    for (uint32_t it = 0; it < rank; ++it) {  // every round drops at least one key
+        const uint32_t m = __reduce_min_sync(0xffffffffu, k[0]);
+        const bool hit = k[0] == m;
+        removed += (uint32_t)__popc(__ballot_sync(0xffffffffu, hit));
+        if (removed >= rank) {  // warp-uniform
+            x = m;
+            break;
+        }
+        if (hit) {
+#pragma unroll
+            for (int i = 0; i < kThrRegs - 1; ++i) k[i] = k[i + 1];
+            k[kThrRegs - 1] = 0xFFFFFFFFu;
+        }
+    }
+    return x;
+}
+
 // Exact distances of cur[0..kp) (direct difference, oracle order: eight partial
 // sums over d mod 8, fixed final tree).  Candidate rows are staged in shared
 // memory ([rows][D + 1]: conflict-free per-lane walks) four rows at a time with
@@ -319,15 +362,22 @@ __global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandS
     const int n = (int)total;
 
     if (kThr) {
-        // smallest key x with at least thr_rank keys not above it (radix-4 search, two bits
-        // per round: x's digit at bits [b0, b0 + 2) is the number of the thresholds
-        // x | d 2^b0 | (2^b0 - 1), d = 0, 1, 2, with fewer than thr_rank keys not above them)
+        // smallest key x with at least thr_rank keys not above it
         uint32_t x = 0;
-        for (int b0 = 30; b0 >= 0; b0 -= 2) {
-            const uint32_t low = (1u << b0) - 1u;
-            const uint32_t d = radix4_digit(buf, n, x | low, x | (1u << b0) | low, x | (2u << b0) | low,
-                                            (uint32_t)c.thr_rank, [](uint64_t v) { return (uint32_t)(v >> 32); });
-            x |= d << b0;
+        if (n <= 32 * kThrRegs && c.thr_rank <= kThrRankRegs) {
+            // few keys, small rank: each lane sorts its keys in registers, then the warp takes
+            // minima in rank order (each round removes the lanes' heads equal to the minimum)
+            x = rank_in_registers(buf, n, (uint32_t)c.thr_rank);
+        } else {
+            // radix-4 search, two bits per round: x's digit at bits [b0, b0 + 2) is the number
+            // of the thresholds x | d 2^b0 | (2^b0 - 1), d = 0, 1, 2, with fewer than thr_rank
+            // keys not above them
+            for (int b0 = 30; b0 >= 0; b0 -= 2) {
+                const uint32_t low = (1u << b0) - 1u;
+                const uint32_t d = radix4_digit(buf, n, x | low, x | (1u << b0) | low, x | (2u << b0) | low,
+                                                (uint32_t)c.thr_rank, [](uint64_t v) { return (uint32_t)(v >> 32); });
+                x |= d << b0;
+            }
         }
         if (lane == 0) {
             const float key = ord2f(x);
