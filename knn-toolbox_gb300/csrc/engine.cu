@@ -425,7 +425,7 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
     int tn = 128, pc = 32;
     if (tf32) {
         P->accs = 4;
-        P->ring = tscan_ring();
+        P->ring = tscan_ring(dpb <= 128);  // rows of up to 128 columns: queries in tensor memory
     } else {
         P->accs = o.scan_accs ? o.scan_accs : kScanAccsAuto;
         if (scan_plan(dpb, o.scan_boxes, &P->bps, &P->ring, fp8, P->accs) != 0)
@@ -577,14 +577,22 @@ struct TscanStages {
     // the queries' TF32 hi / lo copies and the tensor maps of the scan's query operand
     int split_queries()
     {
-        KNN_CUDA(launch_split(queries, Q, ldq, D, c.dp, (float*)E.qhi.p, (float*)E.qlo.p, (uint32_t*)E.qlof.p,
-                              q_any_lo, run_if, s));
-        ++launches;
         memset(&a, 0, sizeof(a));
-        int rc = encode_rows(&a.tm_qhi, (const float*)E.qhi.p, Q, c.dp, c.dp);
-        if (!rc) rc = encode_rows(&a.tm_qlo, (const float*)E.qlo.p, Q, c.dp, c.dp);
-        if (rc) return rc;
-        a.qlo_flags = (const uint32_t*)E.qlof.p;
+        if (c.dp <= 128) {
+            // the kernel splits the queries into tensor memory itself
+            a.tmem_a = 1;
+            a.queries = queries;
+            a.ldq = ldq;
+            a.D = D;
+        } else {
+            KNN_CUDA(launch_split(queries, Q, ldq, D, c.dp, (float*)E.qhi.p, (float*)E.qlo.p, (uint32_t*)E.qlof.p,
+                                  q_any_lo, run_if, s));
+            ++launches;
+            int rc = encode_rows(&a.tm_qhi, (const float*)E.qhi.p, Q, c.dp, c.dp);
+            if (!rc) rc = encode_rows(&a.tm_qlo, (const float*)E.qlo.p, Q, c.dp, c.dp);
+            if (rc) return rc;
+            a.qlo_flags = (const uint32_t*)E.qlof.p;
+        }
         a.cand = (uint64_t*)E.cand.p;
         a.cnt = (uint32_t*)E.cnt.p;
         a.err = (int*)E.err.p;

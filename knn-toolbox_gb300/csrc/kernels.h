@@ -175,9 +175,15 @@ struct TscanArgs {
     int split0;                   // first split of this launch
     int ring;                     // ring slots (tscan_ring())
     const uint32_t* run_if;       // optional: the kernel returns at once when *run_if == 0
+    // dp <= 128: the queries' TF32 hi / lo parts in tensor memory, split by the kernel from the
+    // FP32 queries (tm_qhi, tm_qlo, qlo_flags unused); the ring carries corpus chunks only
+    int tmem_a;
+    const float* queries;         // [Q][ldq] fp32 (tmem_a)
+    int64_t ldq;
+    int D;
 };
-size_t tscan_smem_bytes(int ring);
-int tscan_ring();
+size_t tscan_smem_bytes(int ring, bool tmem_a);
+int tscan_ring(bool tmem_a);
 cudaError_t launch_tscan(const TscanArgs& a, int splits, cudaStream_t s);
 
 // Merge of the per-split shortlists, optional exact re-rank, final top-k.
