@@ -103,7 +103,7 @@ def measured_peaks():
 NCU_TRAFFIC = {
     ("scan_kernel", "int1m"): 389.8e6,
     ("scan_kernel", "aniso8m"): 2537.0e6,
-    ("tscan_kernel", "uniform64k"): 70.21e6,
+    ("tscan_kernel", "uniform64k"): 70.0e6,
 }
 
 
