@@ -178,16 +178,6 @@ __global__ void __launch_bounds__(kScanThreads, 1)
     const int64_t n_begin = (int64_t)split * a.split_len;
     const int64_t n_end = min(a.N, n_begin + a.split_len);
     const int ntiles = n_end > n_begin ? (int)((n_end - n_begin + TN - 1) / TN) : 0;
-    // The CTAs of one split start one tile apart (query tile x at tile x mod ntiles) and wrap
-    // around: all query tiles of a split reading the same corpus tile at the same moment made its
-    // L2 lines a hot spot (three times slower per tile on the seeding samples), while a small
-    // offset keeps the tiles in flight few enough to stay in L2.  The order of the tiles changes
-    // only the order of a segment's candidates, which the selection sorts.
-    const int rot = ntiles > 0 ? (int)(blockIdx.x % (unsigned)ntiles) : 0;
-    auto tile_row = [&](int t) -> int64_t {
-        const int u = t + rot < ntiles ? t + rot : t + rot - ntiles;
-        return n_begin + (int64_t)u * TN;
-    };
 
     if (tid == 0) {
         for (int i = 0; i < R; ++i) {
@@ -230,7 +220,7 @@ __global__ void __launch_bounds__(kScanThreads, 1)
             int it = 0;
             bool ok = true;
             for (int t = 0; t < ntiles && ok; ++t) {
-                const int64_t n0 = tile_row(t);
+                const int64_t n0 = n_begin + (int64_t)t * TN;
                 for (int c = 0; c < slots_per_tile; ++c, ++it) {
                     const int st = it % R;
                     const uint32_t ph = (uint32_t)(it / R) & 1u;
@@ -369,8 +359,7 @@ __global__ void __launch_bounds__(kScanThreads, 1)
             const float* nrm = s.norms + ns * TN;
             const float* scl = scales + ns * TN;
             const uint32_t tb = tmem + (uint32_t)b * TN + lane_base;
-            const int64_t tr = tile_row(t);
-            const uint32_t nb = (uint32_t)tr;
+            const uint32_t nb = (uint32_t)(n_begin + (int64_t)t * TN);
             const int c1 = W1 * part, c2 = B2 + W2 * part, c3 = B3 + W3 * part;
             // all loads in flight together, one wait, then the accumulator is released:
             // the MMA may overwrite it while the keys are formed (in place) and tested
@@ -389,7 +378,7 @@ __global__ void __launch_bounds__(kScanThreads, 1)
             uint32_t ga, gb, gc = 0u;
             if constexpr (kNM) {
                 // the accumulator holds the keys; the view's last tile masks its rows past the view
-                const int64_t rem = a.N - tr;
+                const int64_t rem = a.N - (n_begin + (int64_t)t * TN);
                 if (rem < TN) {
                     chunk_mask<W1>(va, c1, (int)rem);
                     chunk_mask<W2>(vb, c2, (int)rem);

@@ -115,13 +115,6 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_kernel(const __grid_constan
     const int64_t n_begin = (int64_t)split * a.split_len;
     const int64_t n_end = min(a.N, n_begin + a.split_len);
     const int ntiles = n_end > n_begin ? (int)((n_end - n_begin + kTN - 1) / kTN) : 0;
-    // CTAs of one split start one tile apart (see scan_bf16.cu: L2 hot spots otherwise); the tile
-    // order changes only the order of a segment's candidates, which the selection sorts
-    const int rot = ntiles > 0 ? (int)(blockIdx.x % (unsigned)ntiles) : 0;
-    auto tile_row = [&](int t) -> int64_t {
-        const int u = t + rot < ntiles ? t + rot : t + rot - ntiles;
-        return n_begin + (int64_t)u * kTN;
-    };
     const int nch = a.dp / 32;
 
     if (tid == 0) {
@@ -161,7 +154,7 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_kernel(const __grid_constan
             int it = 0;
             bool ok = true;
             for (int t = 0; t < ntiles && ok; ++t) {
-                const int64_t n0 = tile_row(t);
+                const int64_t n0 = n_begin + (int64_t)t * kTN;
                 // view rows are whole 128-row tiles of the flags' corpus (main pass: split_len % 128 == 0)
                 const uint32_t clo = a.clo_flags ? __ldg(a.clo_flags + n0 / kTN) : 1u;
                 for (int c = 0; c < nch; ++c, ++it) {
@@ -270,7 +263,7 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_kernel(const __grid_constan
             const float* nrm = s.norms + ns * kTN + 32 * part;
             const uint32_t g = chunk_keys<32, false>(v, nrm, nrm, -2.0f, T, v);
             if (__any_sync(0xffffffffu, g != 0u))
-                chunk_append<32>(v, g, T, (uint32_t)tile_row(t) + (uint32_t)(32 * part), out, cap, cnt);
+                chunk_append<32>(v, g, T, (uint32_t)(n_begin + (int64_t)t * kTN) + (uint32_t)(32 * part), out, cap, cnt);
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&s.nempty[ns]);
         }
@@ -370,13 +363,6 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_ta_kernel(const __grid_cons
     const int64_t n_begin = (int64_t)split * a.split_len;
     const int64_t n_end = min(a.N, n_begin + a.split_len);
     const int ntiles = n_end > n_begin ? (int)((n_end - n_begin + kTN - 1) / kTN) : 0;
-    // CTAs of one split start one tile apart (see scan_bf16.cu: L2 hot spots otherwise); the tile
-    // order changes only the order of a segment's candidates, which the selection sorts
-    const int rot = ntiles > 0 ? (int)(blockIdx.x % (unsigned)ntiles) : 0;
-    auto tile_row = [&](int t) -> int64_t {
-        const int u = t + rot < ntiles ? t + rot : t + rot - ntiles;
-        return n_begin + (int64_t)u * kTN;
-    };
     const int nch = a.dp / 32;
 
     if (tid == 0) {
@@ -415,7 +401,7 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_ta_kernel(const __grid_cons
             int it = 0;
             bool ok = true;
             for (int t = 0; t < ntiles && ok; ++t) {
-                const int64_t n0 = tile_row(t);
+                const int64_t n0 = n_begin + (int64_t)t * kTN;
                 const uint32_t clo = a.clo_flags ? __ldg(a.clo_flags + n0 / kTN) : 1u;
                 for (int c = 0; c < nch; ++c, ++it) {
                     const int st = it % R;
@@ -539,7 +525,7 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_ta_kernel(const __grid_cons
             const float* nrm = s.norms + ns * kTN + 32 * part;
             const uint32_t g = chunk_keys<32, false>(v, nrm, nrm, -2.0f, T, v);
             if (__any_sync(0xffffffffu, g != 0u))
-                chunk_append<32>(v, g, T, (uint32_t)tile_row(t) + (uint32_t)(32 * part), out, cap, cnt);
+                chunk_append<32>(v, g, T, (uint32_t)(n_begin + (int64_t)t * kTN) + (uint32_t)(32 * part), out, cap, cnt);
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&s.nempty[ns]);
         }
