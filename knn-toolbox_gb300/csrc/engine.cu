@@ -548,6 +548,7 @@ struct TscanStages {
     const uint32_t* run_if;
     uint32_t* q_any_lo;  // a word the queries' split ORs its low-part flag into
     DevBuf& fail;
+    DevBuf& thr2;        // fix-up thresholds
     cudaStream_t s;
     int launches = 0;
     TscanArgs a;
@@ -566,13 +567,13 @@ struct TscanStages {
         if (!rc) rc = E.cnv.ensure(sp.norm_words * sizeof(float));
         if (!rc) rc = fail.ensure((size_t)(Q + 1) * sizeof(uint32_t));
         if (!rc) rc = E.part.ensure(sp.part_words * sizeof(uint64_t));
-        if (!rc) rc = E.thr2.ensure(Q * sizeof(uint32_t));
+        if (!rc) rc = thr2.ensure(Q * sizeof(uint32_t));
         return rc;
     }
     size_t workspace() const
     {
         return E.qhi.cap + E.qlo.cap + E.qlof.cap + E.tq.cap + E.cand.cap + E.cnt.cap + E.cnv.cap + fail.cap +
-               E.part.cap + E.thr2.cap;
+               E.part.cap + thr2.cap;
     }
     // the queries' TF32 hi / lo copies and the tensor maps of the scan's query operand
     int split_queries()
@@ -688,10 +689,10 @@ struct TscanStages {
         if (rows <= 0) return KNNS_OK;
         uint32_t* fail_cnt = (uint32_t*)fail.p;
         int32_t* fail_idx = (int32_t*)fail.p + 1;
-        uint32_t* thr2 = (uint32_t*)E.thr2.p;
-        KNN_CUDA(cudaMemsetAsync(thr2, 0xFF, rows * sizeof(uint32_t), s));
+        uint32_t* t2 = (uint32_t*)thr2.p;
+        KNN_CUDA(cudaMemsetAsync(t2, 0xFF, rows * sizeof(uint32_t), s));
         KNN_CUDA(launch_simt(corpus, N, ldc, cn, queries, rows, ldq, D, c.kp, 32, split_len, splits,
-                             (uint64_t*)E.part.p, thr2, s, nullptr, fail_idx, fail_cnt, qbase));
+                             (uint64_t*)E.part.p, t2, s, nullptr, fail_idx, fail_cnt, qbase));
         SelectExtra ex;
         ex.qmap = fail_idx;
         ex.qcount = fail_cnt;
@@ -737,7 +738,7 @@ static int run_tscan(Engine& E, const Config& c, const float* corpus, int64_t N,
     uint32_t* cflags = (uint32_t*)(pc ? pc->tiles.p : E.loflags.p);
     TscanStages ts{E, c, sp, corpus, N, ldc, queries, Q, ldq, D, k, cn,
                    (const float*)(pc ? pc->hi.p : E.hi.p), (const float*)(pc ? pc->lo.p : E.lo.p), cflags,
-                   (const float*)E.qn.p, dist, idx, idx_f, nullptr, words + 1, E.fail, s};
+                   (const float*)E.qn.p, dist, idx, idx_f, nullptr, words + 1, E.fail, E.thr2, s};
     if ((rc = ts.ensure())) return rc;
     const size_t ws = (pc ? 0 : E.cn.cap + E.hi.cap + E.lo.cap + E.loflags.cap) + E.qn.cap + ts.workspace();
 
@@ -959,11 +960,20 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     TscanStages ts{E, c, sp_tf, corpus, N, ldc, queries, Q, ldq, D, k, cn_ts,
                    (const float*)(pc ? pc->hi.p : E.hi.p), (const float*)(pc ? pc->lo.p : E.lo.p),
                    (const uint32_t*)(pc ? pc->tiles.p : E.loflags.p), (const float*)E.qn.p, dist, idx, idx_f,
-                   (const uint32_t*)E.words.p + 1, (uint32_t*)E.words.p + 5, E.tfail, s};
+                   (const uint32_t*)E.words.p + 1, (uint32_t*)E.words.p + 5, E.tfail, E.tthr2, s};
     if (tf_scan) {
         if ((rc = ts.ensure())) return rc;
-        ws += E.qhi.cap + E.qlo.cap + E.qlof.cap + E.tfail.cap;
+        ws += E.qhi.cap + E.qlo.cap + E.qlof.cap + E.tfail.cap + E.tthr2.cap;
     }
+    // Resident corpora (one stream otherwise): the 3xTF32 scan runs on a side stream beside the
+    // BF16 path, so that the launches of whichever path does not match the data (they return at
+    // once) overlap the other path's kernels instead of adding to the search.  The two paths
+    // share no buffer that both write: candidates, thresholds and results are written by the
+    // path that runs only; failed-query lists and fix-up thresholds are their own.
+    const bool ts_side = tf_scan && !host_corpus && !capture && !o.single_stream;
+    cudaStream_t ts_stream = ts_side ? E.worker_stream(0) : nullptr;
+    if (ts_side && (!ts_stream || !E.order_event(1)))
+        return set_error(KNNS_ERR_CUDA, "stream or event creation failed");
     // Blocked mode (threshold scan on a corpus still in host memory, not under capture): the
     // seeding sample (every sp.stride0-th row, the rows the seeding levels read) is prepared first
     // and the seeding passes run while the corpus is copied in blocks (of whole main-scan splits)
@@ -1329,12 +1339,21 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         }
         // (the TF32 scan's seeding reuses the sample norms and threshold buffers: the BF16
         // levels, run or skipped, are done with them)
-        if (tf_scan && !blocked && (rc = ts.seed())) return rc;
+        if (ts_side) {
+            // the whole TF32 scan on the side stream, from the prepared inputs on
+            KNN_CUDA(cudaEventRecord(E.order_event(0), s));
+            KNN_CUDA(cudaStreamWaitEvent(ts_stream, E.order_event(0), 0));
+            ts.s = ts_stream;
+            if ((rc = ts.seed()) || (rc = ts.main_pass()) || (rc = ts.select()) || (rc = ts.fix())) return rc;
+            KNN_CUDA(cudaEventRecord(E.order_event(1), ts_stream));
+        } else if (tf_scan && !blocked && (rc = ts.seed())) {
+            return rc;
+        }
         if ((rc = mark(2))) return rc;
         // main pass
         if (!blocked) {
             if ((rc = scan_pass(f8 ? f8_p : bf_p, np_p, N, 1, cn, cs_p, T, sp.S, sp.len, sp.cap))) return rc;
-            if (tf_scan && (rc = ts.main_pass())) return rc;
+            if (tf_scan && !ts_side && (rc = ts.main_pass())) return rc;
         } else {
             // block by block on the worker streams (blocks scanned on the two workers overlap each
             // other's tails), each once prepared and once the thresholds are seeded
@@ -1386,7 +1405,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         cs.fail_cnt = fail_cnt;
         KNN_CUDA(launch_select_cand(cs, s));
         ++launches;
-        if (tf_scan && (rc = ts.select())) return rc;
+        if (tf_scan && !ts_side && (rc = ts.select())) return rc;
         if ((rc = mark(4))) return rc;
         // fix-up: failed queries, compacted, through the shortlist kernel without a threshold
         // (launches whose rows are all past the failure count return at once)
@@ -1443,7 +1462,8 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         };
         if ((rc = fix_pass(0, sp.fixA_rows, sp.fixA_S, sp.fixA_len))) return rc;
         if ((rc = fix_pass(sp.fixA_rows, sp.fixB_rows, sp.fixB_S, sp.fixB_len))) return rc;
-        if (tf_scan && (rc = ts.fix())) return rc;
+        if (tf_scan && !ts_side && (rc = ts.fix())) return rc;
+        if (ts_side) KNN_CUDA(cudaStreamWaitEvent(s, E.order_event(1), 0));
         if ((rc = mark(5))) return rc;
     }
     launches += ts.launches;

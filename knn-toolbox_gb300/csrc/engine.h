@@ -50,8 +50,9 @@ struct Engine {
     // E4M3 keys: corpus codes and row scales, query scales, sample scales
     DevBuf f8, cs, qs, csv;
     // 3xTF32 scan: the queries' TF32 hi / lo copies and the low-part flags of their tiles; the
-    // failed-query list of the scan when it runs beside the BF16 scan (exact form)
-    DevBuf qhi, qlo, qlof, tfail;
+    // failed-query list and fix-up thresholds of the scan when it runs beside the BF16 scan
+    // (exact form)
+    DevBuf qhi, qlo, qlof, tfail, tthr2;
     // per-search flag words: [0] some corpus tile has a TF32 low part, [1] corpus or
     // queries not BF16-exact, [2] some value not an integer, [3] max |x| (float bits), [4] zero,
     // [5] some query tile has a TF32 low part
