@@ -1032,24 +1032,9 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
                                                                    !E.worker_stream(Engine::kScanWorkers - 1))))
             return set_error(KNNS_ERR_CUDA, "stream or event creation failed");
     }
-    // the seeding sample read in place from page-locked memory before the block copies start:
-    // sharing the host link, each slowed the other (the flag words are cleared first, since the
-    // sample's preparation ORs into them)
-    const bool early_sample = streamed && !smp_copy;
-    int launches = 0;
-    if (early_sample) {
-        uint32_t* w = (uint32_t*)E.words.p;
-        KNN_CUDA(cudaMemsetAsync(w, 0, 6 * sizeof(uint32_t), s));
-        if (o.tf32_only && !bf16_only) KNN_CUDA(cudaMemsetAsync(w + 1, 0x01, 1, s));
-        KNN_CUDA(launch_prep_rows(smp_src, smp_n, smp_ld, D, c.dpb, E.smp_bf.p, (float*)E.smp_cn.p, smp_pad, w + 1,
-                                  s, w + 2, f8 ? E.smp_f8.p : nullptr, 2 * c.dpf, f8 ? (float*)E.smp_cs.p : nullptr,
-                                  np_keys ? E.smp_np.p : nullptr));
-        ++launches;
-    }
     if (host_corpus != nullptr) {
         cudaStream_t cs_ = E.copy_stream();
         // the copies overwrite the device corpus only once the previous search is done with it
-        // (and, from page-locked memory, once the seeding sample has been read)
         KNN_CUDA(cudaEventRecord(oev(0), s));
         KNN_CUDA(cudaStreamWaitEvent(cs_, oev(0), 0));
         if (streamed) {
@@ -1079,6 +1064,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         return KNNS_OK;
     };
     if ((rc = mark(0))) return rc;
+    int launches = 0;
     float* cn = (float*)(pc ? pc->cn.p : E.cn.p);
     float* qn = (!c.rerank || scan) ? (float*)E.qn.p : nullptr;
     uint64_t* part = (uint64_t*)E.part.p;
@@ -1094,11 +1080,11 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     if (pc) {
         KNN_CUDA(cudaMemcpyAsync(words, pc->words.p, 4 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
         KNN_CUDA(cudaMemsetAsync(words + 4, 0, 2 * sizeof(uint32_t), s));
-    } else if (!early_sample) {
+    } else {
         KNN_CUDA(cudaMemsetAsync(words, 0, 6 * sizeof(uint32_t), s));
     }
     // 3xTF32 keys on request: the data count as not BF16-exact (the preparation only ORs into the word)
-    if (o.tf32_only && !bf16_only && !early_sample) KNN_CUDA(cudaMemsetAsync(words + 1, 0x01, 1, s));
+    if (o.tf32_only && !bf16_only) KNN_CUDA(cudaMemsetAsync(words + 1, 0x01, 1, s));
     if (blocked) {
         // the corpus blocks, prepared on the preparation stream as they land (their flag words
         // only OR into the words just cleared)
@@ -1316,13 +1302,11 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         const void* lv_np = np_p;
         int64_t lv_div = 1;
         if (blocked) {
-            if (!early_sample) {
-                if (smp_copy) KNN_CUDA(cudaStreamWaitEvent(s, oev(1), 0));
-                KNN_CUDA(launch_prep_rows(smp_src, smp_n, smp_ld, D, c.dpb, E.smp_bf.p, (float*)E.smp_cn.p, smp_pad,
-                                          not_exact, s, int_stats, f8 ? E.smp_f8.p : nullptr, 2 * c.dpf,
-                                          f8 ? (float*)E.smp_cs.p : nullptr, np_keys ? E.smp_np.p : nullptr));
-                ++launches;
-            }
+            if (smp_copy) KNN_CUDA(cudaStreamWaitEvent(s, oev(1), 0));
+            KNN_CUDA(launch_prep_rows(smp_src, smp_n, smp_ld, D, c.dpb, E.smp_bf.p, (float*)E.smp_cn.p, smp_pad,
+                                      not_exact, s, int_stats, f8 ? E.smp_f8.p : nullptr, 2 * c.dpf,
+                                      f8 ? (float*)E.smp_cs.p : nullptr, np_keys ? E.smp_np.p : nullptr));
+            ++launches;
             key_src = f8 ? E.smp_f8.p : E.smp_bf.p;
             lv_cn = (const float*)E.smp_cn.p;
             lv_cs = (const float*)E.smp_cs.p;
