@@ -371,10 +371,6 @@ static int64_t seed_stride(int kp)
 struct ScanLevel {
     int64_t n = 0, stride = 1, len = 0, n_pad = 0;
     int j = 0, S = 1, cap = 0;
-    // balanced scan (per > 0): S CTAs of `per` (query tile, corpus tile) pairs each; a query has
-    // at most `ranges` segment ranges (kScanParts segments each); tiles = the view's tile count
-    int64_t per = 0, tiles = 0;
-    int ranges = 0;
 };
 
 struct ScanPlan {
@@ -384,8 +380,6 @@ struct ScanPlan {
     ScanLevel lv[kMaxSeedLevels];
     int64_t len = 0;
     int S = 1, cap = 0;
-    int64_t per = 0, tiles = 0;  // balanced main pass (see ScanLevel)
-    int ranges = 0;
     int sel_words = 0;  // bound on one query's stored main-pass candidates (selection buffer)
     int64_t fixA_rows = 0, fixA_len = 0, fixB_rows = 0, fixB_len = 0;
     int fixA_S = 1, fixB_S = 1;
@@ -423,28 +417,8 @@ static int seed_rank(double m) { return (int)std::ceil(2.0 * m + 4.0 * std::sqrt
 
 // tf32: the plan of the 3xTF32 scan (tiles of 128 rows, 32 columns per segment; fix-up on the
 // CUDA-core kernel); otherwise of the BF16 / E4M3 scan of row width dpb.
-// Balanced form of a BF16 / E4M3 scan pass over nt corpus tiles: one CTA per SM, each an equal
-// run of (query tile, corpus tile) pairs; needs at least two corpus tiles per query tile and a
-// query's segments within kScanMaxSegs.  Returns false to keep the classic split grid.
-static bool plan_balanced(int sms, int64_t qt, int64_t nt, int64_t* per, int* S, int* ranges)
-{
-    if (nt < 2) return false;
-    const int64_t total = qt * nt;
-    const int64_t G = std::min<int64_t>(sms, total);
-    const int64_t p = cdiv(total, G);
-    int r = 0;
-    for (int64_t x = 0; x < qt; ++x) r = std::max(r, scan_ranges_of(x, nt, p));
-    if (kScanParts * r > kScanMaxSegs) return false;
-    *per = p;
-    *S = (int)cdiv(total, p);
-    *ranges = r;
-    return true;
-}
-
-// balanced: the BF16 / E4M3 scan's passes run as balanced launches where they can (the blocked
-// schedule keeps the split grid: its blocks are whole splits)
 static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, const knns_options& o, ScanPlan* P,
-                     bool fp8, bool tf32 = false, bool balanced = false)
+                     bool fp8, bool tf32 = false)
 {
     if (o.scan_accs != 0 && o.scan_accs != 2 && o.scan_accs != 4)
         return set_error(KNNS_ERR_INVALID, "threshold scan: %d accumulators (2 or 4)", o.scan_accs);
@@ -507,21 +481,8 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
             const double hits = (double)P->lv[l - 1].j * (double)v.n / (double)P->lv[l - 1].n;
             v.cap = std::min<int>((int)(v.len / tn * pc), seg_cap(hits * pc / ((double)tn * v.S), 3.0));
         }
-        int nseg = kScanParts * v.S;
-        if (balanced && !tf32 && plan_balanced(E.sms, qt, tiles, &v.per, &v.S, &v.ranges)) {
-            v.tiles = tiles;
-            v.len = tn;  // unused by a balanced launch
-            const int64_t span = std::min<int64_t>(v.per, tiles);  // tiles of one query tile in one CTA
-            if (l == 0) {
-                v.cap = (int)(span * pc);  // every key kept
-            } else {
-                const double hits = (double)P->lv[l - 1].j * (double)v.n / (double)P->lv[l - 1].n;
-                v.cap = std::min<int>((int)(span * pc), seg_cap(hits * pc * (double)span / ((double)tn * tiles), 3.0));
-            }
-            nseg = kScanParts * v.ranges;
-        }
-        P->cand_words = std::max(P->cand_words, (size_t)nseg * Q * v.cap);
-        P->cnt_words = std::max(P->cnt_words, (size_t)nseg * Q);
+        P->cand_words = std::max(P->cand_words, (size_t)kScanParts * v.S * Q * v.cap);
+        P->cnt_words = std::max(P->cnt_words, (size_t)kScanParts * v.S * Q);
         P->norm_words += (size_t)v.n_pad;
     }
     // main pass
@@ -538,16 +499,8 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
     // the fix-up either way); the selection buffer is sized to it, not to its ceiling
     P->sel_words = (int)std::min<double>(
         (double)kCandMax, std::ceil((hm + 6.0 * (double)P->lv[L - 1].stride * std::sqrt((double)P->lv[L - 1].j) + 64.0) / 32.0) * 32.0);
-    int nseg = kScanParts * P->S;
-    if (balanced && !tf32 && plan_balanced(E.sms, qt, tiles, &P->per, &P->S, &P->ranges)) {
-        P->tiles = tiles;
-        P->len = tn;  // unused by a balanced launch
-        const int64_t span = std::min<int64_t>(P->per, tiles);
-        P->cap = std::min<int>((int)(span * pc), seg_cap(hm * pc * (double)span / ((double)tn * tiles), 2.0));
-        nseg = kScanParts * P->ranges;
-    }
-    P->cand_words = std::max(P->cand_words, (size_t)nseg * Q * P->cap);
-    P->cnt_words = std::max(P->cnt_words, (size_t)nseg * Q);
+    P->cand_words = std::max(P->cand_words, (size_t)kScanParts * P->S * Q * P->cap);
+    P->cnt_words = std::max(P->cnt_words, (size_t)kScanParts * P->S * Q);
     // fix-up of failed queries: up to 512 on a full wave, the rest (rare) on 8 splits; shortlists
     // above the tensor-core kernel's kMaxKpTC go to the CUDA-core kernel in tiles of 32 queries
     // (exact FP32 keys): the first 32 failed queries on a wave of splits, the rest on 8
@@ -708,9 +661,7 @@ struct TscanStages {
         uint32_t* fail_cnt = (uint32_t*)fail.p;
         KNN_CUDA(cudaMemsetAsync(fail_cnt, 0, sizeof(uint32_t), s));
         CandSelect cs = cand_select();
-        cs.nseg = kScanParts * (sp.per ? sp.ranges : sp.S);
-        cs.bal_per = sp.per;
-        cs.bal_tiles = sp.tiles;
+        cs.nseg = kScanParts * sp.S;
         cs.cap = sp.cap;
         cs.kp = c.kp;
         cs.k = k;
@@ -873,9 +824,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     if (c.algo == KNNS_ALGO_TC && o.scan != KNNS_SCAN_OFF && E.cc >= 100 && c.dpb <= 256 && c.rerank) {
         const int64_t min_n = (o.scan == KNNS_SCAN_ON || c.kp > kMaxKpTC) ? kScanMinRowsForced : kScanMinRowsAuto;
         if (N >= min_n) {
-            // balanced launches unless the blocked schedule will run (its blocks are whole splits)
-            const bool will_block = !pc && !capture && !o.single_stream && host_corpus != nullptr;
-            rc = plan_scan(E, N, Q, c.fp8 ? c.dpf : c.dpb, c.kp, o, &sp, c.fp8, false, !will_block);
+            rc = plan_scan(E, N, Q, c.fp8 ? c.dpf : c.dpb, c.kp, o, &sp, c.fp8);
             if (rc) return rc;
             scan = true;
         }
@@ -1321,7 +1270,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         // grid rows are the splits split0 .. split0 + splits - 1, launched on stream ls
         auto scan_pass = [&](const void* src, const void* np_src, int64_t nview, int64_t stride, const float* cn_view,
                              const float* cs_view, const float* thr, int splits, int64_t split_len, int cap,
-                             int64_t per, int split0 = 0, cudaStream_t ls = nullptr) -> int {
+                             int split0 = 0, cudaStream_t ls = nullptr) -> int {
             // the map moves bytes: E4M3 rows are described as rows of 16-bit units
             int r = encode_rows_bf16(&a.tm_c, src, nview, sdp, stride * sdp, scan_box_rows(sdp, sp.accs));
             if (!r && np_keys) r = encode_np(&a.tm_np, np_src, nview, stride * kNormParts, scan_box_rows(sdp, sp.accs));
@@ -1333,7 +1282,6 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
             a.split_len = split_len;
             a.cap = cap;
             a.split0 = split0;
-            a.per_cta = per;
             KNN_CUDA(launch_scan(a, splits, ls ? ls : s));
             ++launches;
             return KNNS_OK;
@@ -1377,11 +1325,8 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
                 KNN_CUDA(launch_gather_norms(lv_cs, v.n, v.stride / lv_div, csv, v.n_pad, s, 0.f));
                 launches += 2;
             }
-            if ((rc = scan_pass(key_src, lv_np, v.n, v.stride / lv_div, cnv, csv, T, v.S, v.len, v.cap, v.per)))
-                return rc;
-            cs.nseg = kScanParts * (v.per ? v.ranges : v.S);
-            cs.bal_per = v.per;
-            cs.bal_tiles = v.tiles;
+            if ((rc = scan_pass(key_src, lv_np, v.n, v.stride / lv_div, cnv, csv, T, v.S, v.len, v.cap))) return rc;
+            cs.nseg = kScanParts * v.S;
             cs.cap = v.cap;
             cs.thr_out = Tbuf[l & 1];
             cs.thr_rank = v.j;
@@ -1407,7 +1352,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         if ((rc = mark(2))) return rc;
         // main pass
         if (!blocked) {
-            if ((rc = scan_pass(f8 ? f8_p : bf_p, np_p, N, 1, cn, cs_p, T, sp.S, sp.len, sp.cap, sp.per))) return rc;
+            if ((rc = scan_pass(f8 ? f8_p : bf_p, np_p, N, 1, cn, cs_p, T, sp.S, sp.len, sp.cap))) return rc;
             if (tf_scan && !ts_side && (rc = ts.main_pass())) return rc;
         } else {
             // block by block on the worker streams (blocks scanned on the two workers overlap each
@@ -1418,7 +1363,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
                 KNN_CUDA(cudaStreamWaitEvent(w, oev(2 + nblk + b), 0));
                 KNN_CUDA(cudaStreamWaitEvent(w, oev(3 + 3 * nblk), 0));
                 const int sb = std::min(blk_splits, sp.S - b * blk_splits);
-                if ((rc = scan_pass(f8 ? f8_p : bf_p, np_p, N, 1, cn, cs_p, T, sb, sp.len, sp.cap, 0, b * blk_splits, w)))
+                if ((rc = scan_pass(f8 ? f8_p : bf_p, np_p, N, 1, cn, cs_p, T, sb, sp.len, sp.cap, b * blk_splits, w)))
                     return rc;
                 KNN_CUDA(cudaEventRecord(oev(2 + 2 * nblk + b), w));
             }
@@ -1436,9 +1381,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         }
         if ((rc = mark(3))) return rc;
         KNN_CUDA(cudaMemsetAsync(fail_cnt, 0, sizeof(uint32_t), s));
-        cs.nseg = kScanParts * (sp.per ? sp.ranges : sp.S);
-        cs.bal_per = sp.per;
-        cs.bal_tiles = sp.tiles;
+        cs.nseg = kScanParts * sp.S;
         cs.cap = sp.cap;
         cs.thr_out = nullptr;
         cs.thr_fallback = nullptr;

@@ -140,17 +140,7 @@ struct ScanArgs {
     int fp8;                   // keys from E4M3 operands with per-row scales
     int split0;                // first split of this launch (grid row y is split split0 + y)
     int accs;                  // TMEM accumulators: 2 (tiles of 224 / 192 rows) or 4 (tiles of 96)
-    // balanced mode (per_cta > 0, a 1-D grid): CTA c takes the (query tile, corpus tile) pairs
-    // [c per_cta, (c + 1) per_cta) in query-tile-major order (corpus tiles of the whole view);
-    // its candidates for query tile x go to segment range c - first(x), first(x) =
-    // x * tiles / per_cta (tiles = the view's tile count, at least 2)
-    int64_t per_cta;
 };
-// Segment ranges of query tile x in balanced mode: CTAs first(x) .. last(x).
-__host__ __device__ inline int scan_ranges_of(int64_t x, int64_t tiles, int64_t per_cta)
-{
-    return (int)(((x + 1) * tiles - 1) / per_cta - (x * tiles) / per_cta + 1);
-}
 // corpus rows per tile (MMA N): with 2 accumulators 224 for dpb <= 128, 192 for dpb <= 256;
 // with 4 accumulators 96
 int scan_tile_rows(int dpb, int accs);
@@ -161,7 +151,6 @@ int scan_part_cols(int dpb, int accs);
 size_t scan_smem_bytes(int dpb, int bps, int ring, bool fp8, int accs);
 // Ring geometry for dpb (want_bps = 0: automatic).  Returns 0 on success.
 int scan_plan(int dpb, int want_bps, int* bps, int* ring, bool fp8, int accs);
-// splits: grid rows (one per split) in the classic mode, CTAs in balanced mode
 cudaError_t launch_scan(const ScanArgs& a, int splits, cudaStream_t s);
 
 // Tensor-core 3xTF32 threshold scan (csrc/scan_tf32.cu): 128 queries x 128-row corpus
@@ -246,9 +235,6 @@ struct CandSelect {
     int64_t Q = 0;
     const uint32_t* skip_if = nullptr;       // the kernel does nothing when *skip_if != 0
     const uint32_t* skip_if_zero = nullptr;  // the kernel does nothing when *skip_if_zero == 0
-    // segments of a balanced scan (bal_per > 0): query q has kScanParts * scan_ranges_of(q / 128,
-    // bal_tiles, bal_per) of them (nseg is then their maximum)
-    int64_t bal_per = 0, bal_tiles = 0;
     float* thr_out = nullptr;
     int thr_rank = 0;
     const float* thr_fallback = nullptr;

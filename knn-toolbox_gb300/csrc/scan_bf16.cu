@@ -166,40 +166,18 @@ __global__ void __launch_bounds__(kScanThreads, 1)
     s.acce = s.accf + kMaxAcc;
     s.nfull = s.acce + kMaxAcc;
     s.nempty = s.nfull + kNormSlots;
-    s.aready = s.nempty + kNormSlots;  // two: generation k of the queries in TMEM on aready[k & 1]
-    s.drain = s.aready + 2;
+    s.aready = s.nempty + kNormSlots;
+    s.drain = s.aready + 1;
     uint32_t* words = reinterpret_cast<uint32_t*>(s.drain + 1);
     s.tmem_holder = words;
     s.abort = reinterpret_cast<volatile int*>(words + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    // The CTA's tiles t = 0 .. ntiles - 1, each a (query tile, corpus rows) pair.  Classic mode:
-    // query tile blockIdx.x against the split's rows.  Balanced mode: the pairs [g0, g0 + ntiles)
-    // of the query-tile-major order, so a CTA may move on to the next query tile (and its
-    // queries then replace the old ones in tensor memory) and its candidates go to one segment
-    // range per query tile.
-    const bool bal = a.per_cta > 0;
-    const int64_t vtiles = (a.N + TN - 1) / TN;  // corpus tiles of the view
+    const int64_t q0 = (int64_t)blockIdx.x * kTileQ;
     const int split = a.split0 + (int)blockIdx.y;
     const int64_t n_begin = (int64_t)split * a.split_len;
-    int ntiles;
-    int64_t g0 = 0;
-    if (bal) {
-        const int64_t total = (a.Q + kTileQ - 1) / kTileQ * vtiles;
-        g0 = (int64_t)blockIdx.x * a.per_cta;
-        ntiles = g0 < total ? (int)min(a.per_cta, total - g0) : 0;
-    } else {
-        const int64_t n_end = min(a.N, n_begin + a.split_len);
-        ntiles = n_end > n_begin ? (int)((n_end - n_begin + TN - 1) / TN) : 0;
-    }
-    auto qtile_of = [&](int t) -> int64_t { return bal ? (g0 + t) / vtiles : (int64_t)blockIdx.x; };
-    auto row_of = [&](int t) -> int64_t {
-        return bal ? ((g0 + t) % vtiles) * TN : n_begin + (int64_t)t * TN;
-    };
-    // segment range (first index of the segment group) of query tile x in this CTA
-    auto range_of = [&](int64_t x) -> int64_t {
-        return bal ? (int64_t)blockIdx.x - (x * vtiles) / a.per_cta : (int64_t)split;
-    };
+    const int64_t n_end = min(a.N, n_begin + a.split_len);
+    const int ntiles = n_end > n_begin ? (int)((n_end - n_begin + TN - 1) / TN) : 0;
 
     if (tid == 0) {
         for (int i = 0; i < R; ++i) {
@@ -214,8 +192,7 @@ __global__ void __launch_bounds__(kScanThreads, 1)
             ptx::mbar_init(&s.nfull[b], 1);
             ptx::mbar_init(&s.nempty[b], kEpiWarps);
         }
-        ptx::mbar_init(&s.aready[0], 4);
-        ptx::mbar_init(&s.aready[1], 4);
+        ptx::mbar_init(s.aready, 4);
         ptx::mbar_init(s.drain, kIssuers);
         *s.abort = 0;
         ptx::fence_mbar_init();
@@ -243,7 +220,7 @@ __global__ void __launch_bounds__(kScanThreads, 1)
             int it = 0;
             bool ok = true;
             for (int t = 0; t < ntiles && ok; ++t) {
-                const int64_t n0 = row_of(t);
+                const int64_t n0 = n_begin + (int64_t)t * TN;
                 for (int c = 0; c < slots_per_tile; ++c, ++it) {
                     const int st = it % R;
                     const uint32_t ph = (uint32_t)(it / R) & 1u;
@@ -283,26 +260,10 @@ __global__ void __launch_bounds__(kScanThreads, 1)
         // commit tracks only its own thread's MMAs
         if (lane == 0) {
             const int iss = warp == 1 ? 0 : 1;
-            bool ok = true;
+            bool ok = scan_wait(a, s, s.aready, 0, kDevTimeoutAload);
+            ptx::tc_fence_after();
             const uint32_t a_tmem = tmem + kACol;
-            // the queries in tensor memory: generation k (those of the CTA's k-th query tile)
-            // completes phase k >> 1 of aready[k & 1].  Each query tile has at least two corpus
-            // tiles, so an issuer's consecutive tiles are at most one generation apart; with
-            // generations alternating between two barriers no wait can alias: generation k - 2
-            // completed before k - 1 (which this issuer waited for, or k < 2), and k + 2 cannot
-            // complete before the epilogue has consumed this issuer's tile.
-            int64_t have_k = -1;
-            const int64_t x0 = qtile_of(0);
             for (int t = iss; t < ntiles && ok; t += kIssuers) {
-                const int64_t k = qtile_of(t) - x0;
-                if (k != have_k) {
-                    if (!scan_wait(a, s, &s.aready[k & 1], (uint32_t)((k >> 1) & 1), kDevTimeoutAload)) {
-                        ok = false;
-                        break;
-                    }
-                    ptx::tc_fence_after();
-                    have_k = k;
-                }
                 const int b = t % kNacc;
                 const uint32_t use = (uint32_t)(t / kNacc);
                 if (!scan_wait(a, s, &s.acce[b], (use & 1u) ^ 1u, kDevTimeoutMma)) { ok = false; break; }
@@ -351,60 +312,41 @@ __global__ void __launch_bounds__(kScanThreads, 1)
         const int quad = warp & 3;  // TMEM lane quarter this warp may access
         const int part = ew >> 2;   // one quarter of each tile's columns (see below)
         const int row = quad * 32 + lane;
+        const int64_t q = q0 + row;
+        const bool valid = q < a.Q;
         const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
-        // the query tile being served, this lane's query, threshold, scale factor and segment
-        const int64_t x0 = qtile_of(0);
-        int64_t x = x0, q = 0;
-        bool valid = false;
-        float T = 0.f, m = -2.0f;
-        uint64_t* out = nullptr;
-        size_t seg = 0;
+        if (part == 0) {
+            // A operand: this lane's query into TMEM (BF16 pairs or E4M3 quads per 32-bit column,
+            // lower K index in the low bits); BF16 keys take -2 q (exact: a power of two)
+            const uint32_t* qrow = reinterpret_cast<const uint32_t*>(a.qbf) + (valid ? q : 0) * (a.dpb / 2);
+            for (int bx = 0; bx < nbox; ++bx) {
+                float w[32];
+#pragma unroll
+                for (int u = 0; u < 32; ++u) {
+                    uint32_t x = valid ? __ldg(qrow + bx * 32 + u) : 0u;
+                    if (kNM) {
+                        __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162*>(&x);
+                        h = __hmul2(h, __float2bfloat162_rn(-2.f));
+                        x = *reinterpret_cast<const uint32_t*>(&h);
+                    }
+                    w[u] = __uint_as_float(x);
+                }
+                __syncwarp();
+                ptx::tmem_st32(tmem + lane_base + kACol + (uint32_t)(bx * 32), w);
+            }
+            ptx::tmem_wait_st();
+            ptx::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(s.aready);
+        }
+        // padding lanes of the last query tile collect nothing
+        const float T = valid ? (a.thr ? __ldg(a.thr + q) : __int_as_float(0x7f800000)) : -__int_as_float(0x7f800000);
+        const float m = kF8 ? -2.0f * (valid ? __ldg(a.qs + q) : 0.f) : -2.0f;
+        const size_t seg = (size_t)split * kScanParts + part;
+        uint64_t* out = a.cand + (seg * (size_t)a.Q + (size_t)(valid ? q : 0)) * (size_t)a.cap;
         uint32_t cnt = 0;
         const uint32_t cap = (uint32_t)a.cap;
-        auto enter = [&](int64_t xt) {
-            x = xt;
-            q = x * kTileQ + row;
-            valid = q < a.Q;
-            // padding lanes of the last query tile collect nothing
-            T = valid ? (a.thr ? __ldg(a.thr + q) : __int_as_float(0x7f800000)) : -__int_as_float(0x7f800000);
-            m = kF8 ? -2.0f * (valid ? __ldg(a.qs + q) : 0.f) : -2.0f;
-            seg = (size_t)range_of(x) * kScanParts + part;
-            out = a.cand + (seg * (size_t)a.Q + (size_t)(valid ? q : 0)) * (size_t)a.cap;
-            cnt = 0;
-            if (part == 0) {
-                // A operand: this lane's query into TMEM (BF16 pairs or E4M3 quads per 32-bit
-                // column, lower K index in the low bits); BF16 keys take -2 q (exact: a power of
-                // two).  Every MMA that read the previous queries has completed: this warp has
-                // waited for the accumulators of all earlier tiles.
-                const uint32_t* qrow = reinterpret_cast<const uint32_t*>(a.qbf) + (valid ? q : 0) * (a.dpb / 2);
-                for (int bx = 0; bx < nbox; ++bx) {
-                    float w[32];
-#pragma unroll
-                    for (int u = 0; u < 32; ++u) {
-                        uint32_t v = valid ? __ldg(qrow + bx * 32 + u) : 0u;
-                        if (kNM) {
-                            __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162*>(&v);
-                            h = __hmul2(h, __float2bfloat162_rn(-2.f));
-                            v = *reinterpret_cast<const uint32_t*>(&h);
-                        }
-                        w[u] = __uint_as_float(v);
-                    }
-                    __syncwarp();
-                    ptx::tmem_st32(tmem + lane_base + kACol + (uint32_t)(bx * 32), w);
-                }
-                ptx::tmem_wait_st();
-                ptx::tc_fence_before();
-                __syncwarp();
-                if (lane == 0) ptx::mbar_arrive(&s.aready[(x - x0) & 1]);
-            }
-        };
-        enter(x);
         for (int t = 0; t < ntiles; ++t) {
-            const int64_t xt = qtile_of(t);
-            if (xt != x) {  // warp-uniform: the CTA moves on to the next query tile
-                if (valid) a.cnt[seg * (size_t)a.Q + (size_t)q] = cnt;
-                enter(xt);
-            }
             const int b = t % kNacc;
             const uint32_t use = (uint32_t)(t / kNacc);
             const int ns = t % kNormSlots;
@@ -417,8 +359,7 @@ __global__ void __launch_bounds__(kScanThreads, 1)
             const float* nrm = s.norms + ns * TN;
             const float* scl = scales + ns * TN;
             const uint32_t tb = tmem + (uint32_t)b * TN + lane_base;
-            const int64_t tr = row_of(t);
-            const uint32_t nb = (uint32_t)tr;
+            const uint32_t nb = (uint32_t)(n_begin + (int64_t)t * TN);
             const int c1 = W1 * part, c2 = B2 + W2 * part, c3 = B3 + W3 * part;
             // all loads in flight together, one wait, then the accumulator is released:
             // the MMA may overwrite it while the keys are formed (in place) and tested
@@ -437,7 +378,7 @@ __global__ void __launch_bounds__(kScanThreads, 1)
             uint32_t ga, gb, gc = 0u;
             if constexpr (kNM) {
                 // the accumulator holds the keys; the view's last tile masks its rows past the view
-                const int64_t rem = a.N - tr;
+                const int64_t rem = a.N - (n_begin + (int64_t)t * TN);
                 if (rem < TN) {
                     chunk_mask<W1>(va, c1, (int)rem);
                     chunk_mask<W2>(vb, c2, (int)rem);
@@ -462,8 +403,7 @@ __global__ void __launch_bounds__(kScanThreads, 1)
                 if (lane == 0) ptx::mbar_arrive(&s.nempty[ns]);
             }
         }
-        // (a balanced CTA without tiles owns no segment)
-        if (valid && (ntiles > 0 || !bal)) a.cnt[seg * (size_t)a.Q + (size_t)q] = cnt;
+        if (valid) a.cnt[seg * (size_t)a.Q + (size_t)q] = cnt;
     }
 
     ptx::tc_fence_before();
@@ -552,13 +492,7 @@ cudaError_t launch_scan(const ScanArgs& a, int splits, cudaStream_t st)
     if (2 * (nbox / a.bps) > a.ring) return cudaErrorInvalidValue;
     if (a.Q <= 0) return cudaSuccess;
     const int64_t qt = (a.Q + kTileQ - 1) / kTileQ;
-    if (a.per_cta > 0) {
-        // balanced: every query tile has at least two corpus tiles (an issuer is then never more
-        // than one phase of the queries' barrier ahead), and the CTAs cover every pair
-        const int64_t vt = (a.N + tn - 1) / tn;
-        if (vt < 2 || a.split0 != 0 || (int64_t)splits * a.per_cta < qt * vt) return cudaErrorInvalidValue;
-    }
-    dim3 grid = a.per_cta > 0 ? dim3((unsigned)splits, 1) : dim3((unsigned)qt, (unsigned)splits);
+    dim3 grid((unsigned)qt, (unsigned)splits);
     if (tn == 96) return f8 ? launch_scan_t<96, 4, true>(a, grid, smem, st) : launch_scan_t<96, 4, false>(a, grid, smem, st);
     if (tn == 224)
         return f8 ? launch_scan_t<224, 2, true>(a, grid, smem, st) : launch_scan_t<224, 2, false>(a, grid, smem, st);

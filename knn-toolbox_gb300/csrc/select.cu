@@ -303,9 +303,6 @@ __global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandS
     const int64_t q = (int64_t)blockIdx.x * kSelWarps + warp;
     if (q >= c.Q) return;
 
-    // this query's segments: all of them, or in a balanced scan those of the CTAs that served its
-    // query tile
-    const int nseg = c.bal_per > 0 ? kScanParts * scan_ranges_of(q / kTileQ, c.bal_tiles, c.bal_per) : c.nseg;
     // segments s = lane + 32 r: their counts, all loaded at once
     constexpr int kSegPerLane = kScanMaxSegs / 32;
     uint32_t n4[kSegPerLane];
@@ -314,7 +311,7 @@ __global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandS
 #pragma unroll
     for (int r = 0; r < kSegPerLane; ++r) {
         const int s = lane + 32 * r;
-        const uint32_t n = s < nseg ? __ldg(c.cnt + (size_t)s * c.Q + q) : 0u;
+        const uint32_t n = s < c.nseg ? __ldg(c.cnt + (size_t)s * c.Q + q) : 0u;
         found += n;
         over |= n > (uint32_t)c.cap;
         n4[r] = min(n, (uint32_t)c.cap);
@@ -341,7 +338,7 @@ __global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandS
     uint32_t base = 0;
 #pragma unroll
     for (int r = 0; r < kSegPerLane; ++r) {
-        if (32 * r >= nseg) break;  // warp-uniform: no segments left
+        if (32 * r >= c.nseg) break;  // warp-uniform: no segments left
         uint32_t pre = n4[r];
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
