@@ -426,7 +426,7 @@ def run_gb300(args, w):
                 d_, i_ = SH.sharded_search(c, r0, q, k, stream=stream, check=False, timing=timing, precision=p,
                                            shortlist=shortlist, scan=scan_mode, scan_boxes=args.scan_boxes,
                                            tf32_only=tf32_only, scan_accs=args.scan_accs,
-                                           single_stream=single_stream)
+                                           single_stream=single_stream, splits=args.splits)
                 dist_out.copy_(d_)
                 idx_out.copy_(i_)
             return step
@@ -434,7 +434,8 @@ def run_gb300(args, w):
         def step(timing):
             cuknns.search(c, q, k, dist=dist_out, idx=idx_out, stream=stream, check=False, timing=timing,
                           precision=p, shortlist=shortlist, scan=scan_mode, scan_boxes=args.scan_boxes,
-                          tf32_only=tf32_only, scan_accs=args.scan_accs, single_stream=single_stream)
+                          tf32_only=tf32_only, scan_accs=args.scan_accs, single_stream=single_stream,
+                          splits=args.splits)
         return step
 
     # ---- headline: the requested form, inputs resident in HBM
@@ -723,6 +724,7 @@ def main():
                          "profiler captures)")
     ap.add_argument("--scan-accs", type=int, default=0, choices=[0, 2, 4],
                     help="threshold scan: tensor-memory accumulators (0 = auto)")
+    ap.add_argument("--splits", type=int, default=0, help="corpus splits of the main scan (0 = auto)")
     ap.add_argument("--rate", type=float, default=4000.0, help="serving: offered requests per second")
     ap.add_argument("--requests", type=int, default=4000, help="serving: requests in the timed run")
     ap.add_argument("--recall-queries", type=int, default=0,
