@@ -285,9 +285,14 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_kernel(const __grid_constan
 // (high and low parts, 2 x 16 KB per slot) and each MMA reads one operand from shared memory:
 // with both operands there, the MMA reads and the TMA fills together exceed the shared-memory
 // bandwidth.  Tensor memory: A hi [0, dp), A lo [dp, 2 dp), two 128-column accumulators at
-// 256 and 384.  One MMA issuer (warp 1): a 3xTF32 tile is long enough that two accumulators
-// cover the epilogue's round trip.  Keys, epilogue and segments are those of tscan_kernel, so
-// the candidates are the same.
+// 256 and 384.  MMA issuers: warp 1 for every tile, or, when a tile's chunks fill at most
+// half the ring (rows of up to 96 columns), warps 1 and 18 for the even and odd tiles, one
+// accumulator each: the tensor pipe queues little work beyond the MMA being issued, so one
+// thread's barrier waits and commits idle it.  Two issuers are safe there: tiles t - 1 and t
+// use different slots, and an issuer waits for tile t's accumulator before its slots, after
+// which the epilogue has consumed tile t - 2 (so every earlier fill of those slots has
+// landed, and no slot wait can alias an older phase).  Keys, epilogue and segments are those
+// of tscan_kernel, so the candidates are the same.
 constexpr int kAccTA = 2;
 constexpr uint32_t kAccColTA = 256;
 constexpr uint32_t kSlotTA = 2u * kBox;  // corpus hi, corpus lo
@@ -364,6 +369,7 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_ta_kernel(const __grid_cons
     const int64_t n_end = min(a.N, n_begin + a.split_len);
     const int ntiles = n_end > n_begin ? (int)((n_end - n_begin + kTN - 1) / kTN) : 0;
     const int nch = a.dp / 32;
+    const int niss = 2 * nch <= R ? 2 : 1;  // MMA issuers (see above)
 
     if (tid == 0) {
         for (int i = 0; i < R; ++i) {
@@ -379,7 +385,7 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_ta_kernel(const __grid_cons
             ptx::mbar_init(&s.nempty[b], kEpi);
         }
         ptx::mbar_init(s.aready, 4);
-        ptx::mbar_init(s.drain, 1);
+        ptx::mbar_init(s.drain, niss);
         *s.abort = 0;
         *s.alo = 0;
         ptx::fence_mbar_init();
@@ -429,19 +435,21 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_ta_kernel(const __grid_cons
                 for (int j = first; j < it; ++j) ptx::mbar_wait(&s.full[j % R], (uint32_t)(j / R) & 1u, kTimeout);
             }
         }
-    } else if (warp == 1) {
-        // ------------------------------------------------------------ MMA issuer
+    } else if (warp == 1 || (warp == 2 + kEpi && niss == 2)) {
+        // ------------------------------------------------------------ MMA issuers
+        // issuer i takes the tiles t = i (mod niss); each commit tracks only its own MMAs
         if (lane == 0) {
+            const int iss = warp == 1 ? 0 : 1;
             bool ok = ta_wait(a, s, s.aready, 0, kDevTimeoutAload);
             ptx::tc_fence_after();
             const uint32_t alo = *s.alo;
-            int it = 0;
-            for (int t = 0; t < ntiles && ok; ++t) {
+            for (int t = iss; t < ntiles && ok; t += niss) {
                 const int b = t % kAccTA;
                 const uint32_t use = (uint32_t)(t / kAccTA);
                 if (!ta_wait(a, s, &s.acce[b], (use & 1u) ^ 1u, kDevTimeoutMma)) { ok = false; break; }
                 ptx::tc_fence_after();
                 const uint32_t d_tmem = tmem + kAccColTA + (uint32_t)b * kTN;
+                int it = t * nch;
                 for (int c = 0; c < nch; ++c, ++it) {
                     const int st = it % R;
                     const uint32_t ph = (uint32_t)(it / R) & 1u;

@@ -151,3 +151,18 @@ def test_small_corpus_fp32_and_integer_data_on_the_tf32_scan(engine, oracle):
     od, oi = oracle.knn_gemm(Xi, Qi, 24, kp=st["kp"], rerank=True)
     np.testing.assert_array_equal(i, oi)
     np.testing.assert_array_equal(d, od)
+
+
+@pytest.mark.parametrize("D,Q,k", [(96, 300, 16), (32, 257, 10), (64, 130, 40)])
+def test_two_issuer_tiles_integer_data_bit_exact(engine, oracle, D, Q, k):
+    # rows of up to 96 columns: the queries sit in tensor memory and two MMA issuers alternate the
+    # corpus tiles; integer data keep every TF32 product and sum exact, so the answers are the
+    # oracle's bit for bit (many tiles per CTA, a ragged last query tile)
+    rng = np.random.default_rng(D + Q)
+    X = rng.integers(0, 256, (120_000, D)).astype(np.float32)
+    Qs = rng.integers(0, 256, (Q, D)).astype(np.float32)
+    d, i, st = run(engine, X, Qs, k, scan=engine.SCAN_TF32)
+    assert st["scan_keys"] == 2
+    od, oi = oracle.knn_gemm(X, Qs, k, kp=st["kp"], rerank=True)
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_array_equal(d, od)
