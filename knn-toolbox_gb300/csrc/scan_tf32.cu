@@ -285,14 +285,18 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_kernel(const __grid_constan
 // (high and low parts, 2 x 16 KB per slot) and each MMA reads one operand from shared memory:
 // with both operands there, the MMA reads and the TMA fills together exceed the shared-memory
 // bandwidth.  Tensor memory: A hi [0, dp), A lo [dp, 2 dp), two 128-column accumulators at
-// 256 and 384.  MMA issuers: warp 1 for every tile, or, when a tile's chunks fill at most
-// half the ring (rows of up to 96 columns), warps 1 and 18 for the even and odd tiles, one
+// 256 and 384.  Two MMA issuers, warps 1 and 18, take the even and the odd tiles, one
 // accumulator each: the tensor pipe queues little work beyond the MMA being issued, so one
-// thread's barrier waits and commits idle it.  Two issuers are safe there: tiles t - 1 and t
-// use different slots, and an issuer waits for tile t's accumulator before its slots, after
-// which the epilogue has consumed tile t - 2 (so every earlier fill of those slots has
-// landed, and no slot wait can alias an older phase).  Keys, epilogue and segments are those
-// of tscan_kernel, so the candidates are the same.
+// thread's barrier waits and commits idle it.  A slot wait must not read an older phase of
+// the slot's barrier as complete.  An issuer waits for tile t's accumulator before its slots,
+// after which the epilogue has consumed tile t - 2: every use of the ring up to tile t - 2
+// has landed and been released.  With at most as many chunks per tile as ring slots (4 and
+// 6), a slot's use two rounds back lies in tile t - 2 or earlier, so it is released.  If the
+// slot's previous use was one of this issuer's own, it waited for that fill; if it was the
+// other issuer's, the issuer first waits for that use's release (which follows its fill) and
+// only then for the slot's next fill.  The release wait costs nothing: the producer waits for
+// it before refilling the slot.  Keys, epilogue and segments are those of tscan_kernel, so
+// the candidates are the same.
 constexpr int kAccTA = 2;
 constexpr uint32_t kAccColTA = 256;
 constexpr uint32_t kSlotTA = 2u * kBox;  // corpus hi, corpus lo
@@ -369,7 +373,7 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_ta_kernel(const __grid_cons
     const int64_t n_end = min(a.N, n_begin + a.split_len);
     const int ntiles = n_end > n_begin ? (int)((n_end - n_begin + kTN - 1) / kTN) : 0;
     const int nch = a.dp / 32;
-    const int niss = 2 * nch <= R ? 2 : 1;  // MMA issuers (see above)
+    const int niss = nch <= R ? 2 : 1;  // MMA issuers (see above; the launcher keeps nch <= R)
 
     if (tid == 0) {
         for (int i = 0; i < R; ++i) {
@@ -453,6 +457,13 @@ __global__ void __launch_bounds__(kThreads, 1) tscan_ta_kernel(const __grid_cons
                 for (int c = 0; c < nch; ++c, ++it) {
                     const int st = it % R;
                     const uint32_t ph = (uint32_t)(it / R) & 1u;
+                    // the slot's previous use in the other issuer's tile: its release first
+                    const int prev = it - R;
+                    if (niss == 2 && prev >= 0 && (prev / nch) % 2 != iss &&
+                        !ta_wait(a, s, &s.empty[st], ph ^ 1u, kDevTimeoutMma)) {
+                        ok = false;
+                        break;
+                    }
                     if (!ta_wait(a, s, &s.full[st], ph, kDevTimeoutMma)) { ok = false; break; }
                     ptx::tc_fence_after();
                     const uint32_t clo = s.slot_lo[st];

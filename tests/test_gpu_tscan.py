@@ -153,11 +153,12 @@ def test_small_corpus_fp32_and_integer_data_on_the_tf32_scan(engine, oracle):
     np.testing.assert_array_equal(d, od)
 
 
-@pytest.mark.parametrize("D,Q,k", [(96, 300, 16), (32, 257, 10), (64, 130, 40)])
+@pytest.mark.parametrize("D,Q,k", [(96, 300, 16), (32, 257, 10), (64, 130, 40), (128, 300, 16), (100, 200, 20)])
 def test_two_issuer_tiles_integer_data_bit_exact(engine, oracle, D, Q, k):
-    # rows of up to 96 columns: the queries sit in tensor memory and two MMA issuers alternate the
-    # corpus tiles; integer data keep every TF32 product and sum exact, so the answers are the
-    # oracle's bit for bit (many tiles per CTA, a ragged last query tile)
+    # rows of up to 128 columns: the queries sit in tensor memory and two MMA issuers alternate
+    # the corpus tiles (sharing ring slots at 128 columns); integer data keep every TF32 product
+    # and sum exact, so the answers are the oracle's bit for bit (many tiles per CTA, a ragged
+    # last query tile)
     rng = np.random.default_rng(D + Q)
     X = rng.integers(0, 256, (120_000, D)).astype(np.float32)
     Qs = rng.integers(0, 256, (Q, D)).astype(np.float32)
