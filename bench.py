@@ -48,6 +48,10 @@ WORKLOADS = {
     "mix4m": dict(desc="Gaussian mixture corpus 4,000,000 x 96 (1,024 centres N(0,1), sigma 0.15, rows "
                        "L2-normalised), 10,000 queries, k=10, seed 2",
                   gen="gauss_mixture", N=4_000_000, D=96, Q=10_000, k=10, seed=2),
+    # profiling-sized cut of mix4m for ncu captures of the 3xTF32 scan (corpus still larger than L2)
+    "mix1m": dict(desc="Gaussian mixture corpus 1,000,000 x 96 (1,024 centres N(0,1), sigma 0.15, rows "
+                       "L2-normalised), 2,500 queries, k=10, seed 2",
+                  gen="gauss_mixture", N=1_000_000, D=96, Q=2_500, k=10, seed=2),
     # serving form: resident corpus, Poisson arrivals of requests of uneven size and k
     "serve2m": dict(desc="serving: int-descriptor corpus 2,000,000 x 128 resident (FP32 + BF16 + TF32 copies), "
                          "Poisson arrivals, request sizes log-uniform on [1,512], k in {1,10,100}, seed 1",
@@ -103,7 +107,8 @@ def measured_peaks():
 NCU_TRAFFIC = {
     ("scan_kernel", "int1m"): 389.8e6,
     ("scan_kernel", "aniso8m"): 2537.0e6,
-    ("tscan_kernel", "uniform64k"): 70.0e6,
+    ("tscan_kernel", "uniform64k"): 69.9e6,
+    ("tscan_kernel", "mix4m"): 3405.0e6,
 }
 
 
