@@ -356,6 +356,11 @@ constexpr int64_t kSeedStride = 32;
 // against 0.37 ms on the 1M x 128 integer workload, and on the 4M x 96 mixture (BF16 keys) a
 // main pass of 7.7 against 6.8 ms with 0.85 against 0.03 ms of fix-up.
 constexpr int64_t kSeedRatio = 16;
+// Rows of the coarsest sample, whose keys are all kept: at most what the threshold selection ranks
+// in registers (32 lanes x 8 keys).  With 1,024 the 4M-row corpora kept 489 keys per query there:
+// that level and its selection took 82 + 82 us on the 4M x 96 mixture (seeding 1.27 ms, 1.19 with
+// one more level of 31 rows; 8M x 256: 1.64 against 1.36 ms).
+constexpr int64_t kSeedCoarsest = 256;
 
 static int64_t seed_stride(int kp)
 {
@@ -436,14 +441,15 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
         pc = scan_part_cols(dpb, P->accs);  // segment columns per tile
     }
     const int64_t qt = cdiv(Q, kTileQ);  // query tiles
-    // levels, finest first: strides s, kSeedRatio s, ... until the sample fits the selector whole
+    // levels, finest first: strides s, kSeedRatio s, ... until the sample is small enough to keep
+    // every key (kSeedCoarsest rows)
     P->stride0 = seed_stride(kp);
     int64_t st[kMaxSeedLevels];
     int L = 0;
     for (int64_t stride = P->stride0;; stride *= kSeedRatio) {
         if (L == kMaxSeedLevels) return set_error(KNNS_ERR_UNSUPPORTED, "threshold scan: corpus too large to seed");
         st[L++] = stride;
-        if (cdiv(N, stride) <= kCandMax / 2) break;
+        if (cdiv(N, stride) <= kSeedCoarsest) break;
     }
     P->levels = L;
     // level index 0 = coarsest
