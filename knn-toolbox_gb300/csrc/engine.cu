@@ -1031,10 +1031,10 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
     if (!capture) KNN_CUDA(cudaStreamWaitEvent(s, E.last_done, 0));
     // ordering events: [0] start, [1] sample landed, [2 + b] block b landed, [2 + nblk + b]
     // block b prepared, [2 + 2 nblk + b] block b scanned, [2 + 3 nblk] flag words cleared,
-    // [3 + 3 nblk] thresholds seeded
+    // [3 + 3 nblk] thresholds seeded, [4 + 3 nblk] the TF32 scan done
     auto oev = [&](int i) -> cudaEvent_t { return E.order_event(i); };
     if (host_corpus != nullptr || blocked) {
-        if (!oev(4 + 3 * nblk) || !E.copy_stream() || (blocked && (!E.prep_stream() || !E.worker_stream(0) ||
+        if (!oev(5 + 3 * nblk) || !E.copy_stream() || (blocked && (!E.prep_stream() || !E.worker_stream(0) ||
                                                                    !E.worker_stream(Engine::kScanWorkers - 1))))
             return set_error(KNNS_ERR_CUDA, "stream or event creation failed");
     }
@@ -1373,16 +1373,23 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
                     return rc;
                 KNN_CUDA(cudaEventRecord(oev(2 + 2 * nblk + b), w));
             }
+            // What needs the whole corpus, the TF32 copies and the TF32 scan (gated on the data's
+            // BF16-exactness in the exact form), runs on the preparation stream: the copies (their own
+            // buffers) once the last block is prepared, the flag then final; the scan, which writes
+            // the thresholds and candidate segments the BF16 path also uses, once every block is
+            // scanned (a block scanned before a later block cleared the flag ran its BF16 scan), beside
+            // the BF16 selection and fix-up on the search's stream: one of the two paths returns at once.
             for (int b = 0; b < nblk; ++b) KNN_CUDA(cudaStreamWaitEvent(s, oev(2 + 2 * nblk + b), 0));
-            // what needs the whole corpus: the TF32 copies and the TF32 scan (gated on the data's
-            // BF16-exactness in the exact form)
             if (tf_scan) {
+                cudaStream_t ps = E.prep_stream();
                 KNN_CUDA(launch_split(corpus, N, ldc, D, c.dp, (float*)E.hi.p, (float*)E.lo.p, flags, any_lo,
-                                      not_exact, s));
+                                      not_exact, ps));
                 ++launches;
+                ts.s = ps;
                 if ((rc = ts.split_queries())) return rc;
-                if ((rc = ts.seed())) return rc;
-                if ((rc = ts.main_pass())) return rc;
+                for (int b = 0; b < nblk; ++b) KNN_CUDA(cudaStreamWaitEvent(ps, oev(2 + 2 * nblk + b), 0));
+                if ((rc = ts.seed()) || (rc = ts.main_pass()) || (rc = ts.select()) || (rc = ts.fix())) return rc;
+                KNN_CUDA(cudaEventRecord(oev(4 + 3 * nblk), ps));
             }
         }
         if ((rc = mark(3))) return rc;
@@ -1411,7 +1418,7 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         cs.fail_cnt = fail_cnt;
         KNN_CUDA(launch_select_cand(cs, s));
         ++launches;
-        if (tf_scan && !ts_side && (rc = ts.select())) return rc;
+        if (tf_scan && !ts_side && !blocked && (rc = ts.select())) return rc;
         if ((rc = mark(4))) return rc;
         // fix-up: failed queries, compacted, through the shortlist kernel without a threshold
         // (launches whose rows are all past the failure count return at once)
@@ -1468,8 +1475,9 @@ int run_search(Engine& E, const float* corpus, int64_t N, int64_t ldc, const flo
         };
         if ((rc = fix_pass(0, sp.fixA_rows, sp.fixA_S, sp.fixA_len))) return rc;
         if ((rc = fix_pass(sp.fixA_rows, sp.fixB_rows, sp.fixB_S, sp.fixB_len))) return rc;
-        if (tf_scan && !ts_side && (rc = ts.fix())) return rc;
+        if (tf_scan && !ts_side && !blocked && (rc = ts.fix())) return rc;
         if (ts_side) KNN_CUDA(cudaStreamWaitEvent(s, E.order_event(1), 0));
+        if (tf_scan && blocked) KNN_CUDA(cudaStreamWaitEvent(s, oev(4 + 3 * nblk), 0));
         if ((rc = mark(5))) return rc;
     }
     launches += ts.launches;
