@@ -78,7 +78,9 @@ __device__ __forceinline__ void chunk_mask(float (&key)[W], int c0, int rem)
 
 // Append the keys below T of the flagged groups, in increasing corpus index.
 // Words hold the raw key bits above the index; the selection maps them to
-// ordered keys.
+// ordered keys.  A lane whose group holds a single key below T (the usual case
+// where a warp appends at all) stores the group's minimum at the key's position
+// found from the mask of hits; more hits take the column walk.
 template <int W>
 __device__ __forceinline__ void chunk_append(const float (&key)[W], uint32_t gm, float T, uint32_t base,
                                              uint64_t* out, uint32_t cap, uint32_t& cnt)
@@ -87,13 +89,25 @@ __device__ __forceinline__ void chunk_append(const float (&key)[W], uint32_t gm,
 #pragma unroll
     for (int g = 0; g < W / G; ++g) {
         if ((gm >> g) & 1u) {
+            const float* kg = key + G * g;
+            uint32_t hm = 0;
 #pragma unroll
-            for (int j = 0; j < G; ++j) {
-                const float k = key[G * g + j];
-                const bool h = k < T;
-                if (h && cnt < cap)
-                    out[cnt] = ((uint64_t)__float_as_uint(k) << 32) | (uint64_t)(base + (uint32_t)(G * g + j));
-                cnt += h ? 1u : 0u;
+            for (int j = 0; j < G; ++j) hm |= (kg[j] < T ? 1u : 0u) << j;
+            if ((hm & (hm - 1u)) == 0u) {
+                const float k = G == 8 ? min8(kg) : fminf(ptx::fmin3(kg[0], kg[1], kg[2]), kg[G - 1]);
+                if (cnt < cap)
+                    out[cnt] = ((uint64_t)__float_as_uint(k) << 32) |
+                               (uint64_t)(base + (uint32_t)(G * g + __ffs((int)hm) - 1));
+                ++cnt;
+            } else {
+#pragma unroll
+                for (int j = 0; j < G; ++j) {
+                    const float k = kg[j];
+                    const bool h = k < T;
+                    if (h && cnt < cap)
+                        out[cnt] = ((uint64_t)__float_as_uint(k) << 32) | (uint64_t)(base + (uint32_t)(G * g + j));
+                    cnt += h ? 1u : 0u;
+                }
             }
         }
     }
