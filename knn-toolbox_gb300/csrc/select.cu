@@ -393,10 +393,22 @@ __global__ void __launch_bounds__(kSelWarps * 32) select_cand_kernel(const CandS
     const int P = pow2_at_least(kp);
     uint64_t W = kSentinel;
     if (n > kp) {
-        // the kp-th smallest key K (16 rounds over the key half); when the words with keys
-        // up to K fit the sort, all of them are kept and the sort orders K's ties by index
-        uint32_t xk = 0;
-        for (int b0 = 30; b0 >= 0; b0 -= 2) {
+        // the kp-th smallest key K (2-bit digits of the key half); when the words with keys
+        // up to K fit the sort, all of them are kept and the sort orders K's ties by index.
+        // K lies between the smallest and the largest key, so it shares the bits above the
+        // highest one in which they differ: the search starts at that bit's digit.
+        uint32_t kmin = 0xFFFFFFFFu, kmax = 0u;
+        for (int e = lane; e < n; e += 32) {
+            const uint32_t v = (uint32_t)(buf[e] >> 32);
+            kmin = min(kmin, v);
+            kmax = max(kmax, v);
+        }
+        kmin = __reduce_min_sync(0xffffffffu, kmin);
+        kmax = __reduce_max_sync(0xffffffffu, kmax);
+        const uint32_t diff = kmin ^ kmax;
+        const int top = diff ? (31 - __clz(diff)) & ~1 : -2;  // first digit to search
+        uint32_t xk = top >= 30 ? 0u : top < 0 ? kmin : (kmin >> (top + 2)) << (top + 2);
+        for (int b0 = top; b0 >= 0; b0 -= 2) {
             const uint32_t low = (1u << b0) - 1u;
             const uint32_t d = radix4_digit(buf, n, xk | low, xk | (1u << b0) | low, xk | (2u << b0) | low,
                                             (uint32_t)kp, [](uint64_t v) { return (uint32_t)(v >> 32); });
