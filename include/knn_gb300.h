@@ -310,6 +310,26 @@ int knns_debug_tc_dot_tile(const float *corpus, int64_t N, const float *queries,
 int knns_debug_prep(const float *x, int64_t n, int64_t ld, int D, float *norms, void *bf16, void *f8,
                     float *scales, uint32_t *words, void *norm_parts);
 
+/* The threshold scan's plan for an exact-form search (default options), computed on the host
+ * alone (no GPU is touched): the seeding levels, coarsest first, and the main pass.  tf32 = 1
+ * gives the 3xTF32 scan's plan, 0 the BF16 scan's; sms is the GPU's SM count. */
+#define KNNS_MAX_SEED_LEVELS 6
+typedef struct knns_scan_plan_info {
+    int kp;                                      /* shortlist length */
+    int tile_rows;                               /* corpus rows per tile (MMA N) */
+    int levels;
+    int64_t level_rows[KNNS_MAX_SEED_LEVELS];    /* sample rows (every level_stride-th corpus row) */
+    int64_t level_stride[KNNS_MAX_SEED_LEVELS];
+    int level_rank[KNNS_MAX_SEED_LEVELS];        /* rank of the level's threshold among its keys */
+    int level_splits[KNNS_MAX_SEED_LEVELS];
+    int level_cap[KNNS_MAX_SEED_LEVELS];         /* candidate slots per (query, segment) */
+    int splits;                                  /* main pass */
+    int64_t split_len;
+    int cap;
+    int sel_words;                               /* bound on one query's stored main-pass candidates */
+} knns_scan_plan_info;
+int knns_debug_scan_plan(int64_t N, int64_t Q, int D, int k, int sms, int tf32, knns_scan_plan_info *out);
+
 #ifdef __cplusplus
 }
 #endif

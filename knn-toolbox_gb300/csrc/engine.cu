@@ -2036,6 +2036,39 @@ int knns_debug_prep(const float* x, int64_t n, int64_t ld, int D, float* norms, 
     return KNNS_OK;
 }
 
+int knns_debug_scan_plan(int64_t N, int64_t Q, int D, int k, int sms, int tf32, knns_scan_plan_info* out)
+{
+    clear_error();
+    static_assert(KNNS_MAX_SEED_LEVELS == kMaxSeedLevels, "seeding levels of the plan record");
+    if (!out || N < 1 || Q < 1 || D < 1 || k < 1 || k > 512 || sms < 1) return set_error(KNNS_ERR_INVALID, "bad args");
+    // the planner reads only the SM count of the engine: a host-only engine stands in for the GPU's
+    Engine E;
+    E.sms = sms;
+    knns_options o;
+    knns_default_options(&o);
+    int kp = auto_kp(k, 1);
+    if (kp > 512) kp = std::max(round16(k), 32);  // no margin at the limit (as resolve_config)
+    ScanPlan P;
+    const int rc = plan_scan(E, N, Q, (D + 63) & ~63, kp, o, &P, false, tf32 != 0);
+    if (rc) return rc;
+    memset(out, 0, sizeof(*out));
+    out->kp = kp;
+    out->tile_rows = tf32 ? 128 : scan_tile_rows((D + 63) & ~63, P.accs);
+    out->levels = P.levels;
+    for (int l = 0; l < P.levels; ++l) {
+        out->level_rows[l] = P.lv[l].n;
+        out->level_stride[l] = P.lv[l].stride;
+        out->level_rank[l] = P.lv[l].j;
+        out->level_splits[l] = P.lv[l].S;
+        out->level_cap[l] = P.lv[l].cap;
+    }
+    out->splits = P.S;
+    out->split_len = P.len;
+    out->cap = P.cap;
+    out->sel_words = P.sel_words;
+    return KNNS_OK;
+}
+
 int knns_debug_tc_dot_tile(const float* corpus, int64_t N, const float* queries, int64_t Q, int D, float* dump)
 {
     clear_error();

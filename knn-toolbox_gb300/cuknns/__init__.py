@@ -36,7 +36,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_UNSUPPORTED, ERR_DEVICE_TIMEOUT, ERR_NOMEM = rang
 EXPORTED = ["knns_default_options", "knns_search_device", "knns_search_host", "knns_check_device", "knns_merge_topk",
             "knns_last_error", "knns_last_stats", "knns_last_fixups", "knns_version", "knns_debug_tc_dot_tile",
             "knns_debug_stall_next_search",
-            "knns_debug_prep",
+            "knns_debug_prep", "knns_debug_scan_plan",
             "knns_timing_collect", "knns_timing_collect5", "knns_search_device_noalloc", "knns_noalloc_prepare",
             "knns_index_create", "knns_index_search", "knns_index_destroy", "knns_autotune_shortlist",
             "knns_server_default_config", "knns_server_create", "knns_server_submit", "knns_server_wait",
@@ -63,6 +63,14 @@ class Stats(ctypes.Structure):
                 ("stages", ctypes.c_int), ("launches", ctypes.c_int), ("pilot", ctypes.c_int),
                 ("workspace_bytes", ctypes.c_int64), ("scan", ctypes.c_int), ("scan_splits", ctypes.c_int),
                 ("scan_cap", ctypes.c_int), ("scan_ring", ctypes.c_int), ("scan_keys", ctypes.c_int)]
+
+
+class ScanPlanInfo(ctypes.Structure):
+    _fields_ = [("kp", ctypes.c_int), ("tile_rows", ctypes.c_int), ("levels", ctypes.c_int),
+                ("level_rows", ctypes.c_int64 * 6), ("level_stride", ctypes.c_int64 * 6),
+                ("level_rank", ctypes.c_int * 6), ("level_splits", ctypes.c_int * 6), ("level_cap", ctypes.c_int * 6),
+                ("splits", ctypes.c_int), ("split_len", ctypes.c_int64), ("cap", ctypes.c_int),
+                ("sel_words", ctypes.c_int)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -109,6 +117,7 @@ def lib():
     L.knns_debug_tc_dot_tile.argtypes = [vp, i64, vp, i64, ci, vp]
     L.knns_debug_stall_next_search.argtypes = [i64]
     L.knns_debug_prep.argtypes = [vp, i64, i64, ci, vp, vp, vp, vp, vp, vp]
+    L.knns_debug_scan_plan.argtypes = [i64, i64, ci, ci, ci, ci, ctypes.POINTER(ScanPlanInfo)]
     L.knns_timing_collect.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
     L.knns_timing_collect5.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
     L.knns_search_device_noalloc.argtypes = [vp, i64, i64, vp, i64, i64, ci, ci, vp, vp, vp]
@@ -265,6 +274,19 @@ def search_host(corpus, queries, k, *, algo=ALGO_AUTO, splits=0, rerank=True, kp
     _check(lib().knns_search_host(corpus.ctypes.data, N, queries.ctypes.data, Q, D, k, dist.ctypes.data,
                                   idx.ctypes.data, ctypes.byref(o)))
     return dist, idx
+
+
+def scan_plan(N, Q, D, k, sms=152, tf32=False) -> dict:
+    """The threshold scan's plan for an exact-form search, computed on the host (no GPU): seeding
+    levels coarsest first (rows, stride, rank, splits, cap) and the main pass."""
+    p = ScanPlanInfo()
+    _check(lib().knns_debug_scan_plan(N, Q, D, k, sms, int(bool(tf32)), ctypes.byref(p)))
+    L = p.levels
+    return {"kp": p.kp, "tile_rows": p.tile_rows, "levels": L,
+            "level_rows": list(p.level_rows[:L]), "level_stride": list(p.level_stride[:L]),
+            "level_rank": list(p.level_rank[:L]), "level_splits": list(p.level_splits[:L]),
+            "level_cap": list(p.level_cap[:L]), "splits": p.splits, "split_len": p.split_len, "cap": p.cap,
+            "sel_words": p.sel_words}
 
 
 def debug_prep(x, norm_parts=False):
