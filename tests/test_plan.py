@@ -67,3 +67,6 @@ def test_plan_rejects_bad_arguments(cuknns):
         cuknns.scan_plan(1000, 10, 128, 513)
     with pytest.raises(cuknns.KnnsError):
         cuknns.scan_plan(0, 10, 128, 10)
+    # a successful call clears the library's last error (other tests read it)
+    cuknns.scan_plan(1000, 10, 128, 10)
+    assert cuknns.last_error() == ""
