@@ -344,13 +344,16 @@ int resolve_config(const Engine& E, int64_t N, int64_t Q, int D, int k, const kn
 // selection and searched again without a threshold, so results never depend
 // on the seeds.
 constexpr int kMaxSeedLevels = 6;
-// Finest sampling stride: a coarser sample makes seeding cheaper and the main
-// pass collect more candidates (about 2 kp + 4 sqrt(kp * stride) per query);
-// 32 gave the lowest seeding + scan + selection time on the 1M x 128 and the
-// 4M x 96 workloads (16 and 64 were each slower on one of them).  Long
-// shortlists take a finer stride, so that a query's main-pass candidates
-// (mean + six standard deviations) still fit the selection's buffer.
+// Finest sampling stride: a coarser sample makes seeding cheaper (its cost grows with N / stride)
+// and the main pass and its selection handle more candidates (about 2 kp + 4 sqrt(kp * stride)
+// per query, whatever N).  Per search: 1M x 128, 2.429 ms with 32 against 2.447 with 64; 4M x 96
+// (BF16 keys) 7.32 against 7.31; 8M x 256 (E4M3 keys) 32.4 against 31.7 (seeding 1.34 against
+// 0.80 ms).  So 64 from 6M corpus rows on.  Long shortlists take a finer stride,
+// so that a query's main-pass candidates (mean + six standard deviations) still fit the
+// selection's buffer.
 constexpr int64_t kSeedStride = 32;
+constexpr int64_t kSeedStrideWide = 64;
+constexpr int64_t kSeedStrideWideRows = 6000000;
 // Stride ratio of neighbouring levels.  32 would leave two levels for a million rows where 16
 // needs three, but its coarser thresholds cost more than the level they save: seeding 0.46
 // against 0.37 ms on the 1M x 128 integer workload, and on the 4M x 96 mixture (BF16 keys) a
@@ -362,9 +365,9 @@ constexpr int64_t kSeedRatio = 16;
 // one more level of 31 rows; 8M x 256: 1.64 against 1.36 ms).
 constexpr int64_t kSeedCoarsest = 256;
 
-static int64_t seed_stride(int kp)
+static int64_t seed_stride(int kp, int64_t N)
 {
-    int64_t s = kSeedStride;
+    int64_t s = N >= kSeedStrideWideRows ? kSeedStrideWide : kSeedStride;
     while (s > 4) {
         const double mean = 2.0 * kp + 4.0 * std::sqrt((double)kp * s), spread = 6.0 * std::sqrt(2.0 * kp * s);
         if (mean + spread + 64.0 <= (double)kCandMax) break;
@@ -443,7 +446,7 @@ static int plan_scan(const Engine& E, int64_t N, int64_t Q, int dpb, int kp, con
     const int64_t qt = cdiv(Q, kTileQ);  // query tiles
     // levels, finest first: strides s, kSeedRatio s, ... until the sample is small enough to keep
     // every key (kSeedCoarsest rows)
-    P->stride0 = seed_stride(kp);
+    P->stride0 = seed_stride(kp, N);
     int64_t st[kMaxSeedLevels];
     int L = 0;
     for (int64_t stride = P->stride0;; stride *= kSeedRatio) {

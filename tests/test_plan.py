@@ -42,8 +42,9 @@ def test_plan_invariants(cuknns, N, Q, D, k, tf32):
     kp, L = p["kp"], p["levels"]
     assert kp >= k and kp % 16 == 0
     strides, rows = p["level_stride"], p["level_rows"]
-    # nested samples: the finest stride 32 (finer for long shortlists), x16 per coarser level
-    assert strides[-1] in (4, 8, 16, 32)
+    # nested samples: the finest stride 32 (64 from 6M rows; finer for long shortlists), x16 per
+    # coarser level
+    assert strides[-1] in ((4, 8, 16, 32, 64) if N >= 6_000_000 else (4, 8, 16, 32))
     for lv in range(L - 1):
         assert strides[lv] == 16 * strides[lv + 1]
     for lv in range(L):
@@ -60,6 +61,12 @@ def test_plan_invariants(cuknns, N, Q, D, k, tf32):
     assert sl % tn == 0 and 1 <= S <= 128
     assert S * sl >= N > (S - 1) * sl
     assert p["cap"] >= 1 and kp <= p["sel_words"] <= 2048
+
+
+def test_finest_stride_by_corpus_size(cuknns):
+    # seeding cost grows with N / stride, the main pass's extra candidates do not: 64 from 6M rows
+    assert cuknns.scan_plan(4_000_000, 10_000, 96, 10)["level_stride"][-1] == 32
+    assert cuknns.scan_plan(8_000_000, 16_384, 256, 32)["level_stride"][-1] == 64
 
 
 def test_plan_rejects_bad_arguments(cuknns):
